@@ -1,0 +1,284 @@
+/*
+ * recview_gb300.h -- C ABI of the GB300-native convolution back-projection library.
+ *
+ * Two groups of entry points:
+ *
+ *  1. The drop-in set.  These are exactly the symbols RecView's document/queue code binds from
+ *     the CUDA back-end (source/cudaReconst.h:16-28,42-59 and source/cudaReconstDummy.cpp), with
+ *     the same RECONST_INFO layout (source/reconstinfo.h:21-101), the same argument meaning, the
+ *     same void-return + ri->iStatus error convention and the same numeric error codes.
+ *     A RecView build links this library in place of cudaReconst.cu/cudaReconstHost.cpp.
+ *
+ *  2. New entry points (prefix Rv) that have no counterpart in the reference: the fused
+ *     raw-frame stack path (normalise -> filter -> back-project for many slices in one call),
+ *     the filter-table helper, geometry/error utilities and the reduced-storage modes.
+ *
+ * All signatures use plain pointers and sizes; no torch or CUDA C++ types cross the boundary.
+ * Device pointers are typed void* / plain element pointers and streams are passed as void*.
+ */
+#ifndef RECVIEW_GB300_H_
+#define RECVIEW_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- constants shared with the reference (values must stay identical) ------------------- */
+/* source/constants.h:39-53 */
+#define RV_LOG_SCALE 3000
+#define RV_BACKPROJ_SCALE 100
+#define RV_DBPT_GINTP 16
+#define RV_SINOGRAM_PIXEL_MIN8bit 3
+#define RV_SINOGRAM_PIXEL_MIN16bit 20
+#define RV_ZOOMING_NONE 2
+#define RECONST_INFO_IDLE 0
+#define RECONST_INFO_BUSY 1
+#define RECONST_INFO_ERROR 2
+/* source/DlgQueue.h:19-26 */
+#define RV_RQFLAGS_ZERNIKE 2
+#define RV_RQFLAGS_DRIFTLIST 4
+#define RV_RQFLAGS_DRIFTPARAMS 8
+#define RV_RQFLAGS_USEONLYEVENFRAMES 16
+#define RV_RQFLAGS_USEONLYODDFRAMES 32
+#define RV_RQFLAGS_SINOGRAMKEPT 128
+/* source/StdAfx.h:28-31 */
+#define RV_BINC_WHITE 0
+#define RV_BINC_SAMPLE 1
+#define RV_BINC_NOUSE 2
+#define RV_BINC_SKIP 4
+/* source/general.h:35-36 (ri->iFlag bit) */
+#define RV_READTIF8bit 2
+/* source/DlgReconOpt.h:4-8; RV_FILT_SHEPP is this library's addition (the reference has no
+ * Shepp-Logan window; any kind >= 5 gives an all-ones table there). */
+#define RV_FILT_HAN 0
+#define RV_FILT_HAM 1
+#define RV_FILT_RAMP 2
+#define RV_FILT_PARZN 3
+#define RV_FILT_BUTER 4
+#define RV_FILT_SHEPP 5
+/* source/cudaReconst.h:8-13 */
+#define CUDA_ERROR_DEVICEINFO_MASK 0x0000ffff
+#define CUDA_ERROR_INSUFFICIENT_DRIVER 0x00010000
+#define CUDA_ERROR_INSUFFICIENT_COMPUTE_CAPABILITY 0x00020000
+#define CUDA_ERROR_VIRTUAL_DEVICE_DETECTED 0x00040000
+#define CUDA_ERROR_DEVICE_GETPROPERTY 0x00080000
+#define CUDA_ERROR_DEVICE_GETCOUNT 0x00100000
+
+/* Error codes logged by the reference host code (source/cudaReconstHost.cpp:666-811), kept. */
+#define RV_ERR_DEVICE_OOM 28801     /* device allocation failed */
+#define RV_ERR_HOST_ALLOC 28802     /* host allocation failed */
+#define RV_ERR_PINNED_ALLOC 28803   /* pinned host allocation failed */
+#define RV_ERR_COPY_H2D 28804
+#define RV_ERR_COPY_D2H 28805
+#define RV_ERR_MEMSET 28806
+#define RV_ERR_STREAM 28807
+/* Codes added by this library (no reference counterpart). */
+#define RV_ERR_BAD_ARGUMENT 28850   /* NULL pointer / inconsistent RECONST_INFO field */
+#define RV_ERR_UNSUPPORTED 28851    /* size beyond a documented limit, unimplemented option */
+#define RV_ERR_LAUNCH 28852         /* kernel launch / execution error */
+#define RV_ERR_SET_DEVICE 28853     /* cudaSetDevice failed */
+#define RV_ERR_KERNEL_STATUS 28854  /* a kernel reported a bounded-wait timeout or bad index */
+#define RV_ERR_ABORTED 28855        /* the progress callback asked to stop */
+
+/* ---- RECONST_INFO: byte-for-byte layout of source/reconstinfo.h:21-101 (x64) ------------- */
+typedef struct RvFloat2 { float x, y; } RvFloat2;
+
+typedef struct RECONST_INFO {
+    unsigned char iStatus;
+    int ixdim;
+    int iInterpolation;
+    double center;
+    int iSinoCenter;
+    int iLenSinogr;
+    int* iReconst;
+    int iStartSino;
+    int iStepSino;
+    unsigned int* pDoc;
+    int* nSinogr;
+    char dataName[61];
+    char* bInc;
+    float* fdeg;
+    float* fexp;
+    int iMultiplex;
+    int iOffset;
+    int maxSinogrLen;
+    short** iSinogr;
+    float* fFilter;
+    unsigned int dReconFlags;
+    float fTiltAngle;
+    int drStart;
+    int drEnd;
+    double drX;
+    double drY;
+    int drOmit;               /* BOOL */
+    unsigned int threadID;
+    uintptr_t hThread;
+    unsigned int max_d_ifp;
+    unsigned int max_d_igp;
+    int* d_ifp;
+    int* d_igp;
+    float* d_filt;
+    unsigned int max_d_filt;
+    short* d_strip;
+    unsigned int max_d_strip;
+    RvFloat2* d_p;            /* this library keeps its per-RECONST_INFO context here */
+    unsigned int max_d_p;     /* == RV_CTX_TAG while d_p holds a context */
+    float* d_px;
+    unsigned int max_d_px;
+    int fftplan;              /* cufftHandle */
+    unsigned int ifftdim;
+    void* stream1;            /* cudaStream_t */
+    void* stream2;
+    unsigned long long i64result;
+    unsigned long long i64sum;
+    short** ppRef;
+    short** ppQry;
+    unsigned int uiMaxRef;
+    unsigned int uiMaxQry;
+    void* pcxyz1;             /* CXyz* */
+    void* pcxyz2;
+    int iLsqBin;
+    int iLsqBxref;
+    int* piDrift;
+    int iFlag;
+} RECONST_INFO;
+
+#define RV_CTX_TAG 0x52564742u  /* 'RVGB' */
+
+/* ==== 1. Drop-in entry points (source/cudaReconst.h) ====================================== */
+
+/* Filtered back-projection of one slice (replaces source/cudaReconstHost.cpp:629-813).
+ * Reads ri->iSinogr rows i*iMultiplex+iOffset for views i = iStartSino, iStartSino+iStepSino, ...
+ * that are SAMPLE frames, filters them with ri->fFilter, back-projects them and OVERWRITES
+ * ri->iReconst[ixdimp*ixdimp] (int32, row-major iy*ixdimp+ix).  Increments *ri->nSinogr per
+ * used view.  RQFLAGS_SINOGRAMKEPT + cached buffers reuse the previous call's filtered views
+ * with an integer centre shift (source/cudaReconstHost.cpp:658,775).  The arithmetic follows
+ * the reference CPU routine (source/general.cpp:2020-2163) bit-for-bit.  On failure sets
+ * ri->iStatus = RECONST_INFO_ERROR and reports a code through RvSetErrorCallback.
+ * bEnStream selects the two cached streams ri->stream1/2 (created on first use). */
+void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool bEnStream);
+/* Same computation (source/cudaReconstHost.cpp:220-291 used cuFFT; this library always uses its
+ * own on-device FFT, so both entry points share one implementation). */
+void CudaReconstHostFFT(RECONST_INFO* ri, int idev, bool bReport);
+/* Frees the device buffers cached in ri (source/cudaReconstHost.cpp:142-203). */
+void CudaReconstMemFree(RECONST_INFO* ri);
+/* Destroys ri->stream1/2 and frees buffers; bCudaDeviceReset additionally synchronises and
+ * resets the device (source/cudaReconstHost.cpp:205-214).  The reset ends only this process's
+ * context. */
+void CudaReconstResourceFree(RECONST_INFO* ri, bool bCudaDeviceReset);
+/* Flat/dark log normalisation of the raw uint16 rows in ri->iSinogr, in place, with the
+ * semantics of the reference CPU routine GenerateSinogramThread (source/general.cpp:2377-2532),
+ * which the reference uses instead of its own CUDA variant (source/cudaReconstHost.cpp:815-901).
+ * Frames i with i % iStepSino == iStartSino are processed; ri->maxSinogrLen = frame count. */
+void CudaSinogramHost(RECONST_INFO* ri, int idev, bool bReport);
+
+/* Device queries (source/cudaReconst.cu:449-538). */
+int GetCudaDeviceCount(int iMinComputeCapability);
+int GetCudaMaxThreadsPerBlock(int iDevice);
+int GetCudaWarpSize(int iDevice);
+int GetCudaDeviceName(int iDevice, char* pcName, int iszcName);
+int GetCudaDeviceComputingCapability(int iDevice, int* piMajor, int* piMinor);
+int GetCudaNumberOfCores(int iDevice, int* piCores, int* piProcessors);
+int GetCudaClockRate(int iDevice, int* piClockRate, int* piMemRate);
+
+/* Pinned host buffers (source/cudaReconstHost.cpp:216-218).  Return a cudaError_t value. */
+int CUDA_MALLOC_HOST_INT(int** ptr, size_t size);
+int CUDA_FREE_HOST(void* ptr);
+
+/* 3-D stitching (least squares) is outside this library's scope: these stubs keep the symbol
+ * set of source/cudaReconstDummy.cpp:27-39, do nothing and report RV_ERR_UNSUPPORTED. */
+void CudaLsqfitMemAlloc(short** d_ppRefPixel, short** d_ppQryPixel, int* pMaxRefPixel,
+                        int* pMaxQryPixel, short** ppRefPixel, short** ppQryPixel, int nRefFiles,
+                        int nQryFiles, int ixref, unsigned long long** d_result);
+void CudaLsqfitMemFree(short** d_ppRefPixel, short** d_ppQryPixel, int nRefFiles, int nQryFiles,
+                       unsigned long long* d_result);
+void CudaLsqfitHost(short* d_ref, short* d_qry, int ixref, int iyref, int ixqry, int iyqry, int ix,
+                    int iy, unsigned long long* ilsq, unsigned long long* nlsq,
+                    unsigned long long* d_result, unsigned long long* h_result);
+
+/* The progress/abort callback the reference host calls every 20 views
+ * (source/general.cpp:2352-2375).  A RecView build defines it; this library calls it when
+ * bReport is set, through a weak reference, or through the hook set by
+ * RvSetProgressCallback when the application does not define the symbol. */
+bool DBProjDlgCtrl(RECONST_INFO* ri, int iProgStep, int iSino, int* pCurrStep);
+
+/* ==== 2. Entry points added by this library =============================================== */
+
+/* Error reporting: the reference logs codes through its CError object; this library calls
+ * the registered callback (may be NULL) and also keeps the last code per calling thread. */
+typedef void (*RvErrorCallback)(int code, const char* message);
+void RvSetErrorCallback(RvErrorCallback cb);
+int RvGetLastError(void);                 /* last code on this thread, 0 if none */
+const char* RvGetLastErrorMessage(void);  /* message for the last code on this thread */
+void RvClearLastError(void);
+typedef bool (*RvProgressCallback)(RECONST_INFO* ri, int iProgStep, int iSino, int* pCurrStep);
+void RvSetProgressCallback(RvProgressCallback cb);
+
+/* Filter table in the reference layout (mirrors CGazoDoc::SetFilter, source/gazoDoc.cpp:
+ * 3747-3812): one-sided float[ndim]; kinds RV_FILT_*.  Returns 0 or RV_ERR_BAD_ARGUMENT. */
+int RvSetFilter(int kind, double cutoff, double order, int ndim, float* out);
+
+/* Derived sizes for a detector width and iInterpolation code (source/general.cpp:2022-2028). */
+typedef struct RvDims {
+    int ixdim, iZooming, iIntpDim, ndimp, ndim, ixdimp, ixdimh, ihoffset;
+} RvDims;
+int RvGetDims(int ixdim, int iInterpolation, RvDims* out);
+
+/* ---- fused stack path: raw uint16 frames -> normalised -> filtered -> slices -------------- */
+/* Reconstruction modes. */
+#define RV_MODE_REF 0   /* reference semantics: 1/16 sub-sample int table, int32 slices (bit-exact) */
+#define RV_MODE_LIN 1   /* linear interpolation, FP32 filtered rows, FP32 slices */
+#define RV_MODE_LIN_F16 2  /* as LIN, filtered rows stored as FP16 with a per-row scale */
+#define RV_MODE_LIN_BF16 3 /* as LIN, filtered rows stored as BF16 with a per-row scale */
+
+/* One stack = the frames of a RecView dataset for nslices detector rows, stored like the
+ * reference's sinogram buffer: raw[(frame*nslices + slice)*ixdim + x], frames 0..nframes-1 are
+ * the flat (WHITE) and SAMPLE frames in acquisition order, frame nframes is the dark. */
+typedef struct RvStackDesc {
+    int ixdim;              /* detector width (after trim/binning, as ri->ixdim) */
+    int iInterpolation;     /* 2 = none; 3/4/5 = x2/x4/x8 zoom (source/gazoDoc.cpp:1864-1870) */
+    double center;          /* rotation centre in ri->center convention */
+    int nframes;            /* frames excluding the dark */
+    int nslices;            /* detector rows per frame (ri->iMultiplex) */
+    const char* bInc;       /* [nframes] RV_BINC_* flags (host) */
+    const float* fdeg;      /* [nframes] angles in degrees (host) */
+    const float* fexp;      /* [nframes] acquisition times used to interpolate flats (host) */
+    float fTiltAngle;
+    const float* fFilter;   /* [ndim] filter table in the reference layout (host) */
+    unsigned int dReconFlags;  /* RV_RQFLAGS_USEONLY{EVEN,ODD}FRAMES honoured */
+    int iFlag;              /* RV_READTIF8bit selects the 8-bit sample threshold */
+    int mode;               /* RV_MODE_* */
+    int input_is_sinogram;  /* 1: raw already holds log-normalised int16 rows (skip R1) */
+} RvStackDesc;
+
+typedef struct RvStack RvStack;
+/* Validates the description, builds per-view geometry and allocates device buffers. */
+int RvStackCreate(const RvStackDesc* desc, RvStack** out);
+void RvStackDestroy(RvStack* st);
+/* Bytes of one output slice (ixdimp^2 * 4) and of the raw input ((nframes+1)*nslices*ixdim*2). */
+size_t RvStackSliceBytes(const RvStack* st);
+size_t RvStackInputBytes(const RvStack* st);
+int RvStackNumViews(const RvStack* st);    /* SAMPLE views that are back-projected */
+int RvStackOutputDim(const RvStack* st);   /* ixdimp */
+/* Device-resident run: d_raw and d_out are device pointers, stream a cudaStream_t (or NULL for
+ * the legacy default stream).  Output: nslices slices of ixdimp^2 int32 (REF) or float (LIN*). */
+int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, void* stream);
+/* Host-buffer run: copies h_raw in, runs, copies the slices to h_out, synchronises.  Host
+ * buffers may be pageable or pinned (pinned is faster). */
+int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void* stream);
+/* Per-stage device timings (ms) of the last RvStackRunDevice/RunHost call, measured with CUDA
+ * events on the launching stream: [0] filter stage, [1] back-projection, [2] whole call. */
+int RvStackLastTimings(const RvStack* st, float* ms3);
+/* Number of kernels launched by the last run. */
+int RvStackLastLaunchCount(const RvStack* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RECVIEW_GB300_H_ */

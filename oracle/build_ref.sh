@@ -1,0 +1,58 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/librvref.so from RecView's own sources, unmodified, where they lie.
+#
+# TEST INFRASTRUCTURE ONLY: the library is the parity pin for the oracle restatement
+# (oracle/rv_oracle.c) and is used by tests and fixture generation in the container that has
+# the reference checkout.  Nothing is copied into the repository: whole files are compiled by
+# path, and the three function bodies below are spliced between small wrapper heads/tails
+# (oracle/ref_wrap) through a pipe straight into the compiler.  Outputs go to oracle/_ref only.
+#
+#   source/cfft.cpp, source/ccmplx.cpp             compiled by path
+#   source/general.cpp:2020-2163                  CPU back-projection body (scalar loop)
+#   source/general.cpp:2377-2532                  GenerateSinogramThread
+#   source/gazoDoc.cpp:3748-3812                  body of CGazoDoc::SetFilter
+#   oracle/ref_wrap/libm_pin.cpp                  correctly rounded cosf/sinf for the twiddles
+#
+# The extracted ranges are checked against SHA-256 sums so a different checkout fails loudly
+# instead of silently compiling the wrong lines.
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+SRC="${RECVIEW_REFERENCE:-/root/reference}/source"
+OUT="$HERE/_ref"
+if [ ! -d "$SRC" ]; then
+    echo "build_ref: reference sources not found at $SRC; skipping" >&2
+    exit 3
+fi
+mkdir -p "$OUT/obj" "$OUT/gen"
+# source/cfft.cpp:530 includes <sys\timeb.h> with a Windows path separator; on Linux that is a
+# file name containing a backslash, generated here (outside the repository's tracked files).
+printf '#include <afx.h>\n' > "$OUT/gen/sys\\timeb.h"
+
+check() {  # file first last sha256
+    local got
+    got="$(sed -n "$2,$3p" "$SRC/$1" | sha256sum | cut -d' ' -f1)"
+    if [ "$got" != "$4" ]; then
+        echo "build_ref: $1:$2-$3 differs from the audited checkout ($got)" >&2
+        exit 4
+    fi
+}
+check general.cpp 2020 2163 0363b3ff22cd95c6b3c1aa74a56ec5eb8c6fd5e225459306ffdbaa97adf2ff28
+check general.cpp 2377 2532 2f41a4c98ee29e23f3a3dc7d8e5ddc1289e70dd46e097b141a26bd4c4a033981
+check gazoDoc.cpp 3748 3812 74de08b2b13fbf43c047b1fdca2bff6aae955307240a1aed58a8024175e90a3d
+
+CXX="${CXX:-g++}"
+# -ffp-contract=off: the reference's x64 build rounds every float operation separately.
+FLAGS=(-O2 -ffp-contract=off -fPIC -w -fpermissive -I"$HERE/ref_shim" -I"$OUT/gen" -I"$SRC")
+
+cd "$OUT/obj"   # empty directory: quote includes of the piped units resolve via -I only
+"$CXX" "${FLAGS[@]}" -c "$SRC/cfft.cpp" -o cfft.o
+"$CXX" "${FLAGS[@]}" -c "$SRC/ccmplx.cpp" -o ccmplx.o
+{ cat "$HERE/ref_wrap/fbp_head.inc"; sed -n 2020,2163p "$SRC/general.cpp"; cat "$HERE/ref_wrap/fbp_tail.inc"; } \
+    | "$CXX" "${FLAGS[@]}" -x c++ -c - -o fbp.o
+{ cat "$HERE/ref_wrap/sino_head.inc"; sed -n 2377,2532p "$SRC/general.cpp"; cat "$HERE/ref_wrap/sino_tail.inc"; } \
+    | "$CXX" "${FLAGS[@]}" -x c++ -c - -o sino.o
+{ cat "$HERE/ref_wrap/filter_head.inc"; sed -n 3748,3812p "$SRC/gazoDoc.cpp"; cat "$HERE/ref_wrap/filter_tail.inc"; } \
+    | "$CXX" "${FLAGS[@]}" -x c++ -c - -o filter.o
+"$CXX" "${FLAGS[@]}" -fno-builtin -c "$HERE/ref_wrap/libm_pin.cpp" -o libm_pin.o
+"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o libm_pin.o -lm
+echo "build_ref: $OUT/librvref.so"

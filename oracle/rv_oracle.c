@@ -1,0 +1,656 @@
+/*
+ * rv_oracle.c -- CPU restatement of RecView's convolution back-projection path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the timed CPU baseline.
+ * Nothing in the product links this file.  Build with -ffp-contract=off (gcc otherwise fuses
+ * a*b+c into an FMA on aarch64 and changes the bits the reference produces).
+ *
+ * Every function follows one piece of the reference (file:line in its comment) in the same
+ * floating-point operation order.  Parity pins: oracle/_ref (the reference sources compiled
+ * unmodified by oracle/build_ref.sh) and the golden vectors in tests/golden.
+ */
+#include "rv_oracle.h"
+
+#include <limits.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* source/constants.h:3-5 (double literals of the reference, kept to the digit) */
+#define RVO_DEG_TO_RAD 0.0174532925199
+#define RVO_PI 3.1415926535897
+#define RVO_PI2 6.283185307178
+
+/* ---------------------------------------------------------------- R3: sizes / geometry ---- */
+void rvo_dims(int ixdim, int iInterpolation, RvDims* d) {
+    /* source/general.cpp:2021-2035 */
+    d->ixdim = ixdim;
+    d->iZooming = (iInterpolation > RV_ZOOMING_NONE) ? (iInterpolation - RV_ZOOMING_NONE) : 0;
+    d->iIntpDim = (int)pow(2.0, d->iZooming);
+    d->ndimp = (int)(log((double)ixdim) / 0.69314718055994530941723212145818) + 1 + d->iZooming;
+    d->ndim = (int)pow(2.0, d->ndimp);
+    d->ixdimp = ixdim * d->iIntpDim;
+    d->ixdimh = d->ixdimp / 2;
+    d->ihoffset = d->ndim / 2 - 1 - d->ixdimh;
+}
+
+float rvo_fcenter(const RvDims* d, double center) {
+    /* source/general.cpp:2036-2037: float arithmetic, (int)center truncates the double. */
+    const int ic = (int)center;
+    if (d->iIntpDim == 1) {
+        float a = (float)d->ixdimh + (float)center;
+        a = a - (float)ic;
+        return a * (float)RV_DBPT_GINTP;
+    }
+    float fr = (float)center - (float)ic;
+    fr = fr * (float)d->iIntpDim;
+    fr = (float)d->ixdimh + fr;
+    return fr * (float)RV_DBPT_GINTP;
+}
+
+void rvo_view_geometry(const RvDims* d, double center, float fdeg, float tilt, float* fcos,
+                       float* fsin, float* foffset) {
+    /* source/general.cpp:2139-2142: th from a float sum, cos/sin in double, float results. */
+    const float deg = fdeg + tilt;
+    const double th = (double)deg * RVO_DEG_TO_RAD;
+    const float c = (float)(cos(th) * RV_DBPT_GINTP);
+    const float s = (float)(-sin(th) * RV_DBPT_GINTP);
+    const float sum = c + s;
+    const float prod = (float)d->ixdimh * sum;
+    *fcos = c;
+    *fsin = s;
+    *foffset = rvo_fcenter(d, center) - prod;
+}
+
+/* ---------------------------------------------------------------- R4: filter table ------- */
+int rvo_set_filter(int kind, double cutoff, double order_d, int ndim, float* F) {
+    /* source/gazoDoc.cpp:3762-3811 */
+    if (!F || ndim <= 0) return RV_ERR_BAD_ARGUMENT;
+    const int ndimh = (int)(ndim * cutoff);
+    const float order = (float)order_d;
+    const float revndim = 1.f / (float)ndim;
+    int i;
+    switch (kind) {
+    case RV_FILT_HAN:
+        for (i = 0; i < ndimh; i++) {
+            const float frac = (float)i / (float)ndimh;
+            const float w = (float)(1 + cos(RVO_PI * (double)frac));
+            F[i] = ((0.5f * revndim) * (float)i) * w;
+        }
+        for (i = ndimh; i < ndim; i++) F[i] = 0;
+        break;
+    case RV_FILT_HAM:
+        for (i = 0; i < ndimh; i++) {
+            const float frac = (float)i / (float)ndimh;
+            const float w = (float)(0.54 + 0.46 * cos(RVO_PI * (double)frac));
+            F[i] = (revndim * (float)i) * w;
+        }
+        for (i = ndimh; i < ndim; i++) F[i] = 0;
+        break;
+    case RV_FILT_RAMP:
+        for (i = 0; i < ndimh; i++) F[i] = revndim * (float)i;
+        for (i = ndimh; i < ndim; i++) F[i] = 0;
+        break;
+    case RV_FILT_PARZN:
+        for (i = 0; i < ndimh / 2; i++) {
+            const float frac = (float)i / (float)ndimh;
+            float t = 6.0f * frac;
+            t = t * frac;
+            t = t * (1.0f - frac);
+            F[i] = (revndim * (float)i) * (1.0f - t);
+        }
+        for (i = ndimh / 2; i < ndimh; i++) {
+            const float frac = (float)i / (float)ndimh;
+            const float om = 1.0f - frac;
+            float v = (revndim * (float)i) * 2.0f;
+            v = v * om;
+            v = v * om;
+            F[i] = v * om;
+        }
+        for (i = ndimh; i < ndim; i++) F[i] = 0;
+        break;
+    case RV_FILT_BUTER:
+        /* the reference calls pow(float, float) and sqrt(float): the C++ float overloads */
+        for (i = 0; i < ndim; i++) {
+            const float frac = (float)i / (float)ndimh;
+            const float den = sqrtf(1.0f + powf(frac, order));
+            F[i] = (revndim * (float)i) / den;
+        }
+        break;
+    case RV_FILT_SHEPP:
+        /* Project-defined: Shepp-Logan window sinc(pi f / 2) in the same one-sided layout. */
+        for (i = 0; i < ndimh; i++) {
+            const float frac = (float)i / (float)ndimh;
+            const double x = RVO_PI * (double)frac * 0.5;
+            const float w = (i == 0) ? 1.0f : (float)(sin(x) / x);
+            F[i] = (revndim * (float)i) * w;
+        }
+        for (i = ndimh; i < ndim; i++) F[i] = 0;
+        break;
+    default:
+        for (i = 0; i < ndim; i++) F[i] = 1;
+        break;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------- R6: FFT ---------------- */
+void rvo_fft_twiddles(int np, float* wr, float* wi) {
+    /* source/cfft.cpp:374-410 with min0 < 0: p0 = -(float)2pi, a = p0 * (i/n) in float, then
+     * the float overloads cos(float)/sin(float).  Their value is taken correctly rounded (the
+     * double result rounded to float), independent of the platform's cosf/sinf; the reference
+     * build pins the same values (oracle/ref_wrap/libm_pin.cpp). */
+    const int n = 1 << np;
+    float p0 = (float)RVO_PI2;
+    p0 = p0 * -1.0f;
+    for (int i = 0; i < n / 2; i++) {
+        const float a = p0 * ((float)i / (float)n);
+        wr[i] = (float)cos((double)a);
+        wi[i] = (float)sin((double)a);
+    }
+}
+
+/* One radix-2 Stockham pass (the inner stages of source/cfft.cpp:224-244 and :300-336):
+ *   y[2*m*al + q]      = x[m*al + q] + x[m*al + q + n/2] * w[q*bt]
+ *   y[2*m*al + q + al] = x[m*al + q] - x[m*al + q + n/2] * w[q*bt]
+ * with the complex product evaluated as (xr*wr - xi*wi, xr*wi + xi*wr), each op rounded. */
+static void rvo_pass(int n, int al, const float* wr, const float* wi, const float* xr,
+                     const float* xi, float* yr, float* yi) {
+    const int half = n / 2, bt = half / al;
+    for (int m = 0; m < bt; m++) {
+        for (int q = 0; q < al; q++) {
+            const int a = m * al + q, b = a + half, t = q * bt, o = 2 * m * al + q;
+            const float p1 = xr[b] * wr[t], p2 = xi[b] * wi[t];
+            const float p3 = xr[b] * wi[t], p4 = xi[b] * wr[t];
+            const float sr = p1 - p2, si = p3 + p4;
+            yr[o] = xr[a] + sr;
+            yi[o] = xi[a] + si;
+            yr[o + al] = xr[a] - sr;
+            yi[o + al] = xi[a] - si;
+        }
+    }
+}
+
+void rvo_fft_forward(int np, const float* wr, const float* wi, float* re, float* im,
+                     float* work) {
+    const int n = 1 << np, half = n / 2;
+    float *ar = work, *ai = work + n, *br = work + 2 * n, *bi = work + 3 * n;
+    /* first pass reads the input back to front (source/cfft.cpp:197-209) */
+    for (int j = 0; j < half; j++) {
+        const int u = half - 1 - j, v = n - 1 - j;
+        ar[2 * j] = re[u] + re[v];
+        ai[2 * j] = im[u] + im[v];
+        ar[2 * j + 1] = re[u] - re[v];
+        ai[2 * j + 1] = im[u] - im[v];
+    }
+    int al = 2;
+    for (int l = 1; l < np - 1; l++) {
+        rvo_pass(n, al, wr, wi, ar, ai, br, bi);
+        float* t;
+        t = ar; ar = br; br = t;
+        t = ai; ai = bi; bi = t;
+        al *= 2;
+    }
+    /* last pass writes front to back reversed (source/cfft.cpp:246-265) */
+    re[0] = ar[0] + ar[half];
+    im[0] = ai[0] + ai[half];
+    re[half] = ar[0] - ar[half];
+    im[half] = ai[0] - ai[half];
+    for (int k = 1; k < half; k++) {
+        const float p1 = ar[half + k] * wr[k], p2 = ai[half + k] * wi[k];
+        const float p3 = ar[half + k] * wi[k], p4 = ai[half + k] * wr[k];
+        const float sr = p1 - p2, si = p3 + p4;
+        re[n - k] = ar[k] + sr;
+        im[n - k] = ai[k] + si;
+        re[half - k] = ar[k] - sr;
+        im[half - k] = ai[k] - si;
+    }
+}
+
+void rvo_fft_inverse(int np, const float* wr, const float* wi, float* re, float* im,
+                     float* work) {
+    const int n = 1 << np, half = n / 2;
+    float *ar = work, *ai = work + n, *br = work + 2 * n, *bi = work + 3 * n;
+    /* source/cfft.cpp:283-295 */
+    for (int j = 0; j < half; j++) {
+        ar[2 * j] = re[j] + re[j + half];
+        ai[2 * j] = im[j] + im[j + half];
+        ar[2 * j + 1] = re[j] - re[j + half];
+        ai[2 * j + 1] = im[j] - im[j + half];
+    }
+    int al = 2;
+    for (int l = 1; l < np - 1; l++) {
+        rvo_pass(n, al, wr, wi, ar, ai, br, bi);
+        float* t;
+        t = ar; ar = br; br = t;
+        t = ai; ai = bi; bi = t;
+        al *= 2;
+    }
+    /* last pass with min < 0 swaps the two halves (source/cfft.cpp:355-368) */
+    for (int k = 0; k < half; k++) {
+        const float p1 = ar[half + k] * wr[k], p2 = ai[half + k] * wi[k];
+        const float p3 = ar[half + k] * wi[k], p4 = ai[half + k] * wr[k];
+        const float sr = p1 - p2, si = p3 + p4;
+        br[k] = ar[k] - sr;
+        bi[k] = ai[k] - si;
+        br[k + half] = ar[k] + sr;
+        bi[k + half] = ai[k] + si;
+    }
+    /* CFft::FFT1 epilogue (source/cfft.cpp:418-425): reverse and scale by 1/n (exact). */
+    const float a = 1.f / (float)n;
+    for (int i = 0; i < n; i++) {
+        re[i] = br[n - 1 - i] * a;
+        im[i] = bi[n - 1 - i] * a;
+    }
+}
+
+/* ---------------------------------------------------------------- R5 / R7 --------------- */
+void rvo_place_row(const RvDims* d, double center, const short* strip, float* re, float* im) {
+    /* source/general.cpp:2105-2126 */
+    const int ndim = d->ndim, z = d->iIntpDim, ixdim = d->ixdim, ic = (int)center;
+    memset(re, 0, sizeof(float) * ndim);
+    memset(im, 0, sizeof(float) * ndim);
+    const int idx0 = (0 - ic) * z + (ndim / 2 - 1);
+    const int idx1 = (ixdim - 1 - ic) * z + (ndim / 2 - 1) + 1;
+    for (int m = 0; m < idx0; m++) re[m] = strip[0];
+    for (int m = idx1; m < ndim; m++) re[m] = strip[ixdim - 1];
+    for (int k = 0; k < ixdim; k++) {
+        const int idx = (k - ic) * z + (ndim / 2 - 1);
+        if (idx < 0) continue;
+        if (idx >= ndim) break;
+        re[idx] = strip[k];
+        if (k == ixdim - 1) break;
+        for (int j = 1; j < z; j++) {
+            if (idx + j >= ndim) break;
+            re[idx + j] = (float)(strip[k] * (z - j) / z + strip[k + 1] * j / z);
+        }
+    }
+}
+
+void rvo_filter_row(const RvDims* d, double center, const short* strip, const float* filt,
+                    const float* wr, const float* wi, float* q, float* work) {
+    const int ndim = d->ndim;
+    float* re = work;
+    float* im = work + ndim;
+    float* scratch = work + 2 * ndim;
+    rvo_place_row(d, center, strip, re, im);
+    rvo_fft_forward(d->ndimp, wr, wi, re, im, scratch);
+    for (int k = 0; k < ndim; k++) { /* CCmplx::operator*=(float), source/ccmplx.cpp:42-44 */
+        re[k] = re[k] * filt[k];
+        im[k] = im[k] * filt[k];
+    }
+    rvo_fft_inverse(d->ndimp, wr, wi, re, im, scratch);
+    for (int j = 0; j < d->ixdimp; j++) q[j] = re[j + d->ihoffset];
+}
+
+void rvo_row_table(int ixdimp, const float* q, int* igp) {
+    /* source/general.cpp:2130-2137 */
+    for (int j = 0; j < ixdimp; j++) {
+        const float p0 = q[j] * (float)RV_BACKPROJ_SCALE;
+        float p1p0 = 0.0f;
+        if (j != ixdimp - 1) {
+            const float diff = q[j + 1] - q[j];
+            p1p0 = (diff / (float)RV_DBPT_GINTP) * (float)RV_BACKPROJ_SCALE;
+        }
+        for (int k = 0; k < RV_DBPT_GINTP; k++) {
+            const float step = p1p0 * (float)k;
+            igp[j * RV_DBPT_GINTP + k] = (int)(p0 + step);
+        }
+    }
+}
+
+/* ---------------------------------------------------------------- R8 -------------------- */
+void rvo_backproject_view(int ixdimp, float fcos, float fsin, float foffset, const int* igp,
+                          int* ifp, int iy0, int iy1) {
+    /* source/general.cpp:2147-2158 (scalar path, bUseSIMD == false) */
+    const int ixdimpg = ixdimp * RV_DBPT_GINTP;
+    for (int iy = iy0; iy < iy1; iy++) {
+        int ifpidx = iy * ixdimp - 1;
+        const float fyoff = (float)iy * fsin + foffset;
+        for (int ix = 0; ix < ixdimp; ix++) {
+            const float fx = (float)ix * fcos + fyoff;
+            const int ix0 = (int)fx;
+            ifpidx++;
+            if (ix0 < 0) continue;
+            if (ix0 >= ixdimpg) continue;
+            ifp[ifpidx] += igp[ix0];
+        }
+    }
+}
+
+static int rvo_view_used(const RECONST_INFO* ri, int i, int* sidx_out) {
+    /* source/general.cpp:2087-2102 (the `break` on sidx is reported as -1) */
+    if (!(ri->bInc[i] & RV_BINC_SAMPLE)) return 0;
+    const int sidx = i * ri->iMultiplex + ri->iOffset;
+    if (sidx >= ri->maxSinogrLen) return -1;
+    if (ri->dReconFlags & (RV_RQFLAGS_USEONLYEVENFRAMES | RV_RQFLAGS_USEONLYODDFRAMES)) {
+        if (i & 1) {
+            if (ri->dReconFlags & RV_RQFLAGS_USEONLYEVENFRAMES) return 0;
+        } else {
+            if (ri->dReconFlags & RV_RQFLAGS_USEONLYODDFRAMES) return 0;
+        }
+    }
+    *sidx_out = sidx;
+    return 1;
+}
+
+int rvo_reconstruct(RECONST_INFO* ri) {
+    RvDims d;
+    rvo_dims(ri->ixdim, ri->iInterpolation, &d);
+    const int ixdimp = d.ixdimp, ndim = d.ndim;
+    const double center = ri->center;
+    float* work = (float*)malloc(sizeof(float) * (size_t)ndim * 7);
+    float* wr = (float*)malloc(sizeof(float) * (size_t)ndim);
+    float* q = (float*)malloc(sizeof(float) * (size_t)ixdimp);
+    int* igp = (int*)malloc(sizeof(int) * (size_t)ixdimp * RV_DBPT_GINTP);
+    if (!work || !wr || !q || !igp) {
+        free(work); free(wr); free(q); free(igp);
+        ri->iStatus = RECONST_INFO_ERROR;
+        return RV_ERR_HOST_ALLOC;
+    }
+    float* wi = wr + ndim / 2;
+    rvo_fft_twiddles(d.ndimp, wr, wi);
+    /* source/general.cpp:2063-2066 */
+    const int ibatch = ri->iStartSino, ncpu = ri->iStepSino;
+    const int iy0 = (ixdimp * ibatch + ncpu - 1) / ncpu;
+    const int iy1 = (ixdimp * (ibatch + 1) + ncpu - 1) / ncpu;
+    for (int i = 0; i < ri->iLenSinogr - 1; i++) {
+        int sidx = 0;
+        const int u = rvo_view_used(ri, i, &sidx);
+        if (u < 0) break;
+        if (u == 0) continue;
+        if (ri->iStartSino == 0) (*(ri->nSinogr))++;
+        rvo_filter_row(&d, center, ri->iSinogr[sidx], ri->fFilter, wr, wi, q, work);
+        rvo_row_table(ixdimp, q, igp);
+        float fcos, fsin, foffset;
+        rvo_view_geometry(&d, center, ri->fdeg[i], ri->fTiltAngle, &fcos, &fsin, &foffset);
+        rvo_backproject_view(ixdimp, fcos, fsin, foffset, igp, ri->iReconst, iy0, iy1);
+    }
+    free(work); free(wr); free(q); free(igp);
+    if (ri->iStatus != RECONST_INFO_ERROR) ri->iStatus = RECONST_INFO_IDLE;  /* :2181-2182 */
+    return 0;
+}
+
+typedef struct { RECONST_INFO ri; int rc; } rvo_job;
+static void* rvo_worker(void* arg) {
+    rvo_job* j = (rvo_job*)arg;
+    j->rc = rvo_reconstruct(&j->ri);
+    return NULL;
+}
+
+int rvo_reconstruct_mt(RECONST_INFO* ri, int nthreads) {
+    if (nthreads <= 1) {
+        RECONST_INFO one = *ri;
+        one.iStartSino = 0;
+        one.iStepSino = 1;
+        int rc = rvo_reconstruct(&one);
+        ri->iStatus = one.iStatus;
+        return rc;
+    }
+    rvo_job* jobs = (rvo_job*)calloc((size_t)nthreads, sizeof(rvo_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!jobs || !th) { free(jobs); free(th); return RV_ERR_HOST_ALLOC; }
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t].ri = *ri;
+        jobs[t].ri.iStartSino = t;
+        jobs[t].ri.iStepSino = nthreads;
+        pthread_create(&th[t], NULL, rvo_worker, &jobs[t]);
+    }
+    int rc = 0;
+    for (int t = 0; t < nthreads; t++) {
+        pthread_join(th[t], NULL);
+        if (jobs[t].rc) rc = jobs[t].rc;
+    }
+    free(jobs); free(th);
+    return rc;
+}
+
+/* ---------------------------------------------------------------- R1 -------------------- */
+int rvo_generate_sinogram(RECONST_INFO* ri) {
+    /* source/general.cpp:2393-2520 */
+    const int isino = ri->maxSinogrLen;
+    const int ixlen = ri->ixdim;
+    const int mult = ri->iMultiplex;
+    const int ibin = (ri->iInterpolation == 0) ? 4 : ((ri->iInterpolation == 1) ? 2 : 1);
+    short** rows = ri->iSinogr;
+    const char* bInc = ri->bInc;
+    const float* fexp = ri->fexp;
+    const float* fdeg = ri->fdeg;
+    const int pixmin = (ri->iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit
+                                                    : RV_SINOGRAM_PIXEL_MIN16bit;
+    double* dinc = (double*)malloc(sizeof(double) * (size_t)ixlen);
+    if (!dinc) { ri->iStatus = RECONST_INFO_ERROR; return 1; }
+    int i0 = -1, i1 = -1;
+    for (int i = 0; i < isino - 1; i++) {
+        if (bInc[i] & RV_BINC_NOUSE) continue;
+        if (!(bInc[i] & RV_BINC_SAMPLE)) { i0 = i; break; }
+    }
+    for (int i = 0; i < isino - 1; i++) {
+        if ((bInc[i] & RV_BINC_NOUSE) && !(bInc[i] & RV_BINC_SAMPLE)) continue;
+        if (!(bInc[i] & RV_BINC_SAMPLE)) { i0 = i; i1 = -1; continue; }
+        if (i1 < 0) {
+            for (int j = i; j < isino - 1; j++) {
+                if (bInc[j] & RV_BINC_SAMPLE) continue;
+                i1 = j;
+                break;
+            }
+            if (i1 < 0) {
+                if (i0 >= 0) i1 = i0;
+                else { ri->iStatus = RECONST_INFO_ERROR; break; }
+            }
+        }
+        if (i0 < 0 || i1 < 0) { ri->iStatus = RECONST_INFO_ERROR; free(dinc); return 1; }
+        if (i % ri->iStepSino != ri->iStartSino) continue;
+        float t0 = fexp[i0];
+        const float t1 = fexp[i1];
+        const float ti = fexp[i];
+        if (t0 == t1) t0 = 0;
+        else t0 = (ti - t0) / (t1 - t0);
+        const double cth = cos(fdeg[i] * RVO_DEG_TO_RAD);
+        const double sth = sin(fdeg[i] * RVO_DEG_TO_RAD);
+        int idrift = 0;
+        if ((ri->drEnd > ri->drStart) && (ri->dReconFlags & RV_RQFLAGS_DRIFTPARAMS)) {
+            if ((ri->drStart < i) && (i < ri->drEnd) && ri->drOmit) {
+                for (int k = 0; k < mult; k++) memset(rows[mult * i + k], 0, sizeof(short) * ixlen);
+                continue;
+            }
+            const double dd = ri->drX * cth - ri->drY * sth;
+            if (i >= ri->drEnd) idrift = (int)dd;
+            else if (i > ri->drStart)
+                idrift = (int)(dd * (i - ri->drStart) / (ri->drEnd - ri->drStart));
+        }
+        if (bInc[i] & RV_BINC_SKIP) {
+            for (int k = 0; k < mult; k++) memset(rows[mult * i + k], 0, sizeof(short) * ixlen);
+            continue;
+        }
+        if ((ri->dReconFlags & RV_RQFLAGS_DRIFTLIST) && ri->piDrift) idrift -= ri->piDrift[i];
+        for (int k = 0; k < mult; k++) {
+            const unsigned short* dark = (const unsigned short*)rows[mult * (isino - 1) + k];
+            const unsigned short* in0 = (const unsigned short*)rows[mult * i0 + k];
+            const unsigned short* in1 = (const unsigned short*)rows[mult * i1 + k];
+            for (int j = 0; j < ixlen; j++) {
+                /* int*float, ushort+float and float-ushort all evaluate in float (:2475);
+                 * only the result is widened to double. */
+                const float prod = (float)((int)in1[j] - (int)in0[j]) * t0;
+                const float s1 = (float)in0[j] + prod;
+                dinc[j] = (double)(s1 - (float)dark[j]);
+            }
+            short* strip = rows[mult * i + k];
+            const unsigned short* ustrip = (const unsigned short*)strip;
+            if (ri->dReconFlags & RV_RQFLAGS_ZERNIKE) {
+                for (int j = 0; j < ixlen; j++) {
+                    if (dinc[j] <= 0) { strip[j] = 0; continue; }
+                    const int s = (int)ustrip[j] - dark[j];
+                    if (s < pixmin) { strip[j] = 0; continue; }
+                    strip[j] = (short)(int)(dinc[j] * 1000 / s + 0.5);
+                }
+            } else {
+                for (int j = 0; j < ixlen; j++) {
+                    if (dinc[j] <= 0) { strip[j] = 0; continue; }
+                    const int s = (int)ustrip[j] - dark[j];
+                    if (s < pixmin) { strip[j] = 0; continue; }
+                    strip[j] = (short)(int)(log(dinc[j] / s) * RV_LOG_SCALE + 0.5);
+                }
+            }
+            const int sh = idrift / ibin;
+            if (idrift > 0) {
+                for (int j = ixlen - 1; j >= 0; j--) {
+                    if (j + sh >= ixlen) continue;
+                    strip[j + sh] = strip[j];
+                }
+                for (int j = sh - 1; j >= 0; j--) strip[j] = 0;
+            } else if (idrift < 0) {
+                for (int j = 0; j < ixlen; j++) {
+                    if (j + sh < 0) continue;
+                    strip[j + sh] = strip[j];
+                }
+                for (int j = ixlen + sh; j < ixlen; j++) strip[j] = 0;
+            }
+        }
+    }
+    free(dinc);
+    if (ri->iStatus == RECONST_INFO_ERROR) return 1;
+    ri->iStatus = RECONST_INFO_IDLE;  /* source/general.cpp:2529-2530 */
+    return 0;
+}
+
+/* ---------------------------------------------------------------- R9 -------------------- */
+void rvo_rescale(int* rec, int ixdimp, double center, int ipintp, int ibinning, int* pimin,
+                 int* pimax) {
+    /* source/gazoDoc.cpp:3993-3997,4007-4021 */
+    const int n2 = ixdimp * ixdimp;
+    int imax = 0, imin = INT_MAX;
+    for (int i = 0; i < n2; i++) {
+        imax = rec[i] > imax ? rec[i] : imax;
+        imin = rec[i] < imin ? rec[i] : imin;
+    }
+    if (imin == imax) imax++;
+    const double a = ipintp * center / ibinning;
+    const double b = ixdimp - ipintp * center / ibinning;
+    int irad2 = (a < b) ? (int)a : (int)b;
+    irad2 *= irad2;
+    const int ixdimh = ixdimp / 2;
+    for (int i = 0; i < ixdimp; i++) {
+        int i2 = i - ixdimh;
+        i2 *= i2;
+        for (int j = 0; j < ixdimp; j++) {
+            const int j2 = j - ixdimh;
+            const int idx = i * ixdimp + j;
+            if (i2 + j2 * j2 > irad2) rec[idx] = 0;
+            else {
+                const float num = (float)(rec[idx] - imin) * (float)(USHRT_MAX - 1);
+                rec[idx] = (int)(num / (float)(imax - imin));
+            }
+        }
+    }
+    if (pimin) *pimin = imin;
+    if (pimax) *pimax = imax;
+}
+
+/* ---------------------------------------------------------------- FP64 oracle ----------- */
+static void rvo_pass64(int n, int al, const double* wr, const double* wi, const double* xr,
+                       const double* xi, double* yr, double* yi) {
+    const int half = n / 2, bt = half / al;
+    for (int m = 0; m < bt; m++)
+        for (int q = 0; q < al; q++) {
+            const int a = m * al + q, b = a + half, t = q * bt, o = 2 * m * al + q;
+            const double sr = xr[b] * wr[t] - xi[b] * wi[t];
+            const double si = xr[b] * wi[t] + xi[b] * wr[t];
+            yr[o] = xr[a] + sr; yi[o] = xi[a] + si;
+            yr[o + al] = xr[a] - sr; yi[o + al] = xi[a] - si;
+        }
+}
+
+/* The same linear map as rvo_fft_forward/inverse (identical index conventions), in double
+ * with exact twiddles: the transform the float routine approximates. */
+static void rvo_fft64(int np, int inverse, const double* wr, const double* wi, double* re,
+                      double* im, double* work) {
+    const int n = 1 << np, half = n / 2;
+    double *ar = work, *ai = work + n, *br = work + 2 * n, *bi = work + 3 * n;
+    for (int j = 0; j < half; j++) {
+        const int u = inverse ? j : half - 1 - j, v = inverse ? j + half : n - 1 - j;
+        ar[2 * j] = re[u] + re[v]; ai[2 * j] = im[u] + im[v];
+        ar[2 * j + 1] = re[u] - re[v]; ai[2 * j + 1] = im[u] - im[v];
+    }
+    int al = 2;
+    for (int l = 1; l < np - 1; l++) {
+        rvo_pass64(n, al, wr, wi, ar, ai, br, bi);
+        double* t;
+        t = ar; ar = br; br = t;
+        t = ai; ai = bi; bi = t;
+        al *= 2;
+    }
+    for (int k = 0; k < half; k++) {
+        const double sr = ar[half + k] * wr[k] - ai[half + k] * wi[k];
+        const double si = ar[half + k] * wi[k] + ai[half + k] * wr[k];
+        if (!inverse) {
+            const int ip = k ? n - k : 0, im_ = k ? half - k : half;
+            br[ip] = ar[k] + sr; bi[ip] = ai[k] + si;
+            br[im_] = ar[k] - sr; bi[im_] = ai[k] - si;
+        } else {
+            br[k] = ar[k] - sr; bi[k] = ai[k] - si;
+            br[k + half] = ar[k] + sr; bi[k + half] = ai[k] + si;
+        }
+    }
+    if (!inverse) {
+        memcpy(re, br, sizeof(double) * n);
+        memcpy(im, bi, sizeof(double) * n);
+    } else {
+        for (int i = 0; i < n; i++) {
+            re[i] = br[n - 1 - i] / n;
+            im[i] = bi[n - 1 - i] / n;
+        }
+    }
+}
+
+int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
+    RvDims d;
+    rvo_dims(ri->ixdim, ri->iInterpolation, &d);
+    const int ixdimp = d.ixdimp, ndim = d.ndim;
+    const double center = ri->center;
+    double* buf = (double*)malloc(sizeof(double) * (size_t)ndim * 8);
+    float* fre = (float*)malloc(sizeof(float) * (size_t)ndim * 2);
+    if (!buf || !fre) { free(buf); free(fre); return RV_ERR_HOST_ALLOC; }
+    double *re = buf, *im = buf + ndim, *wr = buf + 2 * ndim, *wi = wr + ndim / 2;
+    double* work = buf + 3 * ndim;
+    for (int i = 0; i < ndim / 2; i++) {
+        const double a = -2.0 * M_PI * (double)i / (double)ndim;
+        wr[i] = cos(a);
+        wi[i] = sin(a);
+    }
+    memset(out, 0, sizeof(double) * (size_t)ixdimp * ixdimp);
+    const double cen = (double)d.ixdimh + (center - (int)center) * d.iIntpDim;
+    for (int i = 0; i < ri->iLenSinogr - 1; i++) {
+        int sidx = 0;
+        const int u = rvo_view_used(ri, i, &sidx);
+        if (u < 0) break;
+        if (u == 0) continue;
+        rvo_place_row(&d, center, ri->iSinogr[sidx], fre, fre + ndim);
+        for (int k = 0; k < ndim; k++) { re[k] = fre[k]; im[k] = 0; }
+        rvo_fft64(d.ndimp, 0, wr, wi, re, im, work);
+        for (int k = 0; k < ndim; k++) { re[k] *= ri->fFilter[k]; im[k] *= ri->fFilter[k]; }
+        rvo_fft64(d.ndimp, 1, wr, wi, re, im, work);
+        const double* qd = re + d.ihoffset;
+        const double th = (double)(ri->fdeg[i] + ri->fTiltAngle) * (M_PI / 180.0);
+        const double c = cos(th), s = -sin(th);
+        const double off = cen - d.ixdimh * (c + s);
+        for (int iy = 0; iy < ixdimp; iy++) {
+            for (int ix = 0; ix < ixdimp; ix++) {
+                const double x = ix * c + iy * s + off;
+                if (!(x >= 0.0) || !(x < ixdimp)) continue;
+                int j = (int)x;
+                if (j > ixdimp - 1) j = ixdimp - 1;
+                const double f = x - j;
+                const double q1 = (j + 1 < ixdimp) ? qd[j + 1] : qd[j];
+                out[(size_t)iy * ixdimp + ix] += (qd[j] + (q1 - qd[j]) * f) * RV_BACKPROJ_SCALE;
+            }
+        }
+    }
+    free(buf); free(fre);
+    return 0;
+}
