@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark of the full-scale convolution back-projection workload.
+
+Workload (one step): a 2048-pixel detector x 1800 views over 180 degrees, 64 detector rows
+(slices), raw uint16 frames I = Poisson(20000 exp(-p)) + dark (dark ~ N(100, 3), flat
+20000 (1 + 0.02 smooth noise)), 40 random ellipsoids, rotation-centre offset U[-10, 10] px,
+Shepp-Logan filter -> 64 slices of 2048 x 2048.  The step runs the whole hot path on the device:
+flat/dark log normalisation, padding, FFT filtering, 1/16 sub-sample tables and the
+back-projection, in the reference's fixed-point semantics (bit-exact with the reference CPU
+routine; the tests prove it).  Synthetic data stand in for beamline data (none is public).
+
+Metric: Tau = time / (pixels per slice x views x slices) in ns per pixel-view (lower is better),
+with slices/s alongside.  `value` is device time with inputs resident in HBM; `e2e` is the same
+metric through RvStackRunHost with pinned host buffers (host->device frames and device->host
+slices inside the timed region).  The CPU baseline is the oracle restatement of the reference
+CPU routine (bit-identical to it) with the reference's multi-worker scheme on all host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--slices S]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+W_DET, N_VIEWS, N_SLICES = 2048, 1800, 64
+PUBLISHED_TAU_NS = 0.029  # RTX A4000, 2048^2 x 1800 views (reference README, Build-220422)
+WORKLOAD = "fbp-2048det-1800views-64slices-raw-uint16"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slices", type=int, default=N_SLICES, help="slices per step (default: the workload's 64)")
+    ap.add_argument("--mode", default="ref", choices=["ref", "lin", "f16", "bf16"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--seed", type=int, default=2026)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------ data -------
+def centre_of(seed: int) -> float:
+    rng = np.random.default_rng(seed)
+    return (W_DET - 1) / 2.0 + rng.uniform(-10.0, 10.0)
+
+
+def make_stack_gpu(seed: int, nslices: int, device):
+    """Raw frames on the device: [nframes + 1, nslices, W] uint16 stored in an int16 tensor
+    (frame 0 flat, 1..V samples, V+1 flat, last = dark)."""
+    import torch
+    from recview_gb300 import phantom
+    rng = np.random.default_rng(seed)
+    ells3 = phantom.random_ellipsoids(rng, 40)
+    center = centre_of(seed)
+    V, W = N_VIEWS, W_DET
+    fdeg_s = phantom.angle_table(V)
+    theta = torch.tensor(np.deg2rad(fdeg_s.astype(np.float64)), device=device)[:, None]
+    t = torch.tensor(phantom.detector_coords(W, center), device=device)[None, :]
+    ys = (np.arange(nslices) - (nslices - 1) / 2.0) / (max(nslices, 2) / 2.0) * 0.5
+    gen = torch.Generator(device=device).manual_seed(seed)
+    dark = 100.0 + 3.0 * torch.randn(nslices, W, device=device, generator=gen, dtype=torch.float64)
+    flat = torch.tensor(20000.0 * (1.0 + 0.02 * phantom.smooth_noise(rng, (nslices, W), 16.0)), device=device)
+    nframes = V + 2
+    raw = torch.empty((nframes + 1, nslices, W), dtype=torch.int16, device=device)
+
+    def to_u16(x):
+        x = torch.clamp(torch.round(x), 0, 65535).to(torch.int32)
+        return torch.where(x > 32767, x - 65536, x).to(torch.int16)
+
+    for s, y in enumerate(ys):
+        p = torch.zeros((V, W), dtype=torch.float64, device=device)
+        for x0, z0, a, b, phi, mu in phantom.ellipsoid_slice(ells3, y):
+            sft = x0 * torch.cos(theta) + z0 * torch.sin(theta)
+            d = theta - phi
+            a2 = (a * torch.cos(d)) ** 2 + (b * torch.sin(d)) ** 2
+            u = t - sft
+            rad = a2 - u * u
+            p += torch.where(rad > 0, 2.0 * mu * a * b * torch.sqrt(torch.clamp(rad, min=0.0)) / a2, 0.0)
+        mean = (flat[s][None, :] * torch.exp(-p)).float()
+        raw[1:V + 1, s] = to_u16(torch.poisson(mean, generator=gen) + dark[s][None, :])
+        fl = flat[s][None, :].expand(2, W).float().contiguous()
+        f = torch.poisson(fl, generator=gen) + dark[s][None, :]
+        raw[0, s] = to_u16(f[0])
+        raw[V + 1, s] = to_u16(f[1])
+        raw[nframes, s] = to_u16(dark[s])
+    bInc = np.zeros(nframes, np.int8)
+    bInc[1:V + 1] = 1
+    fdeg = np.zeros(nframes, np.float32)
+    fdeg[1:V + 1] = fdeg_s
+    fexp = np.arange(nframes, dtype=np.float32)
+    return raw, bInc, fdeg, fexp, center
+
+
+# ------------------------------------------------------------------------------ clocks -----
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return None
+        rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        smax = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip().lower() == "active"})
+        loaded = [v for v in sm if v > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].strip())}
+
+
+# ------------------------------------------------------------------------------ CPU side ---
+def cpu_one_slice(raw_slice: np.ndarray, bInc, fdeg, fexp, center, F, threads: int, use_ref: bool):
+    """One slice of the workload on the CPU: GenerateSinogramThread then the reference's CPU
+    FBP with `threads` row-band workers.  Returns seconds."""
+    from recview_gb300.reconst import ReconInfo
+    from tests.rvtest import Oracle, ref_lib
+    oracle = Oracle()
+    r = raw_slice.copy()
+    ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=1, maxSinogrLen=r.shape[0])
+    rs = ReconInfo(r.view(np.int16), fdeg, bInc, center=center, fFilter=F, maxSinogrLen=r.shape[0],
+                   nviews=r.shape[0] - 1)
+    t0 = time.perf_counter()
+    oracle.generate_sinogram(ri)
+    if use_ref:
+        import threading
+        L = ref_lib()
+        infos = []
+        for k in range(threads):
+            x = abi_copy(rs.ri)
+            x.iStartSino, x.iStepSino = k, threads
+            infos.append(x)
+        th = [threading.Thread(target=L.rvref_fbp, args=(C.byref(x),)) for x in infos]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    else:
+        oracle.L.rvo_reconstruct_mt(C.byref(rs.ri), threads)
+    return time.perf_counter() - t0
+
+
+def abi_copy(ri):
+    from recview_gb300 import abi
+    x = abi.RECONST_INFO()
+    C.memmove(C.byref(x), C.byref(ri), C.sizeof(abi.RECONST_INFO))
+    return x
+
+
+def host_slice_data(seed: int):
+    """Raw frames of one slice for the CPU side (same distributions as the device data)."""
+    from recview_gb300 import phantom
+    center = centre_of(seed)
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(seed, W_DET, N_VIEWS, 1, center, n_ellipsoids=40)
+    return raw, bInc, fdeg, fexp, center
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    from recview_gb300 import abi
+    from recview_gb300.reconst import dims
+    from tests.rvtest import Oracle, ref_lib
+    threads = os.cpu_count() or 1
+    use_ref = ref_lib() is not None
+    raw, bInc, fdeg, fexp, center = host_slice_data(args.seed)
+    F = Oracle().set_filter(abi.FILT_SHEPP, dims(W_DET).ndim)
+    for _ in range(args.warmup):
+        cpu_one_slice(raw, bInc, fdeg, fexp, center, F, threads, use_ref)
+    ts = [cpu_one_slice(raw, bInc, fdeg, fexp, center, F, threads, use_ref) for _ in range(args.steps)]
+    t = float(np.mean(ts))
+    tau = t * 1e9 / (W_DET * W_DET * N_VIEWS)
+    kind = "reference" if use_ref else "port"
+    line = {
+        "impl": "reference", "metric": "tau_ns_per_pixel_view", "value": tau, "unit": "ns/(pixel*view)",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": tau / PUBLISHED_TAU_NS,
+        "dtype": "f32/i32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "detector": W_DET, "views": N_VIEWS, "slices_per_step": 1,
+                   "slices_in_workload": N_SLICES, "filter": "shepp-logan", "l2": "inputs larger than L2"},
+        "slices_per_s": 1.0 / t,
+        "cpu_baseline": {"value": tau, "unit": "ns/(pixel*view)", "cores": threads, "kind": kind,
+                         "sample": "1 slice of the workload per step (2048^2 x 1800 views, normalisation + FBP), "
+                                   "reference multi-worker scheme (row bands, every worker filters all views)"},
+        "e2e": {"value": tau, "unit": "ns/(pixel*view)", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------ GPU side ---
+def run_ours(args, rank: int, world: int, local_rank: int):
+    import torch
+    import torch.distributed as dist
+    import recview_gb300 as rv
+    from recview_gb300 import abi
+    from recview_gb300.build import build_lib, build_oracle
+
+    build_lib()
+    build_oracle()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    L = rv.lib()
+    S = args.slices
+    mode = {"ref": abi.MODE_REF, "lin": abi.MODE_LIN, "f16": abi.MODE_LIN_F16, "bf16": abi.MODE_LIN_BF16}[args.mode]
+    raw, bInc, fdeg, fexp, center = make_stack_gpu(args.seed + rank, S, dev)
+    F = rv.set_filter(abi.FILT_SHEPP, rv.dims(W_DET).ndim)
+    st = rv.Stack(ixdim=W_DET, nframes=raw.shape[0] - 1, nslices=S, center=center, bInc=bInc, fdeg=fdeg,
+                  fexp=fexp, fFilter=F, mode=mode)
+    npix = st.ixdimp * st.ixdimp
+    out = torch.empty((S, st.ixdimp, st.ixdimp), dtype=torch.int32 if mode == abi.MODE_REF else torch.float32,
+                      device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        tt = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
+
+    for _ in range(args.warmup):
+        st.run_device(raw.data_ptr(), out.data_ptr(), sh)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t_filter = t_bp = 0.0
+    launches = 0
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            st.run_device(raw.data_ptr(), out.data_ptr(), sh)
+            tf, tb, _tt = st.timings()
+            t_filter += tf
+            t_bp += tb
+            launches += st.launches()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    clocks = clk.summary()
+    updates_step = float(npix) * st.nviews * S
+    total_updates = updates_step * world
+    tau = ms * 1e6 / total_updates
+    bp_ms = t_bp / args.steps
+    filt_ms = t_filter / args.steps
+
+    # ---- end to end through the C ABI with pinned host buffers -----------------------------
+    e2e = None
+    if not args.no_e2e:
+        raw_h = torch.empty(raw.shape, dtype=raw.dtype, pin_memory=True)
+        raw_h.copy_(raw)
+        out_h = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+        torch.cuda.synchronize()
+        L.RvStackRunHost(st.h, C.c_void_p(raw_h.data_ptr()), C.c_void_p(out_h.data_ptr()), C.c_void_p(sh))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rc = L.RvStackRunHost(st.h, C.c_void_p(raw_h.data_ptr()), C.c_void_p(out_h.data_ptr()), C.c_void_p(sh))
+            assert rc == 0, rv.last_error()
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+        barrier()
+        e2e = {"value": e2e_ms * 1e6 / total_updates, "unit": "ns/(pixel*view)",
+               "h2d_bytes_per_step": int(raw_h.numel() * raw_h.element_size()),
+               "d2h_bytes_per_step": int(out_h.numel() * out_h.element_size()),
+               "ms_per_step": e2e_ms, "slices_per_s": S * world * 1e3 / e2e_ms}
+        del raw_h, out_h
+
+    # ---- roofline of the dominant kernel (back-projection) ----------------------------------
+    probe = (C.c_double * 2)()
+    L.RvProbeThroughput(probe, 2)
+    fp32_tflops, f2i_gops = probe[0], probe[1]
+    achieved = 4.0 * updates_step / (bp_ms * 1e-3) / 1e12      # 4 FP32 FLOP per pixel-view update
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs")
+    nviews = st.nviews
+    # stage (a) bytes per row: raw uint16 row in + the 16-entry int table (64 B per detector pixel) out
+    filt_bytes = S * nviews * (2.0 * W_DET + 64.0 * st.ixdimp)
+    roof_filter = None
+    if hbm and filt_ms > 0:
+        a = filt_bytes / (filt_ms * 1e-3) / 1e9
+        roof_filter = {"bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
+                       "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+
+    if rank == 0:
+        line = {
+            "metric": "tau_ns_per_pixel_view", "value": tau, "unit": "ns/(pixel*view)", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": tau / PUBLISHED_TAU_NS, "dtype": "f32/i32" if mode == abi.MODE_REF else args.mode,
+            "data": "synthetic (seeded ellipsoid phantom, Poisson uint16 frames)",
+            "config": {"workload": WORKLOAD, "detector": W_DET, "views": nviews, "slices_per_gpu": S,
+                       "output": f"{st.ixdimp}x{st.ixdimp} int32 per slice", "filter": "shepp-logan",
+                       "mode": args.mode, "centre": round(center, 4), "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (raw 472 MB, tables 8 GB per batch)"},
+            "slices_per_s": S * world * 1e3 / ms,
+            "updates_per_s": total_updates / (ms * 1e-3),
+            "stage_ms": {"filter": filt_ms, "backprojection": bp_ms},
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": fp32_tflops, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_tflops if fp32_tflops else None, "traffic": None,
+                         "kernel": "k_bp_ref", "flop_per_update": 4,
+                         "peak_source": "measured in this run (RvProbeThroughput FP32 FMA burst)",
+                         "f2i_gops_measured": f2i_gops,
+                         "updates_per_s_bp": updates_step / (bp_ms * 1e-3)},
+            "roofline_filter": roof_filter,
+            "clocks": clocks,
+        }
+        if not args.no_cpu and world == 1:
+            raw_c, bInc_c, fdeg_c, fexp_c, center_c = host_slice_data(args.seed)
+            threads = os.cpu_count() or 1
+            tcpu = cpu_one_slice(raw_c, bInc_c, fdeg_c, fexp_c, center_c, F, threads, False)
+            tau_cpu = tcpu * 1e9 / (W_DET * W_DET * N_VIEWS)
+            line["cpu_baseline"] = {"value": tau_cpu, "unit": "ns/(pixel*view)", "cores": threads, "kind": "port",
+                                    "sample": "1 of 64 slices (2048^2 x 1800 views, normalisation + FBP), "
+                                              "reference multi-worker scheme", "seconds": tcpu}
+        print(json.dumps(line), flush=True)
+    st.close()
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group(backend="nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

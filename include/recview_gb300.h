@@ -278,6 +278,17 @@ int RvStackLastTimings(const RvStack* st, float* ms3);
 /* Number of kernels launched by the last run. */
 int RvStackLastLaunchCount(const RvStack* st);
 
+/* Validation mode: while enabled, the REF back-projection runs a bounds-checked variant that
+ * skips and counts every table index falling outside the window staged in shared memory (the
+ * production kernel relies on the window bound instead of per-access checks).  Slower; for tests. */
+int RvSetCheckedBackprojection(int enable);
+unsigned long long RvGetWindowViolations(void);
+
+/* Device throughput probes used as roofline denominators for the back-projection, which is
+ * bound by instruction issue rather than HBM or tensor cores: out[0] = FP32 FMA TFLOP/s,
+ * out[1] = float->int32 conversions in G/s, both measured on the current device. */
+int RvProbeThroughput(double* out, int n);
+
 #ifdef __cplusplus
 }
 #endif

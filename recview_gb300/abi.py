@@ -182,6 +182,9 @@ PROTOTYPES = {
     "RvStackRunHost": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "RvStackLastTimings": (C.c_int, [C.c_void_p, c_float_p]),
     "RvStackLastLaunchCount": (C.c_int, [C.c_void_p]),
+    "RvSetCheckedBackprojection": (C.c_int, [C.c_int]),
+    "RvGetWindowViolations": (C.c_ulonglong, []),
+    "RvProbeThroughput": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
 }
 
 

@@ -1,0 +1,109 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/recview_gb300.h"
+
+namespace rv {
+
+// ---- error reporting ---------------------------------------------------------------------
+void set_error(int code, const std::string& msg);
+inline bool cuda_ok(cudaError_t e, int code, const char* what) {
+    if (e == cudaSuccess) return true;
+    set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+// ---- geometry ----------------------------------------------------------------------------
+struct Dims {
+    int ixdim, iZooming, iIntpDim, ndimp, ndim, ixdimp, ixdimh, ihoffset;
+};
+Dims make_dims(int ixdim, int iInterpolation);
+// float geometry of one view in the reference's operation order (source/general.cpp:2139-2142)
+float fcenter_of(const Dims& d, double center);
+void view_geometry(const Dims& d, double center, float fdeg, float tilt, float* fcos, float* fsin,
+                   float* foffset);
+// twiddles of CFft::Init1(np, -1), correctly rounded (float2 per entry, n/2 entries)
+void fft_twiddles(int np, std::vector<float2>& out);
+
+// limits of the on-chip FFT and of the back-projection tile windows
+constexpr int kMaxNdimp = 14;        // ndim <= 16384 (one row per CTA in shared memory)
+constexpr int kMaxIxdimp = 16384;    // 16 * ixdimp < 2^23 keeps the exact truncation trick valid
+
+// ---- per-row job of the filter stage -------------------------------------------------------
+// One filtered row = one (view, slice).  Source rows are either int16 sinogram rows or raw
+// uint16 frames normalised on the fly against flats i0/i1 (weight t0) and the dark row.
+struct RowJob {
+    int src_row;     // row index of the sample (int16 sinogram or raw uint16 frame row)
+    int flat0_row;   // raw mode: bracketing flat rows and dark row
+    int flat1_row;
+    int dark_row;
+    float t0;        // raw mode: flat interpolation weight (source/general.cpp:2443-2447)
+    int dst;         // output slot (view-major within a slice: slice * nviews + v)
+    int zero;        // 1: the row is all zero (SKIP frame)
+    int pad;
+};
+
+struct FilterLaunch {
+    const void* src;          // int16 rows or uint16 raw rows, row stride = ixdim elements
+    int raw;                  // 1: src holds raw uint16 frames (normalise), 0: int16 sinogram
+    int pixmin;               // sample threshold (source/general.cpp:2402)
+    const RowJob* jobs;       // device array
+    int njobs;
+    const float* filt;        // device, ndim
+    const float2* tw;         // device, ndim/2
+    int* table;               // REF output: int table, 16*ixdimp ints per slot (may be null)
+    float* rows;              // LIN output: filtered rows x BACKPROJ_SCALE (may be null)
+    void* rows16;             // LIN_F16/BF16 output: half/bf16 rows (may be null)
+    float* row_scale;         // per-row scale of the 16-bit rows
+    int mode;
+    Dims d;
+    int ic;                   // (int)center
+    long long table_stride;   // ints between table slots
+    long long row_stride;     // elements between filtered rows
+};
+cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
+
+// ---- back-projection ---------------------------------------------------------------------
+struct BackprojLaunch {
+    const int* table;         // REF: int tables, slot-major
+    const float* rows;        // LIN: float rows
+    const void* rows16;       // LIN_F16/BF16 rows
+    const float* row_scale;
+    const float4* geom;       // per view {fcos, fsin, foffset, 0} (REF units: x16)
+    int nviews;               // views per slice
+    int nslices;
+    int ixdimp;
+    long long table_stride;   // ints per view slot
+    long long slice_table_stride;  // ints per slice (nviews * table_stride)
+    long long row_stride;     // LIN: elements per row
+    long long slice_row_stride;
+    void* out;                // int32 (REF) or float (LIN) slices, ixdimp^2 each
+    long long out_slice_stride;  // elements per output slice
+    int center_shift16;       // REF: 16 * integer centre offset added to foffset (R10)
+    int mode;
+    int checked;              // 1: bounds-checked variant that counts window violations
+    unsigned int* status;     // device counter of violations (checked variant)
+};
+cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s);
+
+// ---- normalisation (R1) written back as int16 rows ------------------------------------------
+struct NormLaunch {
+    const uint16_t* raw;      // rows of the raw buffer (device), ixdim each
+    short* out;               // destination rows (device), ixdim each
+    const RowJob* jobs;       // src_row/flat/dark rows; dst = destination row
+    int njobs;
+    int ixdim;
+    int pixmin;
+    int zernike;
+    const int* shift;         // per job drift shift in pixels (may be null)
+};
+cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s);
+
+int kernel_launches_per_filter();
+}  // namespace rv

@@ -1,0 +1,773 @@
+// Device kernels of the convolution back-projection path (sm_103a).
+//
+//  k_normalise  R1      flat/dark log normalisation -> int16 rows (CudaSinogramHost)
+//  k_filter     R1+R5+R6+R7  one CTA per sinogram row: [normalise] -> pad/zoom -> forward
+//                       radix-2 FFT -> filter -> inverse FFT -> 1/16 sub-sample int table
+//                       (REF) or FP32/FP16/BF16 filtered row (LIN modes)
+//  k_bp_ref     R8      pixel-tile back-projection with the reference's fixed-point table
+//  k_bp_lin     R8'     pixel-tile back-projection with linear interpolation (FP32 accumulate)
+//
+// Floating-point discipline: every operation that the reference performs in float is done with
+// an explicitly rounded intrinsic (__fmul_rn/__fadd_rn/__fsub_rn) so nvcc never contracts it into
+// an FMA; the REF outputs are therefore bit-identical to the reference CPU routine.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "rv_internal.h"
+
+namespace rv {
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// x * w evaluated as (xr*wr - xi*wi, xr*wi + xi*wr): source/cfft.cpp:234-235
+__device__ __forceinline__ float2 cmul(float2 x, float2 w) {
+    return make_float2(fsub(fmul(x.x, w.x), fmul(x.y, w.y)), fadd(fmul(x.x, w.y), fmul(x.y, w.x)));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(fadd(a.x, b.x), fadd(a.y, b.y)); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(fsub(a.x, b.x), fsub(a.y, b.y)); }
+
+// ---------------------------------------------------------------------------------------------
+// R1: one normalised sample (source/general.cpp:2466-2503).  The incident intensity is a float
+// expression in the reference (int*float, ushort+float, float-ushort); only the log ratio is in
+// double.  Fast path: FP32 log with an error bound of 7e-3 on v = 3000*log(I0/S) + 0.5; samples
+// whose v lies within 0.02 of an integer are recomputed in FP64 exactly as the reference does.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ short norm_sample(int raw, int f0, int f1, int dark, float t0, int pixmin,
+                                             int zernike) {
+    const float prod = fmul((float)(f1 - f0), t0);
+    const float s1 = fadd((float)f0, prod);
+    const float dinc = fsub(s1, (float)dark);
+    if (!(dinc > 0.0f)) return 0;
+    const int s = raw - dark;
+    if (s < pixmin) return 0;
+    if (zernike) {
+        const double v = __dadd_rn(__ddiv_rn(__dmul_rn((double)dinc, 1000.0), (double)s), 0.5);
+        return (short)__double2int_rz(v);
+    }
+    const float ratio = __fdiv_rn(dinc, (float)s);
+    const float w = fadd(fmul(logf(ratio), 3000.0f), 0.5f);
+    const float dist = fabsf(w - rintf(w));
+    if (dist > 0.02f) return (short)__float2int_rz(w);
+    const double vd = __dadd_rn(__dmul_rn(log(__ddiv_rn((double)dinc, (double)s)), 3000.0), 0.5);
+    return (short)__double2int_rz(vd);
+}
+
+__global__ void k_normalise(NormLaunch p) {
+    const RowJob job = p.jobs[blockIdx.x];
+    const int W = p.ixdim;
+    const uint16_t* r = p.raw + (size_t)job.src_row * W;
+    const uint16_t* f0 = p.raw + (size_t)job.flat0_row * W;
+    const uint16_t* f1 = p.raw + (size_t)job.flat1_row * W;
+    const uint16_t* dk = p.raw + (size_t)job.dark_row * W;
+    short* out = p.out + (size_t)job.dst * W;
+    const int sh = p.shift ? p.shift[blockIdx.x] : 0;
+    for (int x = threadIdx.x; x < W; x += blockDim.x) {
+        short v = 0;
+        const int j = x - sh;  // drift shift (source/general.cpp:2505-2517)
+        if (!job.zero && j >= 0 && j < W)
+            v = norm_sample(r[j], f0[j], f1[j], dk[j], job.t0, p.pixmin, p.zernike);
+        out[x] = v;
+    }
+}
+
+cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
+    if (p.njobs <= 0) return cudaSuccess;
+    k_normalise<<<p.njobs, 256, 0, s>>>(p);  // one CTA per row
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// R5+R6+R7: filter one row per CTA.  Shared memory: buf[n] complex (in-place radix-2 passes with
+// a register hand-off between read and write phases), tw[n/2], strip[ixdim] shorts.
+// The pass structure is the reference's Stockham FFT (source/cfft.cpp:193-369): pass l reads
+// x[j] and x[j + n/2] for butterfly j and writes y[2j - q], y[2j - q + al], q = j mod al.
+// ---------------------------------------------------------------------------------------------
+template <int BPT>
+__global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
+    extern __shared__ __align__(16) float2 sm[];
+    const int n = p.d.ndim, half = n >> 1, np = p.d.ndimp;
+    float2* buf = sm;
+    float2* tw = sm + n;
+    short* strip = reinterpret_cast<short*>(tw + half);
+    const int tid = threadIdx.x, NT = blockDim.x;
+    const RowJob job = p.jobs[blockIdx.x];
+    const int W = p.d.ixdim;
+
+    for (int i = tid; i < half; i += NT) tw[i] = p.tw[i];
+    // ---- sinogram row (R1 on the fly for raw frames) -------------------------------------------
+    if (p.raw) {
+        const uint16_t* base = static_cast<const uint16_t*>(p.src);
+        const uint16_t* r = base + (size_t)job.src_row * W;
+        const uint16_t* f0 = base + (size_t)job.flat0_row * W;
+        const uint16_t* f1 = base + (size_t)job.flat1_row * W;
+        const uint16_t* dk = base + (size_t)job.dark_row * W;
+        for (int x = tid; x < W; x += NT)
+            strip[x] = job.zero ? (short)0 : norm_sample(r[x], f0[x], f1[x], dk[x], job.t0, p.pixmin, 0);
+    } else {
+        const short* r = static_cast<const short*>(p.src) + (size_t)job.src_row * W;
+        for (int x = tid; x < W; x += NT) strip[x] = job.zero ? (short)0 : r[x];
+    }
+    __syncthreads();
+    // ---- R5: placement with edge padding and integer zoom (source/general.cpp:2105-2126) ------
+    {
+        const int z = p.d.iIntpDim;
+        const int idx0 = (0 - p.ic) * z + (half - 1);
+        const int idx1 = (W - 1 - p.ic) * z + (half - 1) + 1;
+        for (int m = tid; m < n; m += NT) {
+            float v;
+            if (m < idx0) v = strip[0];
+            else if (m >= idx1) v = strip[W - 1];
+            else {
+                const int k = (m - idx0) / z, j = (m - idx0) - k * z;
+                if (j == 0) v = strip[k];
+                else v = (float)((int)strip[k] * (z - j) / z + (int)strip[k + 1] * j / z);
+            }
+            buf[m] = make_float2(v, 0.0f);
+        }
+    }
+    __syncthreads();
+
+    float2 a[BPT], b[BPT];
+    // ---- forward transform (CFft::FFT1Rev) ----------------------------------------------------
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        a[i] = buf[half - 1 - j];
+        b[i] = buf[n - 1 - j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        buf[2 * j] = cadd(a[i], b[i]);
+        buf[2 * j + 1] = csub(a[i], b[i]);
+    }
+    __syncthreads();
+    for (int l = 1; l < np - 1; l++) {
+        const int al = 1 << l, mask = al - 1, sh = np - 1 - l;  // bt = half >> l = 1 << sh
+#pragma unroll
+        for (int i = 0; i < BPT; i++) {
+            const int j = tid + i * NT;
+            a[i] = buf[j];
+            b[i] = cmul(buf[j + half], tw[(j & mask) << sh]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < BPT; i++) {
+            const int j = tid + i * NT;
+            const int o = 2 * j - (j & mask);
+            buf[o] = cadd(a[i], b[i]);
+            buf[o + al] = csub(a[i], b[i]);
+        }
+        __syncthreads();
+    }
+    // last forward pass writes reversed (source/cfft.cpp:246-265); the filter multiply
+    // (source/general.cpp:2128, CCmplx::operator*=(float)) is applied on the way out.
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        a[i] = buf[j];
+        b[i] = (j == 0) ? buf[j + half] : cmul(buf[j + half], tw[j]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        const int op = (j == 0) ? 0 : n - j;
+        const int om = (j == 0) ? half : half - j;
+        const float2 vp = cadd(a[i], b[i]), vm = csub(a[i], b[i]);
+        const float fp = __ldg(p.filt + op), fm = __ldg(p.filt + om);
+        buf[op] = make_float2(fmul(vp.x, fp), fmul(vp.y, fp));
+        buf[om] = make_float2(fmul(vm.x, fm), fmul(vm.y, fm));
+    }
+    __syncthreads();
+    // ---- inverse transform (CFft::FFT1) --------------------------------------------------------
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        a[i] = buf[j];
+        b[i] = buf[j + half];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        buf[2 * j] = cadd(a[i], b[i]);
+        buf[2 * j + 1] = csub(a[i], b[i]);
+    }
+    __syncthreads();
+    for (int l = 1; l < np - 1; l++) {
+        const int al = 1 << l, mask = al - 1, sh = np - 1 - l;
+#pragma unroll
+        for (int i = 0; i < BPT; i++) {
+            const int j = tid + i * NT;
+            a[i] = buf[j];
+            b[i] = cmul(buf[j + half], tw[(j & mask) << sh]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < BPT; i++) {
+            const int j = tid + i * NT;
+            const int o = 2 * j - (j & mask);
+            buf[o] = cadd(a[i], b[i]);
+            buf[o + al] = csub(a[i], b[i]);
+        }
+        __syncthreads();
+    }
+    // last inverse pass with the two halves swapped (source/cfft.cpp:355-368)
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        a[i] = buf[j];
+        b[i] = cmul(buf[j + half], tw[j]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; i++) {
+        const int j = tid + i * NT;
+        buf[j] = csub(a[i], b[i]);
+        buf[j + half] = cadd(a[i], b[i]);
+    }
+    __syncthreads();
+
+    // ---- R7: CFft::FFT1 reversal + 1/n (source/cfft.cpp:418-425), extraction at ihoffset and
+    // the 1/16 sub-sample int table (source/general.cpp:2130-2137).
+    const float inv_n = 1.0f / (float)n;
+    const int ixdimp = p.d.ixdimp;
+    const int rbase = n - 1 - p.d.ihoffset;  // q[j] = buf[rbase - j].x / n
+    if (p.table) {
+        int* tab = p.table + (size_t)job.dst * p.table_stride;
+        for (int j = tid; j < ixdimp; j += NT) {
+            const float qj = fmul(buf[rbase - j].x, inv_n);
+            const float p0 = fmul(qj, 100.0f);
+            float p1p0 = 0.0f;
+            if (j != ixdimp - 1) {
+                const float qn = fmul(buf[rbase - j - 1].x, inv_n);
+                p1p0 = fmul(fmul(fsub(qn, qj), 0.0625f), 100.0f);  // (q1-q0)/16*100
+            }
+            int v[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) v[k] = __float2int_rz(fadd(p0, fmul(p1p0, (float)k)));
+            int4* dst = reinterpret_cast<int4*>(tab + 16 * (size_t)j);
+            dst[0] = make_int4(v[0], v[1], v[2], v[3]);
+            dst[1] = make_int4(v[4], v[5], v[6], v[7]);
+            dst[2] = make_int4(v[8], v[9], v[10], v[11]);
+            dst[3] = make_int4(v[12], v[13], v[14], v[15]);
+        }
+    }
+    if (p.rows) {
+        float* row = p.rows + (size_t)job.dst * p.row_stride;
+        for (int j = tid; j < ixdimp; j += NT) row[j] = fmul(fmul(buf[rbase - j].x, inv_n), 100.0f);
+    }
+    if (p.rows16) {
+        // per-row scale: max |q*100| over the row / 16384 keeps FP16 far from overflow
+        __shared__ float red[32];
+        float m = 0.0f;
+        for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(buf[rbase - j].x));
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((tid & 31) == 0) red[tid >> 5] = m;
+        __syncthreads();
+        if (tid < 32) {
+            m = (tid < (NT >> 5)) ? red[tid] : 0.0f;
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (tid == 0) red[0] = m;
+        }
+        __syncthreads();
+        const float amax = red[0] * inv_n * 100.0f;
+        const float scale = amax > 0.0f ? amax / 16384.0f : 1.0f;
+        const float rs = 1.0f / scale;
+        if (tid == 0) p.row_scale[job.dst] = scale;
+        if (p.mode == RV_MODE_LIN_F16) {
+            __half* row = static_cast<__half*>(p.rows16) + (size_t)job.dst * p.row_stride;
+            for (int j = tid; j < ixdimp; j += NT)
+                row[j] = __float2half_rn(buf[rbase - j].x * inv_n * 100.0f * rs);
+        } else {
+            __nv_bfloat16* row = static_cast<__nv_bfloat16*>(p.rows16) + (size_t)job.dst * p.row_stride;
+            for (int j = tid; j < ixdimp; j += NT)
+                row[j] = __float2bfloat16_rn(buf[rbase - j].x * inv_n * 100.0f * rs);
+        }
+    }
+}
+
+cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {
+    if (p.njobs <= 0) return cudaSuccess;
+    const int n = p.d.ndim, half = n / 2;
+    const int nt = half < 512 ? half : 512;
+    const int bpt = half / nt;
+    const size_t smem = (size_t)n * sizeof(float2) + (size_t)half * sizeof(float2) +
+                        (((size_t)p.d.ixdim * sizeof(short) + 15) & ~(size_t)15);
+    cudaError_t e = cudaSuccess;
+    auto go = [&](auto kern) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return;
+        kern<<<p.njobs, nt, smem, s>>>(p);
+        e = cudaGetLastError();
+    };
+    switch (bpt) {
+    case 1: go(k_filter<1>); break;
+    case 2: go(k_filter<2>); break;
+    case 4: go(k_filter<4>); break;
+    case 8: go(k_filter<8>); break;
+    case 16: go(k_filter<16>); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return e;
+}
+
+// ---------------------------------------------------------------------------------------------
+// R8 (REF): pixel-tile back-projection with the reference's fixed-point table.
+//
+// CTA = 64x64 pixel tile of one slice, 256 threads, 4x4 pixels per thread (strided by 16 so a
+// warp covers an 8x4 pixel block per register -> 32 lanes read nearby table entries).
+// Views are processed in chunks of VC; for each view the CTA stages the window of the view's
+// int table that its tile can touch (<= 1456 ints) into shared memory with cp.async (zero-fill
+// outside [0, 16*ixdimp)), double-buffered so the next chunk streams in during compute.
+// Per pixel and view (source/general.cpp:2150-2156):
+//      fx  = fl(fl(ix*fcos) + fl(fl(iy*fsin) + foffset));   ix0 = (int)fx;   acc += igp[ix0]
+// The two products are per column / per row and are tabulated per chunk.  Truncation: when
+// every fx of the (tile, view) is >= 0 the exact floor comes from one round-toward-zero add of
+// 2^23 (FP32 pipe) whose bit pattern is the index; otherwise cvt.rzi (F2I) is used so that
+// fx in (-1, 0) still maps to entry 0 as in the reference.  Entries outside the table are zeros
+// in the window, which implements the reference's two range checks without a branch.
+// ---------------------------------------------------------------------------------------------
+constexpr int BP_T = 64;        // tile edge
+constexpr int BP_THREADS = 256;
+constexpr int BP_WIN = 1456;    // ints per view window (>= 63*16*sqrt(2) + margins, 16B multiple)
+constexpr unsigned kMagicBits = 0x4B000000u;  // bit pattern of 2^23
+
+struct ViewMeta { int lo; int nwin4; int fast; int pad; };
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ int lds_s32(unsigned addr) {
+    int v;
+    asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ void cp_async16(unsigned dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
+
+template <int VC, bool CHECKED>
+__global__ void __launch_bounds__(BP_THREADS, 2) k_bp_ref(BackprojLaunch p) {
+    extern __shared__ __align__(16) int smi[];
+    int* win = smi;                                                   // [2][VC][BP_WIN]
+    float* xs = reinterpret_cast<float*>(win + 2 * VC * BP_WIN);      // [3][VC][64]
+    float* ys = xs + 3 * VC * 64;                                     // [3][VC][64]
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * 64);   // [3][VC]
+
+    const int ixdimp = p.ixdimp;
+    const int tiles_x = (ixdimp + BP_T - 1) / BP_T;
+    const int X0 = (blockIdx.x % tiles_x) * BP_T;
+    const int Y0 = (blockIdx.x / tiles_x) * BP_T;
+    const int slice = blockIdx.y;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = (warp & 1) * 8 + (lane & 7);
+    const int ty = (warp >> 1) * 4 + (lane >> 3);
+    const int* tab = p.table + (size_t)slice * p.slice_table_stride;
+    const int N16 = 16 * ixdimp;
+    const int nviews = p.nviews;
+    const int nchunks = (nviews + VC - 1) / VC;
+    unsigned viol = 0;
+
+    // per-view window + tabulated products for chunk c into meta/xs/ys slot ms
+    auto prepare = [&](int c, int ms) {
+        const int v0 = c * VC;
+        if (tid < VC && v0 + tid < nviews) {
+            const float4 g = __ldg(p.geom + v0 + tid);
+            float lo = 3.0e38f, hi = -3.0e38f;
+#pragma unroll
+            for (int cy = 0; cy < 2; cy++) {
+                const float fy = fadd(fmul((float)(Y0 + cy * (BP_T - 1)), g.y), g.z);
+#pragma unroll
+                for (int cx = 0; cx < 2; cx++) {
+                    const float fx = fadd(fmul((float)(X0 + cx * (BP_T - 1)), g.x), fy);
+                    lo = fminf(lo, fx);
+                    hi = fmaxf(hi, fx);
+                }
+            }
+            ViewMeta m;
+            const int ilo = (int)floorf(lo) - 2;
+            m.lo = ilo & ~3;
+            const int ihi = (int)floorf(hi) + 3;
+            int nwin = ihi - m.lo;
+            nwin = (nwin + 3) & ~3;
+            if (nwin > BP_WIN) nwin = BP_WIN;
+            m.nwin4 = nwin >> 2;
+            m.fast = (lo >= 2.0f) ? 1 : 0;
+            m.pad = 0;
+            meta[ms * VC + tid] = m;
+        }
+        for (int e = tid; e < VC * 128; e += BP_THREADS) {
+            const int vv = e >> 7, w = e & 127;
+            if (v0 + vv >= nviews) continue;
+            const float4 g = __ldg(p.geom + v0 + vv);
+            if (w < 64) {
+                const int x = X0 + (w >> 2) + 16 * (w & 3);
+                xs[(ms * VC + vv) * 64 + w] = fmul((float)x, g.x);
+            } else {
+                const int ww = w - 64;
+                const int y = Y0 + (ww >> 2) + 16 * (ww & 3);
+                ys[(ms * VC + vv) * 64 + ww] = fadd(fmul((float)y, g.y), g.z);
+            }
+        }
+    };
+    // cp.async of the windows of chunk c (meta slot ms) into window buffer wb
+    auto stage = [&](int c, int ms, int wb) {
+        const int v0 = c * VC;
+        for (int vv = 0; vv < VC; vv++) {
+            if (v0 + vv >= nviews) break;
+            const ViewMeta m = meta[ms * VC + vv];
+            const int* src = tab + (size_t)(v0 + vv) * p.table_stride;
+            int* dst = win + (wb * VC + vv) * BP_WIN;
+            for (int e = tid; e < m.nwin4; e += BP_THREADS) {
+                const int g = m.lo + 4 * e;
+                const bool in = (g >= 0) && (g + 4 <= N16);
+                cp_async16(smem_u32(dst + 4 * e), in ? (const void*)(src + g) : (const void*)src, in ? 16 : 0);
+            }
+        }
+    };
+
+    int acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[r][c] = 0;
+
+    prepare(0, 0);
+    if (nchunks > 1) prepare(1, 1);
+    __syncthreads();
+    stage(0, 0, 0);
+    cp_async_commit();
+
+    for (int k = 0; k < nchunks; k++) {
+        const int wb = k & 1, ms = k % 3;
+        if (k + 1 < nchunks) {
+            stage(k + 1, (k + 1) % 3, wb ^ 1);
+            cp_async_commit();
+        }
+        if (k + 2 < nchunks) prepare(k + 2, (k + 2) % 3);
+        if (k + 1 < nchunks) cp_async_wait<1>(); else cp_async_wait<0>();
+        __syncthreads();
+        const int nv = min(VC, nviews - k * VC);
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[ms * VC + vv];
+            const float4 xa = *reinterpret_cast<const float4*>(xs + (ms * VC + vv) * 64 + tx * 4);
+            const float4 ya = *reinterpret_cast<const float4*>(ys + (ms * VC + vv) * 64 + ty * 4);
+            const float xv[4] = {xa.x, xa.y, xa.z, xa.w};
+            const float yv[4] = {ya.x, ya.y, ya.z, ya.w};
+            const unsigned wbase = smem_u32(win + (wb * VC + vv) * BP_WIN);
+            if (m.fast) {
+                const unsigned base = wbase - 4u * (unsigned)m.lo - 4u * kMagicBits;
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const float fx = fadd(xv[c], yv[r]);
+                        const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
+                        if (CHECKED) {
+                            const int idx = (int)(bits - kMagicBits) - m.lo;
+                            if (fx < 0.0f || idx < 0 || idx >= 4 * m.nwin4) { viol++; continue; }
+                        }
+                        acc[r][c] += lds_s32(base + 4u * bits);
+                    }
+            } else {
+                const unsigned base = wbase - 4u * (unsigned)m.lo;
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const float fx = fadd(xv[c], yv[r]);
+                        const int ix0 = __float2int_rz(fx);
+                        if (CHECKED) {
+                            const int idx = ix0 - m.lo;
+                            if (idx < 0 || idx >= 4 * m.nwin4) { viol++; continue; }
+                        }
+                        acc[r][c] += lds_s32(base + 4u * (unsigned)ix0);
+                    }
+            }
+        }
+        __syncthreads();
+    }
+    if (CHECKED && viol) atomicAdd(p.status, viol);
+
+    int* out = static_cast<int*>(p.out) + (size_t)slice * p.out_slice_stride;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int y = Y0 + ty + 16 * r;
+        if (y >= ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int x = X0 + tx + 16 * c;
+            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// R8' (LIN): the same tiling with true linear interpolation of the filtered row at the FP32
+// detector coordinate u = ix*cos + iy*(-sin) + off (detector-pixel units) and FP32
+// accumulation.  The window holds (r[j], r[j+1]-r[j]) pairs so one 64-bit shared load feeds
+// one FMA; FP16/BF16 rows are expanded to FP32 pairs while staging (per-row scale applied).
+// ---------------------------------------------------------------------------------------------
+constexpr int LIN_WIN = 128;    // detector pixels per view window (>= 63*sqrt(2) + margins)
+
+template <int VC, int MODE>
+__global__ void __launch_bounds__(BP_THREADS, 2) k_bp_lin(BackprojLaunch p) {
+    __shared__ __align__(16) float2 win[VC][LIN_WIN];
+    __shared__ __align__(16) float xs[VC][64];
+    __shared__ __align__(16) float ys[VC][64];
+    __shared__ int los[VC];
+
+    const int ixdimp = p.ixdimp;
+    const int tiles_x = (ixdimp + BP_T - 1) / BP_T;
+    const int X0 = (blockIdx.x % tiles_x) * BP_T;
+    const int Y0 = (blockIdx.x / tiles_x) * BP_T;
+    const int slice = blockIdx.y;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = (warp & 1) * 8 + (lane & 7);
+    const int ty = (warp >> 1) * 4 + (lane >> 3);
+    const int nviews = p.nviews;
+    float acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[r][c] = 0.0f;
+
+    for (int v0 = 0; v0 < nviews; v0 += VC) {
+        const int nv = min(VC, nviews - v0);
+        if (tid < nv) {
+            const float4 g = __ldg(p.geom + v0 + tid);
+            float lo = 3.0e38f;
+#pragma unroll
+            for (int cy = 0; cy < 2; cy++)
+#pragma unroll
+                for (int cx = 0; cx < 2; cx++)
+                    lo = fminf(lo, fmaf((float)(X0 + cx * (BP_T - 1)), g.x, fmaf((float)(Y0 + cy * (BP_T - 1)), g.y, g.z)));
+            los[tid] = (int)floorf(lo) - 2;
+        }
+        for (int e = tid; e < VC * 128; e += BP_THREADS) {
+            const int vv = e >> 7, w = e & 127;
+            if (vv >= nv) continue;
+            const float4 g = __ldg(p.geom + v0 + vv);
+            if (w < 64) xs[vv][w] = (float)(X0 + (w >> 2) + 16 * (w & 3)) * g.x;
+            else {
+                const int ww = w - 64;
+                ys[vv][ww] = fmaf((float)(Y0 + (ww >> 2) + 16 * (ww & 3)), g.y, g.z);
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < VC * LIN_WIN; e += BP_THREADS) {
+            const int vv = e / LIN_WIN, w = e - vv * LIN_WIN;
+            if (vv >= nv) continue;
+            // pair j: (r[j], r[j+1] - r[j]) for 0 <= j < ixdimp, slope 0 at the last sample
+            // (source/general.cpp:2132-2133); zero outside the detector.
+            const int j = los[vv] + w;
+            const size_t rb = (size_t)slice * p.slice_row_stride + (size_t)(v0 + vv) * p.row_stride;
+            float r0 = 0.0f, r1 = 0.0f;
+            if (j >= 0 && j < ixdimp) {
+                const int j1 = (j + 1 < ixdimp) ? j + 1 : j;
+                if (MODE == RV_MODE_LIN) {
+                    const float* row = p.rows + rb;
+                    r0 = __ldg(row + j);
+                    r1 = __ldg(row + j1);
+                } else {
+                    const float sc = __ldg(p.row_scale + (size_t)slice * p.nviews + v0 + vv);
+                    if (MODE == RV_MODE_LIN_F16) {
+                        const __half* row = static_cast<const __half*>(p.rows16) + rb;
+                        r0 = __half2float(row[j]) * sc;
+                        r1 = __half2float(row[j1]) * sc;
+                    } else {
+                        const __nv_bfloat16* row = static_cast<const __nv_bfloat16*>(p.rows16) + rb;
+                        r0 = __bfloat162float(row[j]) * sc;
+                        r1 = __bfloat162float(row[j1]) * sc;
+                    }
+                }
+            }
+            win[vv][w] = make_float2(r0, r1 - r0);
+        }
+        __syncthreads();
+        for (int vv = 0; vv < nv; vv++) {
+            const float4 xa = *reinterpret_cast<const float4*>(&xs[vv][tx * 4]);
+            const float4 ya = *reinterpret_cast<const float4*>(&ys[vv][ty * 4]);
+            const float xv[4] = {xa.x, xa.y, xa.z, xa.w};
+            const float yv[4] = {ya.x, ya.y, ya.z, ya.w};
+            const float flo = (float)los[vv];
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float u = xv[c] + yv[r] - flo;   // >= 0 inside the window
+                    const float fl = floorf(u);
+                    const int j = (int)fl;
+                    const float f = u - fl;
+                    const float2 w2 = win[vv][min(j, LIN_WIN - 1)];
+                    acc[r][c] += fmaf(f, w2.y, w2.x);
+                }
+        }
+        __syncthreads();
+    }
+    float* out = static_cast<float*>(p.out) + (size_t)slice * p.out_slice_stride;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int y = Y0 + ty + 16 * r;
+        if (y >= ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int x = X0 + tx + 16 * c;
+            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+        }
+    }
+}
+
+template <int VC>
+static size_t bp_ref_smem() {
+    return (size_t)2 * VC * BP_WIN * sizeof(int) + (size_t)2 * 3 * VC * 64 * sizeof(float) +
+           (size_t)3 * VC * sizeof(ViewMeta);
+}
+
+// Validation mode (RvSetCheckedBackprojection): the REF kernel is replaced by its bounds-checked
+// twin, which skips and counts every table index outside the staged window.
+static int g_checked = 0;
+static unsigned int* g_status = nullptr;
+static unsigned long long g_violations = 0;
+
+}  // namespace rv
+
+extern "C" int RvSetCheckedBackprojection(int enable) {
+    if (enable && !rv::g_status) {
+        if (cudaMalloc(&rv::g_status, sizeof(unsigned int)) != cudaSuccess) return RV_ERR_DEVICE_OOM;
+    }
+    rv::g_checked = enable ? 1 : 0;
+    rv::g_violations = 0;
+    return 0;
+}
+extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
+
+namespace rv {
+
+cudaError_t launch_backproject(const BackprojLaunch& pin, cudaStream_t s) {
+    BackprojLaunch p = pin;
+    if (g_checked && p.mode == RV_MODE_REF) {
+        p.checked = 1;
+        p.status = g_status;
+        cudaError_t e = cudaMemsetAsync(g_status, 0, sizeof(unsigned int), s);
+        if (e != cudaSuccess) return e;
+    }
+    if (p.nslices <= 0) return cudaSuccess;
+    if (p.ixdimp > kMaxIxdimp) return cudaErrorInvalidValue;
+    const int tiles = ((p.ixdimp + BP_T - 1) / BP_T) * ((p.ixdimp + BP_T - 1) / BP_T);
+    dim3 grid(tiles, p.nslices);
+    cudaError_t e = cudaSuccess;
+    if (p.mode == RV_MODE_REF) {
+        constexpr int VC = 8;
+        const size_t smem = bp_ref_smem<VC>();
+        auto go = [&](auto kern) {
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return;
+            kern<<<grid, BP_THREADS, smem, s>>>(p);
+            e = cudaGetLastError();
+        };
+        if (p.checked && p.status) {
+            go(k_bp_ref<VC, true>);
+            unsigned int v = 0;
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&v, p.status, sizeof(v), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            g_violations += v;
+        } else {
+            go(k_bp_ref<VC, false>);
+        }
+        return e;
+    }
+    constexpr int VC = 8;
+    switch (p.mode) {
+    case RV_MODE_LIN: k_bp_lin<VC, RV_MODE_LIN><<<grid, BP_THREADS, 0, s>>>(p); break;
+    case RV_MODE_LIN_F16: k_bp_lin<VC, RV_MODE_LIN_F16><<<grid, BP_THREADS, 0, s>>>(p); break;
+    case RV_MODE_LIN_BF16: k_bp_lin<VC, RV_MODE_LIN_BF16><<<grid, BP_THREADS, 0, s>>>(p); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+int kernel_launches_per_filter() { return 1; }
+
+}  // namespace rv
+
+// ---------------------------------------------------------------------------------------------
+// Throughput probes for the roofline denominators of the back-projection (an FP32/conversion-
+// issue-bound kernel): FP32 FMA rate and float->int conversion rate of the whole device.
+// ---------------------------------------------------------------------------------------------
+namespace rv {
+__global__ void k_probe_fma(float* sink, int iters) {
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = threadIdx.x * 1e-3f + k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = fmaf(a[k], 0.9999f, 1e-3f);
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += a[k];
+    if (s == 1234.5f) sink[0] = s;
+}
+__global__ void k_probe_f2i(int* sink, int iters) {
+    float x[8];
+    int acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { x[k] = threadIdx.x + k * 3.7f; acc[k] = 0; }
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            acc[k] += __float2int_rz(x[k]);
+            x[k] = __fadd_rn(x[k], 1.25f);
+        }
+    }
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += acc[k];
+    if (s == 123457) sink[0] = s;
+}
+}  // namespace rv
+
+extern "C" int RvProbeThroughput(double* out, int n) {
+    if (!out || n < 2) return RV_ERR_BAD_ARGUMENT;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* sink = nullptr;
+    if (cudaMalloc(&sink, 64) != cudaSuccess) return RV_ERR_DEVICE_OOM;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 4, threads = 512, iters = 4096;
+    double res[2] = {0, 0};
+    for (int which = 0; which < 2; which++) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 4; rep++) {
+            cudaEventRecord(e0);
+            if (which == 0) rv::k_probe_fma<<<blocks, threads>>>((float*)sink, iters);
+            else rv::k_probe_f2i<<<blocks, threads>>>((int*)sink, iters);
+            cudaEventRecord(e1);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && ms < best) best = ms;
+        }
+        const double ops = (double)blocks * threads * iters * 8;
+        res[which] = which == 0 ? 2.0 * ops / (best * 1e-3) / 1e12 : ops / (best * 1e-3) / 1e9;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    out[0] = res[0];  // FP32 FMA TFLOP/s
+    out[1] = res[1];  // float->int32 conversions, G/s
+    return cudaGetLastError() == cudaSuccess ? 0 : RV_ERR_LAUNCH;
+}

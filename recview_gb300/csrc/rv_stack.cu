@@ -1,0 +1,329 @@
+// Fused stack path (no reference counterpart): a whole dataset's raw uint16 frames for many
+// detector rows -> normalised -> filtered -> back-projected slices, in a few launches.
+//
+// HBM layout (one stack, nslices slices of ixdimp^2, V back-projected views, W = ixdim):
+//   raw      [(nframes+1) * nslices * W] uint16   the reference's sinogram buffer order
+//   table    [batch * V * 16 * ixdimp]   int32    REF: 1/16 sub-sample tables, slice-major
+//   rows     [batch * V * ixdimp]        f32/f16/bf16 LIN: filtered rows x100 (+ per-row scale)
+//   out      [nslices * ixdimp^2]        int32 (REF) / f32 (LIN)
+// Slices are processed in batches so the tables stay within a device-memory budget
+// (RV_TABLE_BUDGET_MB, default 8192).
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "rv_internal.h"
+
+using namespace rv;
+
+struct RvStack {
+    RvStackDesc desc{};
+    Dims d{};
+    int device = 0;
+    int nviews = 0;                 // back-projected (SAMPLE) views
+    int batch = 1;                  // slices per filter/back-projection batch
+    std::vector<float> filt;
+    std::vector<RowJob> jobs;       // slice-major: jobs[s * nviews + v]
+    std::vector<float4> geom_ref, geom_lin;
+    void* d_jobs = nullptr;
+    void* d_geom = nullptr;
+    void* d_filt = nullptr;
+    void* d_tw = nullptr;
+    void* d_table = nullptr;        // REF tables or LIN rows
+    void* d_scale = nullptr;
+    void* d_in = nullptr;           // RunHost staging
+    void* d_out = nullptr;
+    size_t in_bytes = 0, out_bytes = 0;
+    cudaEvent_t ev[6] = {};
+    int nbatches_last = 0;
+    float t_filter = 0, t_bp = 0, t_total = 0;
+    int launches = 0;
+};
+
+static void stack_free(RvStack* st) {
+    void* bufs[] = {st->d_jobs, st->d_geom, st->d_filt, st->d_tw, st->d_table, st->d_scale, st->d_in, st->d_out};
+    for (void* p : bufs)
+        if (p) cudaFree(p);
+    for (cudaEvent_t& e : st->ev)
+        if (e) cudaEventDestroy(e);
+}
+
+extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
+    if (!desc || !out || !desc->bInc || !desc->fdeg || !desc->fFilter || desc->nframes < 1 || desc->nslices < 1 ||
+        desc->ixdim < 4 || (!desc->input_is_sinogram && !desc->fexp) || desc->mode < RV_MODE_REF ||
+        desc->mode > RV_MODE_LIN_BF16) {
+        set_error(RV_ERR_BAD_ARGUMENT, "RvStackCreate: invalid description");
+        return RV_ERR_BAD_ARGUMENT;
+    }
+    RvStack* st = new RvStack();
+    st->desc = *desc;
+    st->d = make_dims(desc->ixdim, desc->iInterpolation);
+    const Dims& d = st->d;
+    if (d.ndimp > kMaxNdimp || d.ixdimp > kMaxIxdimp) {
+        delete st;
+        set_error(RV_ERR_UNSUPPORTED, "RvStackCreate: ixdim*zoom beyond 16384");
+        return RV_ERR_UNSUPPORTED;
+    }
+    cudaGetDevice(&st->device);
+    const int nf = desc->nframes, S = desc->nslices;
+    const char* bInc = desc->bInc;
+    // ---- views and their flats (GenerateSinogramThread bracketing, source/general.cpp:2415-2447)
+    std::vector<int> views;
+    std::vector<int> vi0, vi1;
+    std::vector<float> vt0;
+    std::vector<int> vzero;
+    int i0 = -1, i1 = -1;
+    for (int i = 0; i < nf; i++) {
+        if (bInc[i] & RV_BINC_NOUSE) continue;
+        if (!(bInc[i] & RV_BINC_SAMPLE)) { i0 = i; break; }
+    }
+    for (int i = 0; i < nf; i++) {
+        if ((bInc[i] & RV_BINC_NOUSE) && !(bInc[i] & RV_BINC_SAMPLE)) continue;
+        if (!(bInc[i] & RV_BINC_SAMPLE)) { i0 = i; i1 = -1; continue; }
+        if (!desc->input_is_sinogram) {
+            if (i1 < 0) {
+                for (int j = i; j < nf; j++) {
+                    if (bInc[j] & RV_BINC_SAMPLE) continue;
+                    i1 = j;
+                    break;
+                }
+                if (i1 < 0 && i0 >= 0) i1 = i0;
+            }
+            if (i0 < 0 || i1 < 0) {
+                delete st;
+                set_error(RV_ERR_BAD_ARGUMENT, "RvStackCreate: a sample frame has no flat frame");
+                return RV_ERR_BAD_ARGUMENT;
+            }
+        }
+        // back-projection selection (source/general.cpp:2087-2102)
+        if (desc->dReconFlags & (RV_RQFLAGS_USEONLYEVENFRAMES | RV_RQFLAGS_USEONLYODDFRAMES)) {
+            if (i & 1) {
+                if (desc->dReconFlags & RV_RQFLAGS_USEONLYEVENFRAMES) continue;
+            } else {
+                if (desc->dReconFlags & RV_RQFLAGS_USEONLYODDFRAMES) continue;
+            }
+        }
+        float t0 = 0.0f;
+        if (!desc->input_is_sinogram) {
+            t0 = desc->fexp[i0];
+            const float t1 = desc->fexp[i1], ti = desc->fexp[i];
+            if (t0 == t1) t0 = 0;
+            else t0 = (ti - t0) / (t1 - t0);
+        }
+        views.push_back(i);
+        vi0.push_back(i0);
+        vi1.push_back(i1);
+        vt0.push_back(t0);
+        vzero.push_back((bInc[i] & RV_BINC_SKIP) ? 1 : 0);
+    }
+    st->nviews = (int)views.size();
+    const int V = st->nviews;
+    if (V == 0) {
+        delete st;
+        set_error(RV_ERR_BAD_ARGUMENT, "RvStackCreate: no sample frames");
+        return RV_ERR_BAD_ARGUMENT;
+    }
+    // ---- geometry: REF in 1/16 units (reference order), LIN in detector pixels (from FP64) ----
+    st->geom_ref.resize(V);
+    st->geom_lin.resize(V);
+    const double cen_lin = (double)d.ixdimh + (desc->center - (int)desc->center) * d.iIntpDim;
+    for (int v = 0; v < V; v++) {
+        float fc, fs, fo;
+        view_geometry(d, desc->center, desc->fdeg[views[v]], desc->fTiltAngle, &fc, &fs, &fo);
+        st->geom_ref[v] = make_float4(fc, fs, fo, 0.0f);
+        const double th = (double)(desc->fdeg[views[v]] + desc->fTiltAngle) * (3.14159265358979323846 / 180.0);
+        const double c = cos(th), sn = -sin(th);
+        st->geom_lin[v] = make_float4((float)c, (float)sn, (float)(cen_lin - d.ixdimh * (c + sn)), 0.0f);
+    }
+    st->filt.assign(desc->fFilter, desc->fFilter + d.ndim);
+    // ---- batch size from the table budget ----------------------------------------------------
+    size_t budget_mb = 8192;
+    if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
+    const size_t per_slice = desc->mode == RV_MODE_REF ? (size_t)V * 16 * d.ixdimp * sizeof(int)
+                                                       : (size_t)V * d.ixdimp * (desc->mode == RV_MODE_LIN ? 4 : 2);
+    size_t b = (budget_mb << 20) / (per_slice ? per_slice : 1);
+    if (b < 1) b = 1;
+    if (b > (size_t)S) b = S;
+    st->batch = (int)b;
+    // row jobs, slice-major; dst = slot inside the slice batch ((s mod batch) * V + v)
+    st->jobs.resize((size_t)S * V);
+    for (int s = 0; s < S; s++)
+        for (int v = 0; v < V; v++) {
+            RowJob j{};
+            j.src_row = views[v] * S + s;
+            j.flat0_row = vi0[v] * S + s;
+            j.flat1_row = vi1[v] * S + s;
+            j.dark_row = nf * S + s;
+            j.t0 = vt0[v];
+            j.zero = vzero[v];
+            j.dst = (s % st->batch) * V + v;
+            st->jobs[(size_t)s * V + v] = j;
+        }
+    // ---- device buffers -------------------------------------------------------------------------
+    std::vector<float2> tw;
+    fft_twiddles(d.ndimp, tw);
+    bool ok = cuda_ok(cudaMalloc(&st->d_jobs, st->jobs.size() * sizeof(RowJob)), RV_ERR_DEVICE_OOM, "jobs") &&
+              cuda_ok(cudaMalloc(&st->d_geom, (size_t)V * sizeof(float4)), RV_ERR_DEVICE_OOM, "geometry") &&
+              cuda_ok(cudaMalloc(&st->d_filt, (size_t)d.ndim * sizeof(float)), RV_ERR_DEVICE_OOM, "filter") &&
+              cuda_ok(cudaMalloc(&st->d_tw, tw.size() * sizeof(float2)), RV_ERR_DEVICE_OOM, "twiddles") &&
+              cuda_ok(cudaMalloc(&st->d_table, per_slice * st->batch), RV_ERR_DEVICE_OOM, "tables") &&
+              cuda_ok(cudaMalloc(&st->d_scale, (size_t)st->batch * V * sizeof(float)), RV_ERR_DEVICE_OOM, "scales");
+    if (ok) {
+        const std::vector<float4>& g = desc->mode == RV_MODE_REF ? st->geom_ref : st->geom_lin;
+        ok = cuda_ok(cudaMemcpy(st->d_jobs, st->jobs.data(), st->jobs.size() * sizeof(RowJob), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "jobs") &&
+             cuda_ok(cudaMemcpy(st->d_geom, g.data(), (size_t)V * sizeof(float4), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "geometry") &&
+             cuda_ok(cudaMemcpy(st->d_filt, st->filt.data(), (size_t)d.ndim * sizeof(float), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "filter") &&
+             cuda_ok(cudaMemcpy(st->d_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "twiddles");
+    }
+    for (cudaEvent_t& e : st->ev)
+        if (ok) ok = cuda_ok(cudaEventCreate(&e), RV_ERR_LAUNCH, "event");
+    if (!ok) {
+        const int code = RvGetLastError();
+        stack_free(st);
+        delete st;
+        return code ? code : RV_ERR_DEVICE_OOM;
+    }
+    *out = st;
+    return 0;
+}
+
+extern "C" void RvStackDestroy(RvStack* st) {
+    if (!st) return;
+    cudaSetDevice(st->device);
+    stack_free(st);
+    delete st;
+}
+
+extern "C" size_t RvStackSliceBytes(const RvStack* st) {
+    return st ? (size_t)st->d.ixdimp * st->d.ixdimp * 4 : 0;
+}
+extern "C" size_t RvStackInputBytes(const RvStack* st) {
+    return st ? (size_t)(st->desc.nframes + 1) * st->desc.nslices * st->desc.ixdim * 2 : 0;
+}
+extern "C" int RvStackNumViews(const RvStack* st) { return st ? st->nviews : 0; }
+extern "C" int RvStackOutputDim(const RvStack* st) { return st ? st->d.ixdimp : 0; }
+
+extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, void* stream) {
+    if (!st || !d_raw || !d_out) {
+        set_error(RV_ERR_BAD_ARGUMENT, "RvStackRunDevice: NULL argument");
+        return RV_ERR_BAD_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const Dims& d = st->d;
+    const int S = st->desc.nslices, V = st->nviews, mode = st->desc.mode;
+    const long long tstride = 16LL * d.ixdimp;
+    const size_t npix = (size_t)d.ixdimp * d.ixdimp;
+    st->launches = 0;
+    float tf = 0, tb = 0;
+    cudaEventRecord(st->ev[4], s);
+    for (int s0 = 0; s0 < S; s0 += st->batch) {
+        const int nb = (S - s0) < st->batch ? (S - s0) : st->batch;
+        FilterLaunch fl{};
+        fl.src = d_raw;
+        fl.raw = st->desc.input_is_sinogram ? 0 : 1;
+        fl.pixmin = (st->desc.iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit : RV_SINOGRAM_PIXEL_MIN16bit;
+        fl.jobs = static_cast<const RowJob*>(st->d_jobs) + (size_t)s0 * V;
+        fl.njobs = nb * V;
+        fl.filt = static_cast<const float*>(st->d_filt);
+        fl.tw = static_cast<const float2*>(st->d_tw);
+        fl.mode = mode;
+        fl.d = d;
+        fl.ic = (int)st->desc.center;
+        if (mode == RV_MODE_REF) {
+            fl.table = static_cast<int*>(st->d_table);
+            fl.table_stride = tstride;
+        } else if (mode == RV_MODE_LIN) {
+            fl.rows = static_cast<float*>(st->d_table);
+            fl.row_stride = d.ixdimp;
+        } else {
+            fl.rows16 = st->d_table;
+            fl.row_scale = static_cast<float*>(st->d_scale);
+            fl.row_stride = d.ixdimp;
+        }
+        cudaEventRecord(st->ev[0], s);
+        cudaError_t e = launch_filter(fl, s);
+        if (!cuda_ok(e, RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
+        cudaEventRecord(st->ev[1], s);
+        BackprojLaunch bl{};
+        bl.table = static_cast<const int*>(st->d_table);
+        bl.rows = static_cast<const float*>(st->d_table);
+        bl.rows16 = st->d_table;
+        bl.row_scale = static_cast<const float*>(st->d_scale);
+        bl.geom = static_cast<const float4*>(st->d_geom);
+        bl.nviews = V;
+        bl.nslices = nb;
+        bl.ixdimp = d.ixdimp;
+        bl.table_stride = tstride;
+        bl.slice_table_stride = tstride * V;
+        bl.row_stride = d.ixdimp;
+        bl.slice_row_stride = (long long)d.ixdimp * V;
+        bl.out = mode == RV_MODE_REF ? (void*)(static_cast<int*>(d_out) + (size_t)s0 * npix)
+                                     : (void*)(static_cast<float*>(d_out) + (size_t)s0 * npix);
+        bl.out_slice_stride = (long long)npix;
+        bl.mode = mode;
+        e = launch_backproject(bl, s);
+        if (!cuda_ok(e, RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
+        cudaEventRecord(st->ev[2], s);
+        st->launches += 2;
+        if (cudaEventSynchronize(st->ev[2]) == cudaSuccess) {
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, st->ev[0], st->ev[1]);
+            cudaEventElapsedTime(&b, st->ev[1], st->ev[2]);
+            tf += a;
+            tb += b;
+        }
+    }
+    cudaEventRecord(st->ev[5], s);
+    cudaError_t e = cudaEventSynchronize(st->ev[5]);
+    if (!cuda_ok(e, RV_ERR_LAUNCH, "stack run")) return RV_ERR_LAUNCH;
+    float tt = 0;
+    cudaEventElapsedTime(&tt, st->ev[4], st->ev[5]);
+    st->t_filter = tf;
+    st->t_bp = tb;
+    st->t_total = tt;
+    return 0;
+}
+
+extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void* stream) {
+    if (!st || !h_raw || !h_out) {
+        set_error(RV_ERR_BAD_ARGUMENT, "RvStackRunHost: NULL argument");
+        return RV_ERR_BAD_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t in_b = RvStackInputBytes(st);
+    const size_t out_b = RvStackSliceBytes(st) * st->desc.nslices;
+    if (st->in_bytes < in_b) {
+        if (st->d_in) cudaFree(st->d_in);
+        st->d_in = nullptr;
+        st->in_bytes = 0;
+        if (!cuda_ok(cudaMalloc(&st->d_in, in_b), RV_ERR_DEVICE_OOM, "input buffer")) return RV_ERR_DEVICE_OOM;
+        st->in_bytes = in_b;
+    }
+    if (st->out_bytes < out_b) {
+        if (st->d_out) cudaFree(st->d_out);
+        st->d_out = nullptr;
+        st->out_bytes = 0;
+        if (!cuda_ok(cudaMalloc(&st->d_out, out_b), RV_ERR_DEVICE_OOM, "output buffer")) return RV_ERR_DEVICE_OOM;
+        st->out_bytes = out_b;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(st->d_in, h_raw, in_b, cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D, "raw frames"))
+        return RV_ERR_COPY_H2D;
+    int rc = RvStackRunDevice(st, st->d_in, st->d_out, stream);
+    if (rc) return rc;
+    if (!cuda_ok(cudaMemcpyAsync(h_out, st->d_out, out_b, cudaMemcpyDeviceToHost, s), RV_ERR_COPY_D2H, "slices") ||
+        !cuda_ok(cudaStreamSynchronize(s), RV_ERR_COPY_D2H, "slices"))
+        return RV_ERR_COPY_D2H;
+    return 0;
+}
+
+extern "C" int RvStackLastTimings(const RvStack* st, float* ms3) {
+    if (!st || !ms3) return RV_ERR_BAD_ARGUMENT;
+    ms3[0] = st->t_filter;
+    ms3[1] = st->t_bp;
+    ms3[2] = st->t_total;
+    return 0;
+}
+
+extern "C" int RvStackLastLaunchCount(const RvStack* st) { return st ? st->launches : 0; }

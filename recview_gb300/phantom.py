@@ -106,7 +106,7 @@ def smooth_noise(rng: np.random.Generator, shape: tuple[int, ...], sigma: float)
         sh = [1] * len(shape)
         sh[ax] = g.size
         out = out * g.reshape(sh)
-    r = np.fft.irfftn(out, s=shape)
+    r = np.fft.irfftn(out, s=shape, axes=tuple(range(len(shape))))
     return r / max(r.std(), 1e-12)
 
 

@@ -1,0 +1,117 @@
+"""Generates tests/golden/golden.npz from the reference sources compiled by oracle/build_ref.sh.
+
+Run in a checkout that has the reference (the GPU machine does not): the fixtures then pin the
+oracle restatement everywhere.  Inputs are stored with the outputs, so the fixtures do not
+depend on the phantom generator's floating-point behaviour on another platform.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+import zlib
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from recview_gb300 import abi, phantom  # noqa: E402
+from recview_gb300.build import build_oracle, build_ref  # noqa: E402
+from recview_gb300.reconst import ReconInfo, dims  # noqa: E402
+
+F32P = C.POINTER(C.c_float)
+
+# (name, ixdim, nviews, center, iInterpolation, filter kind, cutoff, flags, tilt)
+FBP_CASES = [
+    ("plain64", 64, 90, 31.5, 2, abi.FILT_SHEPP, 0.5, 0, 0.0),
+    ("ramp64_off", 64, 75, 29.3, 2, abi.FILT_RAMP, 0.5, 0, 0.0),
+    ("han48_tilt", 48, 60, 24.75, 2, abi.FILT_HAN, 0.5, 0, 0.35),
+    ("ham40_even", 40, 64, 20.2, 2, abi.FILT_HAM, 0.4, abi.RQFLAGS_USEONLYEVENFRAMES, 0.0),
+    ("parz40_odd", 40, 64, 19.9, 2, abi.FILT_PARZN, 0.5, abi.RQFLAGS_USEONLYODDFRAMES, 0.0),
+    ("zoom2_40", 40, 50, 21.6, 3, abi.FILT_SHEPP, 0.5, 0, 0.0),
+    ("zoom4_24", 24, 40, 11.3, 4, abi.FILT_RAMP, 0.5, 0, 0.0),
+    ("zoom8_12", 12, 30, 6.45, 5, abi.FILT_HAN, 0.5, 0, 0.0),
+    ("odd37", 37, 45, 17.8, 2, abi.FILT_SHEPP, 0.5, 0, 0.0),
+]
+
+
+def main() -> None:
+    ref_path = build_ref()
+    if ref_path is None:
+        raise SystemExit("reference checkout not found; fixtures can only be generated where it exists")
+    ref = C.CDLL(str(ref_path))
+    ora = C.CDLL(str(build_oracle()))
+    for f in (ref.rvref_set_filter, ora.rvo_set_filter):
+        f.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, F32P]
+    out: dict[str, np.ndarray] = {}
+    # layout of RECONST_INFO in the reference header
+    offs = (C.c_size_t * 80)()
+    n = ref.rvref_reconstinfo_layout(offs, 80)
+    out["layout"] = np.array(offs[:n], dtype=np.int64)
+    # filter tables
+    for kind in range(5):
+        for cut in (0.5, 0.35, 1.0):
+            for ndim in (64, 1024):
+                t = np.zeros(ndim, np.float32)
+                ref.rvref_set_filter(kind, cut, 3.0, ndim, t.ctypes.data_as(F32P))
+                out[f"filter_{kind}_{cut}_{ndim}"] = t
+    # FFTs
+    ref.rvref_fft.argtypes = [C.c_int, C.c_int, F32P, F32P]
+    for npow in (3, 6, 9, 12):
+        n = 1 << npow
+        rng = np.random.default_rng(100 + npow)
+        re = (rng.normal(size=n) * 100).astype(np.float32)
+        im = rng.normal(size=n).astype(np.float32)
+        out[f"fft_in_{npow}"] = np.stack([re, im])
+        for inv in (0, 1):
+            a, b = re.copy(), im.copy()
+            ref.rvref_fft(npow, inv, a.ctypes.data_as(F32P), b.ctypes.data_as(F32P))
+            out[f"fft_out_{npow}_{inv}"] = np.stack([a, b])
+    # full FBP cases
+    for name, W, V, cen, interp, kind, cut, flags, tilt in FBP_CASES:
+        sino, fdeg = phantom.sinogram_2d(zlib.crc32(name.encode()) % 1000, W, V, cen)
+        d = dims(W, interp)
+        F = np.zeros(d.ndim, np.float32)
+        ref.rvref_set_filter(kind, cut, 2.0, d.ndim, F.ctypes.data_as(F32P))
+        bInc = np.ones(V, np.int8)
+        bInc[::11] = 0
+        res = []
+        for lib, fn in ((ref, "rvref_fbp"), (ora, "rvo_reconstruct")):
+            ri = ReconInfo(sino, fdeg, bInc, center=cen, fFilter=F, iInterpolation=interp,
+                           dReconFlags=flags, tilt=tilt)
+            getattr(lib, fn)(ri.ref)
+            res.append((ri.out.copy(), int(ri.nsino[0])))
+        assert np.array_equal(res[0][0], res[1][0]), f"oracle differs from the reference on {name}"
+        out[f"fbp_{name}_sino"] = sino
+        out[f"fbp_{name}_fdeg"] = fdeg
+        out[f"fbp_{name}_binc"] = bInc
+        out[f"fbp_{name}_filter"] = F
+        out[f"fbp_{name}_out"] = res[0][0]
+        out[f"fbp_{name}_params"] = np.array([W, V, cen, interp, kind, cut, flags, tilt, res[0][1]])
+    # normalisation cases (GenerateSinogramThread)
+    for name, seed, flags, iflag in (("sino_plain", 1, 0, 0), ("sino_zernike", 2, abi.RQFLAGS_ZERNIKE, 0),
+                                     ("sino_8bit", 3, 0, abi.READTIF8bit)):
+        raw, bInc, fdeg, fexp, _ = phantom.raw_stack(seed, 48, 30, 2, 23.7, n_ellipsoids=5,
+                                                     nflat_before=2, nflat_after=2)
+        bInc = bInc.copy()
+        bInc[6] |= abi.BINC_SKIP
+        r = raw.copy()
+        ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=2,
+                       maxSinogrLen=raw.shape[0], dReconFlags=flags, iFlag=iflag)
+        ref.rvref_gen_sinogram(ri.ref)
+        out[f"{name}_raw"] = raw
+        out[f"{name}_binc"] = bInc
+        out[f"{name}_fdeg"] = fdeg
+        out[f"{name}_fexp"] = fexp
+        out[f"{name}_out"] = r
+        out[f"{name}_params"] = np.array([flags, iflag])
+    dst = Path(__file__).with_name("golden.npz")
+    np.savez_compressed(dst, **out)
+    print(f"wrote {dst} ({dst.stat().st_size} bytes, {len(out)} arrays)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,255 @@
+"""GPU parity: the CUDA library through its C ABI against the oracle (the reference CPU routine
+restated, pinned to the reference sources and golden vectors).  REF results must be
+bit-identical; LIN/FP16/BF16 results are judged against the FP64 end-to-end oracle with the
+tolerances written below."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import recview_gb300 as rv
+from recview_gb300 import abi, phantom
+from recview_gb300.reconst import ReconInfo, dims
+from tests.rvtest import fbp_case, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+# (seed, W, V, centre, iInterpolation, filter, flags, tilt)
+SLICE_CASES = [
+    (1, 512, 900, 255.5, 2, abi.FILT_SHEPP, 0, 0.0),        # the single-slice configuration
+    (2, 64, 90, 31.5, 2, abi.FILT_RAMP, 0, 0.0),
+    (3, 100, 120, 49.7, 3, abi.FILT_HAN, 0, 0.0),            # x2 zoom
+    (4, 96, 100, 50.25, 4, abi.FILT_SHEPP, 0, 0.0),          # x4 zoom
+    (5, 48, 60, 20.1, 5, abi.FILT_HAM, 0, 0.0),              # x8 zoom
+    (6, 37, 45, 17.8, 2, abi.FILT_PARZN, 0, 0.0),            # odd width, partial tile
+    (7, 200, 181, 10.4, 2, abi.FILT_SHEPP, 0, 0.0),          # centre far left: negative fx
+    (8, 200, 181, 180.6, 2, abi.FILT_SHEPP, 0, 0.0),         # centre far right
+    (9, 160, 150, 80.3, 2, abi.FILT_BUTER, abi.RQFLAGS_USEONLYEVENFRAMES, 0.7),
+    (10, 160, 150, 79.9, 2, abi.FILT_SHEPP, abi.RQFLAGS_USEONLYODDFRAMES, -1.3),
+    (11, 1000, 400, 499.3, 2, abi.FILT_SHEPP, 0, 0.0),       # not a multiple of the 64 tile
+    (12, 300, 360, 150.0, 2, abi.FILT_RAMP, 0, 0.0),         # 360 views over 180 deg, integer centre
+]
+
+
+def _gpu_slice(ri: ReconInfo, **kw) -> np.ndarray:
+    ri.reset_output()
+    return rv.reconstruct_slice(ri, **kw).copy()
+
+
+@pytest.mark.parametrize("case", SLICE_CASES, ids=lambda c: f"W{c[1]}V{c[2]}c{c[3]}z{c[4]}")
+def test_slice_bit_exact(gpu, oracle, case):
+    seed, W, V, cen, interp, kind, flags, tilt = case
+    ri = fbp_case(seed, W, V, cen, interp, kind=kind, flags=flags, tilt=tilt, skip_every=17, oracle=oracle)
+    want = oracle.reconstruct(ri, threads=8)
+    n_want = int(ri.nsino[0])
+    got = _gpu_slice(ri)
+    assert int(ri.nsino[0]) == n_want
+    assert ri.ri.iStatus != abi.RECONST_INFO_ERROR
+    assert np.array_equal(got, want), f"{np.count_nonzero(got != want)} pixels differ"
+
+
+def test_slice_full_size_bit_exact(gpu, oracle):
+    """2048-pixel detector x 1800 views (the full-scale geometry), one slice, bit-exact."""
+    ri = fbp_case(21, 2048, 1800, 1023.5 + 7.3, 2, oracle=oracle)
+    want = oracle.reconstruct(ri, threads=16)
+    got = _gpu_slice(ri, streams=True)
+    assert np.array_equal(got, want)
+
+
+def test_streams_and_repeat_calls(gpu, oracle):
+    ri = fbp_case(30, 128, 100, 63.5, oracle=oracle)
+    want = oracle.reconstruct(ri)
+    for streams in (False, True, True, False):
+        assert np.array_equal(_gpu_slice(ri, streams=streams), want)
+    rv.lib().CudaReconstResourceFree(ri.ref, False)
+    assert ri.ri.stream1 is None and ri.ri.d_p is None
+    assert np.array_equal(_gpu_slice(ri), want)
+    rv.lib().CudaReconstMemFree(ri.ref)
+
+
+def test_worker_split_sums_to_whole(gpu, oracle):
+    """iStartSino/iStepSino interleave views between workers (source/cudaReconstHost.cpp:712);
+    the host-side sum of the partial slices equals the single-worker slice.  With one GPU
+    every worker uses device 0, so the worker index is passed as idev only when it is 0."""
+    ri = fbp_case(31, 96, 120, 47.2, oracle=oracle)
+    want = oracle.reconstruct(ri)
+    total = np.zeros_like(want)
+    for w in range(3):
+        rw = fbp_case(31, 96, 120, 47.2, oracle=oracle, iStartSino=w, iStepSino=3)
+        rw.reset_output()
+        rv.lib().CudaReconstHost(rw.ref, 0, False, False)
+        assert rw.ri.iStatus != abi.RECONST_INFO_ERROR
+        total += rw.out
+    assert np.array_equal(total, want)
+
+
+def _oracle_kept(oracle, ri: ReconInfo, old_center: float) -> np.ndarray:
+    """The reference's SINOGRAMKEPT path: tables filtered at the old integer centre, geometry of
+    the new centre with foffset + 16 * (int(new) - int(old)) (source/cudaReconst.cu:222)."""
+    L = oracle.L
+    d = ri.d
+    F32P = C.POINTER(C.c_float)
+    rd = abi.RvDims(d.ixdim, d.iZooming, d.iIntpDim, d.ndimp, d.ndim, d.ixdimp, d.ixdimh, d.ihoffset)
+    L.rvo_filter_row.argtypes = [C.POINTER(abi.RvDims), C.c_double, C.POINTER(C.c_short), F32P, F32P, F32P, F32P, F32P]
+    L.rvo_row_table.argtypes = [C.c_int, F32P, C.POINTER(C.c_int)]
+    L.rvo_view_geometry.argtypes = [C.POINTER(abi.RvDims), C.c_double, C.c_float, C.c_float, F32P, F32P, F32P]
+    L.rvo_backproject_view.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), C.c_int, C.c_int]
+    tw = np.zeros(d.ndim, np.float32)
+    L.rvo_fft_twiddles(d.ndimp, tw.ctypes.data_as(F32P), tw[d.ndim // 2:].ctypes.data_as(F32P))
+    work = np.zeros(7 * d.ndim, np.float32)
+    q = np.zeros(d.ixdimp, np.float32)
+    igp = np.zeros(16 * d.ixdimp, np.int32)
+    out = np.zeros((d.ixdimp, d.ixdimp), np.int32)
+    shift = 16 * (int(ri.ri.center) - int(old_center))
+    for i in range(len(ri.fdeg)):
+        if not (ri.bInc[i] & 1):
+            continue
+        L.rvo_filter_row(C.byref(rd), old_center, ri.rowptrs[i], ri.fFilter.ctypes.data_as(F32P),
+                         tw.ctypes.data_as(F32P), tw[d.ndim // 2:].ctypes.data_as(F32P), q.ctypes.data_as(F32P),
+                         work.ctypes.data_as(F32P))
+        L.rvo_row_table(d.ixdimp, q.ctypes.data_as(F32P), igp.ctypes.data_as(C.POINTER(C.c_int)))
+        fc, fs, fo = C.c_float(), C.c_float(), C.c_float()
+        L.rvo_view_geometry(C.byref(rd), ri.ri.center, float(ri.fdeg[i]), 0.0, C.byref(fc), C.byref(fs), C.byref(fo))
+        foff = np.float32(fo.value) + np.float32(shift)
+        L.rvo_backproject_view(d.ixdimp, fc.value, fs.value, float(foff), igp.ctypes.data_as(C.POINTER(C.c_int)),
+                               out.ctypes.data_as(C.POINTER(C.c_int)), 0, d.ixdimp)
+    return out
+
+
+def test_sinogram_kept_integer_centre_shift(gpu, oracle):
+    ri = fbp_case(40, 128, 120, 63.3, oracle=oracle)
+    first = _gpu_slice(ri)
+    assert np.array_equal(first, oracle.reconstruct(ri))
+    assert ri.ri.iSinoCenter == 63
+    ri.ri.dReconFlags |= abi.RQFLAGS_SINOGRAMKEPT
+    ri.ri.center = 66.3
+    got = _gpu_slice(ri)
+    assert ri.ri.iSinoCenter == 63  # kept: the filtered views still belong to centre 63
+    assert np.array_equal(got, _oracle_kept(oracle, ri, 63.3))
+
+
+def test_empty_view_set(gpu, oracle):
+    ri = fbp_case(41, 64, 30, 31.5, oracle=oracle)
+    ri.bInc[:] = 0
+    got = _gpu_slice(ri)
+    assert not got.any() and int(ri.nsino[0]) == 0
+
+
+def test_progress_callback_abort(gpu, oracle):
+    """bReport: the hook is called every 20 views; returning true stops adding views."""
+    calls = []
+
+    def hook(ri_p, step, i, cur):
+        calls.append(i)
+        return i >= 40
+
+    cb = abi.ProgressCallback(hook)
+    rv.lib().RvSetProgressCallback(cb)
+    try:
+        ri = fbp_case(42, 64, 100, 31.5, oracle=oracle)
+        got = _gpu_slice(ri, report=True)
+    finally:
+        rv.lib().RvSetProgressCallback(abi.ProgressCallback())
+    assert calls == [0, 20, 40]
+    ri2 = fbp_case(42, 64, 100, 31.5, oracle=oracle)
+    ri2.bInc[40:] = 0
+    assert np.array_equal(got, oracle.reconstruct(ri2))
+
+
+@pytest.mark.parametrize("W,V,cen,interp", [(512, 900, 255.5, 2), (200, 181, 10.4, 2), (200, 181, 180.6, 2),
+                                            (96, 100, 50.25, 4), (1000, 400, 499.3, 2), (60, 64, 5.5, 5)])
+def test_window_bound_holds(gpu, oracle, W, V, cen, interp):
+    """The production kernel reads the staged table window without per-access checks; the
+    checked twin counts any index outside the window, and must count none."""
+    L = rv.lib()
+    assert L.RvSetCheckedBackprojection(1) == 0
+    try:
+        ri = fbp_case(50, W, V, cen, interp, oracle=oracle, tilt=0.9)
+        got = _gpu_slice(ri)
+        assert L.RvGetWindowViolations() == 0
+    finally:
+        L.RvSetCheckedBackprojection(0)
+    assert np.array_equal(got, oracle.reconstruct(ri, threads=8))
+
+
+# ---- normalisation (R1) ---------------------------------------------------------------------
+@pytest.mark.parametrize("flags,drift,iflag", [(0, None, 0), (abi.RQFLAGS_ZERNIKE, None, 0),
+                                               (abi.RQFLAGS_DRIFTPARAMS, "params", 0),
+                                               (abi.RQFLAGS_DRIFTLIST, "list", 0), (0, None, abi.READTIF8bit)])
+def test_sinogram_host_bit_exact(gpu, oracle, flags, drift, iflag):
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(60, 160, 90, 3, 79.4, n_ellipsoids=8, nflat_before=2, nflat_after=2)
+    bInc = bInc.copy()
+    bInc[10] |= abi.BINC_SKIP
+    outs = []
+    for who in ("gpu", "oracle"):
+        r = raw.copy()
+        ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=3, maxSinogrLen=raw.shape[0],
+                       dReconFlags=flags, iFlag=iflag,
+                       piDrift=(np.arange(raw.shape[0]) % 9 - 4) if drift == "list" else None)
+        if drift == "params":
+            ri.ri.drStart, ri.ri.drEnd, ri.ri.drX, ri.ri.drY = 8, 60, 9.6, -4.2
+        if who == "gpu":
+            rv.normalise(ri)
+        else:
+            oracle.generate_sinogram(ri)
+        outs.append(r)
+    assert np.array_equal(outs[0], outs[1])
+
+
+# ---- fused stack path ---------------------------------------------------------------------------
+def _stack_oracle(oracle, raw, bInc, fdeg, fexp, center, F, interp=2, flags=0):
+    """Oracle of the stack path: GenerateSinogramThread on the raw buffer, then the CPU
+    reconstruction of every slice (iOffset = slice)."""
+    r = raw.copy()
+    S = raw.shape[1]
+    ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=S, maxSinogrLen=raw.shape[0])
+    oracle.generate_sinogram(ri)
+    outs = []
+    for s in range(S):
+        rs = ReconInfo(r.view(np.int16), fdeg, bInc, center=center, fFilter=F, iInterpolation=interp,
+                       iMultiplex=S, iOffset=s, maxSinogrLen=r.shape[0] * S, nviews=raw.shape[0] - 1,
+                       dReconFlags=flags)
+        outs.append(oracle.reconstruct(rs, threads=8))
+    return np.stack(outs)
+
+
+@pytest.mark.parametrize("W,V,S,cen,interp,budget", [(256, 300, 4, 131.7, 2, None), (128, 150, 5, 60.2, 3, 1),
+                                                     (200, 181, 3, 97.9, 2, None)])
+def test_stack_ref_bit_exact(gpu, oracle, monkeypatch, W, V, S, cen, interp, budget):
+    if budget is not None:
+        monkeypatch.setenv("RV_TABLE_BUDGET_MB", str(budget))  # forces several slice batches
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(70, W, V, S, cen, n_ellipsoids=12, nflat_before=2, nflat_after=1)
+    d = dims(W, interp)
+    F = oracle.set_filter(abi.FILT_SHEPP, d.ndim)
+    st = rv.Stack(ixdim=W, nframes=raw.shape[0] - 1, nslices=S, center=cen, bInc=bInc, fdeg=fdeg, fexp=fexp,
+                  fFilter=F, iInterpolation=interp)
+    got = st.run_host(raw)
+    want = _stack_oracle(oracle, raw, bInc, fdeg, fexp, cen, F, interp)
+    st.close()
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("mode,tol", [(abi.MODE_LIN, 2e-5), (abi.MODE_LIN_F16, 1e-3), (abi.MODE_LIN_BF16, 8e-3)])
+def test_stack_lin_modes_vs_fp64(gpu, oracle, mode, tol):
+    """LIN modes: FP32 interpolation/accumulation with FP32/FP16/BF16 filtered rows; relative L2
+    error against the FP64 end-to-end oracle, inside the reconstruction circle."""
+    W, V, S, cen = 256, 300, 2, 127.6
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(80, W, V, S, cen, n_ellipsoids=12, nflat_before=1, nflat_after=1)
+    d = dims(W)
+    F = oracle.set_filter(abi.FILT_SHEPP, d.ndim)
+    st = rv.Stack(ixdim=W, nframes=raw.shape[0] - 1, nslices=S, center=cen, bInc=bInc, fdeg=fdeg, fexp=fexp,
+                  fFilter=F, mode=mode)
+    got = st.run_host(raw)
+    st.close()
+    r = raw.copy()
+    ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=S, maxSinogrLen=raw.shape[0])
+    oracle.generate_sinogram(ri)
+    yy, xx = np.mgrid[:W, :W]
+    circle = (xx - W / 2) ** 2 + (yy - W / 2) ** 2 < (0.45 * W) ** 2
+    for s in range(S):
+        rs = ReconInfo(r.view(np.int16), fdeg, bInc, center=cen, fFilter=F, iMultiplex=S, iOffset=s,
+                       maxSinogrLen=r.shape[0] * S, nviews=raw.shape[0] - 1)
+        ref64 = oracle.lin64(rs)
+        err = rel_l2(got[s][circle], ref64[circle])
+        assert err < tol, (mode, s, err)

@@ -1,0 +1,71 @@
+"""The oracle restatement against golden vectors produced by the reference's own sources
+(tests/golden/make_golden.py).  CPU only; runs everywhere, including where the reference
+checkout is absent."""
+import numpy as np
+import pytest
+
+from recview_gb300 import abi
+from recview_gb300.reconst import ReconInfo
+
+
+def test_reconst_info_layout_matches_reference(golden):
+    import ctypes as C
+    mine = [getattr(abi.RECONST_INFO, n).offset for n in abi.FIELD_ORDER] + [C.sizeof(abi.RECONST_INFO)]
+    assert list(golden["layout"]) == mine
+
+
+@pytest.mark.parametrize("kind", range(5))
+def test_filter_tables(golden, oracle, kind):
+    for cut in (0.5, 0.35, 1.0):
+        for ndim in (64, 1024):
+            want = golden[f"filter_{kind}_{cut}_{ndim}"]
+            got = oracle.set_filter(kind, ndim, cut, 3.0)
+            if kind == abi.FILT_BUTER:
+                # powf is the platform's; allow one float ulp
+                assert np.all(np.abs(got.view(np.int32) - want.view(np.int32)) <= 1)
+            else:
+                assert np.array_equal(got.view(np.int32), want.view(np.int32)), (kind, cut, ndim)
+
+
+@pytest.mark.parametrize("npow", [3, 6, 9, 12])
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_fft_bit_exact(golden, oracle, npow, inverse):
+    re, im = golden[f"fft_in_{npow}"]
+    a, b = oracle.fft(npow, inverse, re, im)
+    want = golden[f"fft_out_{npow}_{inverse}"]
+    assert np.array_equal(a.view(np.int32), want[0].view(np.int32))
+    assert np.array_equal(b.view(np.int32), want[1].view(np.int32))
+
+
+CASES = ["plain64", "ramp64_off", "han48_tilt", "ham40_even", "parz40_odd", "zoom2_40", "zoom4_24",
+         "zoom8_12", "odd37"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fbp_bit_exact(golden, oracle, name):
+    W, V, cen, interp, kind, cut, flags, tilt, nsino = golden[f"fbp_{name}_params"]
+    ri = ReconInfo(golden[f"fbp_{name}_sino"], golden[f"fbp_{name}_fdeg"], golden[f"fbp_{name}_binc"],
+                   center=float(cen), fFilter=golden[f"fbp_{name}_filter"], iInterpolation=int(interp),
+                   dReconFlags=int(flags), tilt=float(tilt))
+    out = oracle.reconstruct(ri)
+    assert int(ri.nsino[0]) == int(nsino)
+    assert np.array_equal(out, golden[f"fbp_{name}_out"])
+
+
+@pytest.mark.parametrize("name", ["sino_plain", "sino_zernike", "sino_8bit"])
+def test_normalisation_bit_exact(golden, oracle, name):
+    flags, iflag = golden[f"{name}_params"]
+    raw = golden[f"{name}_raw"].copy()
+    ri = ReconInfo(raw.view(np.int16), golden[f"{name}_fdeg"], golden[f"{name}_binc"], center=0,
+                   fexp=golden[f"{name}_fexp"], iMultiplex=raw.shape[1], maxSinogrLen=raw.shape[0],
+                   dReconFlags=int(flags), iFlag=int(iflag))
+    assert oracle.generate_sinogram(ri) == 0
+    assert np.array_equal(raw, golden[f"{name}_out"])
+
+
+def test_oracle_threads_equal_single(oracle):
+    from tests.rvtest import fbp_case
+    ri = fbp_case(7, 96, 120, 47.3, oracle=oracle)
+    one = oracle.reconstruct(ri, threads=1)
+    many = oracle.reconstruct(ri, threads=5)
+    assert np.array_equal(one, many)

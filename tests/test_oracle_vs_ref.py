@@ -1,0 +1,55 @@
+"""Randomised parity of the oracle restatement against the reference sources built here
+(oracle/build_ref.sh).  Skipped where the reference checkout is absent (e.g. on the GPU machine);
+the golden fixtures cover those machines."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from recview_gb300 import abi, phantom
+from recview_gb300.reconst import ReconInfo
+from tests.rvtest import fbp_case, ref_lib
+
+REF = ref_lib()
+pytestmark = pytest.mark.skipif(REF is None, reason="reference build not present")
+
+
+@pytest.mark.parametrize("seed,W,V,cen,interp", [
+    (0, 80, 100, 39.5, 2), (1, 77, 91, 41.2, 2), (2, 50, 64, 20.9, 3), (3, 33, 40, 16.1, 4),
+    (4, 128, 160, 70.7, 2), (5, 20, 24, 9.99, 5), (6, 64, 90, 10.4, 2), (7, 64, 90, 52.6, 2)])
+def test_fbp_random(oracle, seed, W, V, cen, interp):
+    ri = fbp_case(seed, W, V, cen, interp, skip_every=9, oracle=oracle)
+    a = oracle.reconstruct(ri)
+    ri.reset_output()
+    REF.rvref_fbp(C.byref(ri.ri))
+    assert np.array_equal(a, ri.out)
+
+
+def test_fbp_all_filters(oracle):
+    for kind in range(6):
+        ri = fbp_case(11 + kind, 48, 50, 23.4, kind=kind, oracle=oracle)
+        a = oracle.reconstruct(ri)
+        ri.reset_output()
+        REF.rvref_fbp(C.byref(ri.ri))
+        assert np.array_equal(a, ri.out), kind
+
+
+@pytest.mark.parametrize("flags,drift", [(0, None), (abi.RQFLAGS_DRIFTPARAMS, "params"),
+                                         (abi.RQFLAGS_DRIFTLIST, "list"), (abi.RQFLAGS_ZERNIKE, None)])
+def test_normalisation_random(oracle, flags, drift):
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(3, 64, 40, 3, 31.7, n_ellipsoids=5, nflat_before=2,
+                                                 nflat_after=3)
+    outs = []
+    for fn in ("ora", "ref"):
+        r = raw.copy()
+        ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=3,
+                       maxSinogrLen=raw.shape[0], dReconFlags=flags,
+                       piDrift=(np.arange(raw.shape[0]) % 7 - 3) if drift == "list" else None)
+        if drift == "params":
+            ri.ri.drStart, ri.ri.drEnd, ri.ri.drX, ri.ri.drY = 5, 30, 6.2, -2.5
+        if fn == "ora":
+            oracle.generate_sinogram(ri)
+        else:
+            REF.rvref_gen_sinogram(C.byref(ri.ri))
+        outs.append(r)
+    assert np.array_equal(outs[0], outs[1])
