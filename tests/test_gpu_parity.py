@@ -62,7 +62,7 @@ def test_streams_and_repeat_calls(gpu, oracle):
     for streams in (False, True, True, False):
         assert np.array_equal(_gpu_slice(ri, streams=streams), want)
     rv.lib().CudaReconstResourceFree(ri.ref, False)
-    assert ri.ri.stream1 is None and ri.ri.d_p is None
+    assert not ri.ri.stream1 and not ri.ri.d_p
     assert np.array_equal(_gpu_slice(ri), want)
     rv.lib().CudaReconstMemFree(ri.ref)
 
