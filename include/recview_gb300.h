@@ -284,6 +284,12 @@ int RvStackLastLaunchCount(const RvStack* st);
 int RvSetCheckedBackprojection(int enable);
 unsigned long long RvGetWindowViolations(void);
 
+/* Tuning of the REF back-projection (process-wide; affects stacks created and slices reconstructed
+ * afterwards): variant 0 = 128x128 tile / 8 views per chunk, 1 = 64x64 / 8, 2 = 128x128 / 4;
+ * pad = 1 stores 17 table words per detector pixel (fewer shared-memory bank conflicts). */
+int RvSetBackprojectionVariant(int variant, int pad);
+int RvGetBackprojectionVariant(int* variant, int* pad);
+
 /* Device throughput probes used as roofline denominators for the back-projection, which is
  * bound by instruction issue rather than HBM or tensor cores: out[0] = FP32 FMA TFLOP/s,
  * out[1] = float->int32 conversions in G/s, both measured on the current device. */

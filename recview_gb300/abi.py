@@ -185,6 +185,8 @@ PROTOTYPES = {
     "RvSetCheckedBackprojection": (C.c_int, [C.c_int]),
     "RvGetWindowViolations": (C.c_ulonglong, []),
     "RvProbeThroughput": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
+    "RvSetBackprojectionVariant": (C.c_int, [C.c_int, C.c_int]),
+    "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
 }
 
 

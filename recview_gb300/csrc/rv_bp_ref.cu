@@ -1,0 +1,414 @@
+// R8 (REF): back-projection with the reference's fixed-point 1/16 sub-sample table
+// (source/general.cpp:2147-2158), bit-identical to the reference CPU routine.
+//
+// Work decomposition.  One CTA = a TX x TY pixel tile of one slice; a warp covers an 8x4 pixel
+// block per register and each thread holds RX x RY int32 accumulators (pixels strided by the
+// warp-grid extent).  Views are processed in chunks of VC.
+//
+// Table windows.  For each view a tile can only touch table entries between the projections of
+// its corners.  Per chunk, one thread issues a TMA bulk copy (cp.async.bulk, completion on an
+// mbarrier) of each view's window from the L2/HBM-resident table into shared memory, double
+// buffered so chunk k+1 lands while chunk k is computed; parts of a window outside the table are
+// zero-filled by the CTA, which implements the reference's range checks (ix0 < 0, ix0 >= 16 N)
+// without a per-pixel branch.
+//
+// Per pixel and view:   fx  = fl(fl(ix*fcos) + fl(fl(iy*fsin) + foffset))      (tabulated terms)
+//                       idx = (int)fx;   acc += igp[idx]
+// (int)fx: when the corner bound shows fx >= 0 for the whole (tile, view), fl_rz(fx + 2^23) has
+// the bit pattern 0x4B000000 + floor(fx) (exact for 0 <= fx < 2^23), so the index comes from the
+// FP32 pipe and folds into the shared-memory address; otherwise cvt.rzi (F2I) keeps the
+// reference's truncation of fx in (-1, 0) to entry 0.
+//
+// Window bound.  |computed fx - exact affine value| <= 2^-24 (|x fcos| + |y fsin| + 2 |fx|)
+// < 0.1 for ixdimp <= 16384, and the affine value is extreme at the tile corners, so every
+// index lies in [floor(min corner) - 1, floor(max corner) + 1]; the window spans
+// [floor(min) - 2 (aligned down), floor(max) + 3).  The bounds-checked twin (CHECKED) counts any
+// index outside the window; tests run it on many geometries and require zero.
+//
+// Optional padded layout (table_pad): 17 words per detector pixel, so lanes whose indices differ
+// by ~16 (views near 0 or 90 degrees) fall into different shared-memory banks.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#include "rv_internal.h"
+
+namespace rv {
+
+__device__ unsigned int g_kernel_status = 0;   // bit 0: an mbarrier wait ran out
+
+constexpr unsigned kMagicBits = 0x4B000000u;   // bit pattern of 2^23
+
+__device__ __forceinline__ float fmulr(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float faddr(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ int lds_s32(unsigned addr) {
+    int v;
+    asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: every spin has an iteration limit (each try_wait itself blocks for a while)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+    for (int i = 0; i < (1 << 20); i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_bulk_g2s(unsigned dst, const void* src, unsigned bytes, unsigned bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+constexpr int isqrt_ceil(int n) {
+    int r = 0;
+    while (r * r < n) r++;
+    return r;
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int PAD>
+struct BpCfg {
+    static constexpr int NT = 32 * WX * WY;
+    static constexpr int GX = 8 * WX, GY = 4 * WY;        // thread grid of the tile
+    static constexpr int TX = GX * RX, TY = GY * RY;      // tile in pixels
+    static constexpr int ALIGN = PAD ? 64 : 4;            // window start alignment (table index)
+    // table-index span of a tile: 16*sqrt((TX-1)^2 + (TY-1)^2) + margins + alignment
+    static constexpr int SPAN = 16 * isqrt_ceil((TX - 1) * (TX - 1) + (TY - 1) * (TY - 1)) + 2 + 3 + ALIGN + 16;
+    static constexpr int WIN = PAD ? ((SPAN * 17 / 16 + 17 + 15) / 16) * 16 : ((SPAN + 15) / 16) * 16;
+    static constexpr size_t SMEM = (size_t)2 * VC * WIN * 4 + (size_t)3 * VC * (TX + TY) * 4 + (size_t)3 * VC * 32 + 16;
+};
+
+struct ViewMeta {
+    int w0;      // window start in table-storage words
+    int nwin;    // window length in storage words (multiple of 4)
+    int a, b;    // in-table part [a, b) of the window (storage words, multiples of 4)
+    int fast;    // 1: every fx of the tile is >= 0 (exact floor by the 2^23 add)
+    int pad0, pad1, pad2;
+};
+
+template <int WX, int WY, int RX, int RY, int VC, int PAD, bool CHECKED>
+__global__ void __launch_bounds__(32 * WX * WY, 1) k_bp_ref(BackprojLaunch p) {
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    constexpr int NT = Cfg::NT, TX = Cfg::TX, TY = Cfg::TY, WIN = Cfg::WIN;
+    extern __shared__ __align__(128) int smi[];
+    int* win = smi;                                                     // [2][VC][WIN]
+    float* xs = reinterpret_cast<float*>(win + 2 * VC * WIN);           // [3][VC][TX]
+    float* ys = xs + 3 * VC * TX;                                       // [3][VC][TY]
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * TY);     // [3][VC]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(meta + 3 * VC);        // [2]
+
+    const int ixdimp = p.ixdimp;
+    const int tiles_x = (ixdimp + TX - 1) / TX;
+    const int X0 = (blockIdx.x % tiles_x) * TX;
+    const int Y0 = (blockIdx.x / tiles_x) * TY;
+    const int slice = blockIdx.y;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = (warp % WX) * 8 + (lane & 7);
+    const int ty = (warp / WX) * 4 + (lane >> 3);
+    const int* tab = p.table + (size_t)slice * p.slice_table_stride;
+    const int nstore = PAD ? ((17 * ixdimp + 3) & ~3) : 16 * ixdimp;   // storage words per table row
+    const int nviews = p.nviews;
+    const int nchunks = (nviews + VC - 1) / VC;
+    unsigned viol = 0;
+
+    if (tid == 0) {
+        mbar_init(smem_u32(&bars[0]), 1);
+        mbar_init(smem_u32(&bars[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+
+    // window bounds and tabulated products of chunk c into meta/xs/ys slot ms
+    auto prepare = [&](int c, int ms) {
+        const int v0 = c * VC;
+        if (tid < VC && v0 + tid < nviews) {
+            const float4 g = __ldg(p.geom + v0 + tid);
+            float lo = 3.0e38f, hi = -3.0e38f;
+#pragma unroll
+            for (int cy = 0; cy < 2; cy++) {
+                const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), g.y), g.z);
+#pragma unroll
+                for (int cx = 0; cx < 2; cx++) {
+                    const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), g.x), fy);
+                    lo = fminf(lo, fx);
+                    hi = fmaxf(hi, fx);
+                }
+            }
+            const int ilo = (int)floorf(lo) - 2;
+            const int lo_a = ilo >= 0 ? (ilo & ~(Cfg::ALIGN - 1)) : -((-ilo + Cfg::ALIGN - 1) & ~(Cfg::ALIGN - 1));
+            const int ihi = (int)floorf(hi) + 3;   // exclusive
+            ViewMeta m;
+            if (PAD) {
+                const int hi16 = (ihi + 15) & ~15;
+                m.w0 = lo_a + lo_a / 16;              // 17 * lo_a / 16 (lo_a multiple of 64)
+                const int w1 = hi16 + hi16 / 16;
+                m.nwin = min(((w1 - m.w0) + 3) & ~3, WIN);
+            } else {
+                m.w0 = lo_a;
+                m.nwin = min(((ihi - lo_a) + 3) & ~3, WIN);
+            }
+            m.a = max(m.w0, 0);
+            m.b = min(m.w0 + m.nwin, nstore);
+            m.fast = (lo >= 2.0f) ? 1 : 0;
+            m.pad0 = m.pad1 = m.pad2 = 0;
+            meta[ms * VC + tid] = m;
+        }
+        for (int e = tid; e < VC * (TX + TY); e += NT) {
+            const int vv = e / (TX + TY), w = e - vv * (TX + TY);
+            if (v0 + vv >= nviews) continue;
+            const float4 g = __ldg(p.geom + v0 + vv);
+            if (w < TX) {
+                const int t = w / RX, c = w - t * RX;          // xs[t*RX + c] = column of (tx=t, c)
+                xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
+            } else {
+                const int w2 = w - TX, t = w2 / RY, r = w2 - t * RY;
+                ys[(ms * VC + vv) * TY + w2] = faddr(fmulr((float)(Y0 + t + Cfg::GY * r), g.y), g.z);
+            }
+        }
+    };
+    // issue chunk c (meta slot ms) into window buffer wb: TMA by thread 0, zero-fill by all
+    auto stage = [&](int c, int ms, int wb) {
+        const int v0 = c * VC;
+        const int nv = min(VC, nviews - v0);
+        if (tid == 0) {
+            unsigned bytes = 0;
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[ms * VC + vv];
+                if (m.b > m.a) bytes += 4u * (unsigned)(m.b - m.a);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const unsigned bar = smem_u32(&bars[wb]);
+            mbar_arrive_expect_tx(bar, bytes);
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[ms * VC + vv];
+                if (m.b <= m.a) continue;
+                const int* src = tab + (size_t)(v0 + vv) * p.table_stride + m.a;
+                const unsigned dst = smem_u32(win + (wb * VC + vv) * WIN + (m.a - m.w0));
+                tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
+            }
+        }
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[ms * VC + vv];
+            int4* w4 = reinterpret_cast<int4*>(win + (wb * VC + vv) * WIN);
+            const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;   // [0, za) zero
+            const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;   // [zb, nwin) zero
+            for (int e = tid; e < za; e += NT) w4[e] = make_int4(0, 0, 0, 0);
+            for (int e = zb + tid; e < (m.nwin >> 2); e += NT) w4[e] = make_int4(0, 0, 0, 0);
+        }
+    };
+
+    int acc[RY][RX];
+#pragma unroll
+    for (int r = 0; r < RY; r++)
+#pragma unroll
+        for (int c = 0; c < RX; c++) acc[r][c] = 0;
+
+    prepare(0, 0);
+    if (nchunks > 1) prepare(1, 1);
+    __syncthreads();
+    stage(0, 0, 0);
+
+    for (int k = 0; k < nchunks; k++) {
+        const int wb = k & 1, ms = k % 3;
+        if (k + 1 < nchunks) stage(k + 1, (k + 1) % 3, wb ^ 1);
+        if (k + 2 < nchunks) prepare(k + 2, (k + 2) % 3);
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[wb]), (unsigned)(k >> 1) & 1u);
+        if (__syncthreads_or(!ok)) {
+            // a bulk copy did not complete in time: report, give the copies a bounded last
+            // chance to land, and leave without touching the output
+            if (tid == 0) atomicOr(&g_kernel_status, 1u);
+            mbar_wait_bounded(smem_u32(&bars[wb]), (unsigned)(k >> 1) & 1u);
+            if (k + 1 < nchunks) mbar_wait_bounded(smem_u32(&bars[wb ^ 1]), (unsigned)((k + 1) >> 1) & 1u);
+            return;
+        }
+        const int nv = min(VC, nviews - k * VC);
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[ms * VC + vv];
+            float xv[RX], yv[RY];
+#pragma unroll
+            for (int c4 = 0; c4 < RX; c4 += 4) {
+                const float4 t4 = *reinterpret_cast<const float4*>(xs + (ms * VC + vv) * TX + tx * RX + c4);
+                xv[c4] = t4.x; xv[c4 + 1] = t4.y; xv[c4 + 2] = t4.z; xv[c4 + 3] = t4.w;
+            }
+#pragma unroll
+            for (int r4 = 0; r4 < RY; r4 += 4) {
+                const float4 t4 = *reinterpret_cast<const float4*>(ys + (ms * VC + vv) * TY + ty * RY + r4);
+                yv[r4] = t4.x; yv[r4 + 1] = t4.y; yv[r4 + 2] = t4.z; yv[r4 + 3] = t4.w;
+            }
+            const unsigned wbase = smem_u32(win + (wb * VC + vv) * WIN) - 4u * (unsigned)m.w0;
+            if (m.fast) {
+                // index v = bits - 2^23 pattern; PAD: storage = v + (v >> 4)
+                const unsigned base = PAD ? wbase - 4u * (kMagicBits + (kMagicBits >> 4)) : wbase - 4u * kMagicBits;
+#pragma unroll
+                for (int r = 0; r < RY; r++)
+#pragma unroll
+                    for (int c = 0; c < RX; c++) {
+                        const float fx = faddr(xv[c], yv[r]);
+                        const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
+                        const unsigned st = PAD ? bits + (bits >> 4) : bits;
+                        if (CHECKED) {
+                            const int v = (int)(bits - kMagicBits);
+                            const int sw = PAD ? v + (v >> 4) : v;
+                            if (fx < 0.0f || sw < m.w0 || sw >= m.w0 + m.nwin) { viol++; continue; }
+                        }
+                        acc[r][c] += lds_s32(base + 4u * st);
+                    }
+            } else {
+#pragma unroll
+                for (int r = 0; r < RY; r++)
+#pragma unroll
+                    for (int c = 0; c < RX; c++) {
+                        const float fx = faddr(xv[c], yv[r]);
+                        const int v = __float2int_rz(fx);
+                        const int sw = PAD ? v + (v >> 4) : v;
+                        if (CHECKED) {
+                            if (sw < m.w0 || sw >= m.w0 + m.nwin) { viol++; continue; }
+                        }
+                        acc[r][c] += lds_s32(wbase + 4u * (unsigned)sw);
+                    }
+            }
+        }
+        __syncthreads();
+    }
+    if (CHECKED && viol) atomicAdd(p.status_counter, viol);
+
+    int* out = static_cast<int*>(p.out) + (size_t)slice * p.out_slice_stride;
+#pragma unroll
+    for (int r = 0; r < RY; r++) {
+        const int y = Y0 + ty + Cfg::GY * r;
+        if (y >= ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < RX; c++) {
+            const int x = X0 + tx + Cfg::GX * c;
+            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+        }
+    }
+}
+
+// ---- configuration ---------------------------------------------------------------------------
+// Variants (RV_BP_VARIANT, for tuning; the default is the measured best):
+//   0: 128x128 tile, 512 threads, 4x8 px/thread, 8 views/chunk
+//   1: 64x64 tile, 256 threads, 4x4 px/thread, 8 views/chunk
+//   2: 128x128 tile, 512 threads, 4x8 px/thread, 4 views/chunk
+static int env_int(const char* name, int dflt) {
+    const char* e = getenv(name);
+    return e ? atoi(e) : dflt;
+}
+static int g_variant = -1, g_pad = -1;
+static void load_defaults() {
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 0);
+    if (g_pad < 0) g_pad = env_int("RV_BP_PAD", 0) ? 1 : 0;
+}
+int ref_table_pad() {
+    load_defaults();
+    return g_pad;
+}
+long long ref_table_stride(int ixdimp, int pad) {
+    return pad ? (((long long)17 * ixdimp + 15) & ~15LL) : 16LL * ixdimp;
+}
+
+static int g_checked = 0;
+static unsigned int* g_counter = nullptr;
+static unsigned long long g_violations = 0;
+
+template <int WX, int WY, int RX, int RY, int VC, int PAD>
+static cudaError_t go_bp(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
+    dim3 grid(tiles, p.nslices);
+    cudaError_t e;
+    if (checked) {
+        auto kern = k_bp_ref<WX, WY, RX, RY, VC, PAD, true>;
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+        if (e == cudaSuccess) {
+            kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(p);
+            e = cudaGetLastError();
+        }
+    } else {
+        auto kern = k_bp_ref<WX, WY, RX, RY, VC, PAD, false>;
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+        if (e == cudaSuccess) {
+            kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(p);
+            e = cudaGetLastError();
+        }
+    }
+    return e;
+}
+
+template <int PAD>
+static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool checked, int variant) {
+    switch (variant) {
+    case 1: return go_bp<2, 4, 4, 4, 8, PAD>(p, s, checked);
+    case 2: return go_bp<4, 4, 4, 8, 4, PAD>(p, s, checked);
+    default: return go_bp<4, 4, 4, 8, 8, PAD>(p, s, checked);
+    }
+}
+
+cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
+    BackprojLaunch p = pin;
+    load_defaults();
+    const int variant = g_variant;
+    const bool checked = g_checked && g_counter;
+    if (checked) {
+        p.status_counter = g_counter;
+        cudaError_t e = cudaMemsetAsync(g_counter, 0, sizeof(unsigned int), s);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = p.table_pad ? dispatch_bp<1>(p, s, checked, variant) : dispatch_bp<0>(p, s, checked, variant);
+    if (checked && e == cudaSuccess) {
+        unsigned int v = 0;
+        e = cudaMemcpyAsync(&v, g_counter, sizeof(v), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        g_violations += v;
+    }
+    return e;
+}
+
+unsigned int take_kernel_status(cudaStream_t s) {
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbolAsync(&v, g_kernel_status, sizeof(v), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 0;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return 0;
+    if (v) cudaMemcpyToSymbolAsync(g_kernel_status, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s);
+    return v;
+}
+
+}  // namespace rv
+
+extern "C" int RvSetCheckedBackprojection(int enable) {
+    if (enable && !rv::g_counter) {
+        if (cudaMalloc(&rv::g_counter, sizeof(unsigned int)) != cudaSuccess) return RV_ERR_DEVICE_OOM;
+    }
+    rv::g_checked = enable ? 1 : 0;
+    rv::g_violations = 0;
+    return 0;
+}
+extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
+
+extern "C" int RvSetBackprojectionVariant(int variant, int pad) {
+    if (variant < 0 || variant > 2 || pad < 0 || pad > 1) return RV_ERR_BAD_ARGUMENT;
+    rv::g_variant = variant;
+    rv::g_pad = pad;
+    return 0;
+}
+extern "C" int RvGetBackprojectionVariant(int* variant, int* pad) {
+    rv::load_defaults();
+    if (variant) *variant = rv::g_variant;
+    if (pad) *pad = rv::g_pad;
+    return 0;
+}

@@ -125,6 +125,7 @@ struct RiContext {
     // filtered views kept for RQFLAGS_SINOGRAMKEPT (source/cudaReconstHost.cpp:658)
     bool kept = false;
     int kept_ixdim = 0, kept_interp = 0, kept_start = 0, kept_step = 0, kept_mult = 0, kept_off = 0;
+    int kept_pad = 0;
     std::vector<int> kept_views;
 
     bool stage(size_t need) {
@@ -260,8 +261,10 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
     bool bDeconv = !(ri->dReconFlags & RV_RQFLAGS_SINOGRAMKEPT) || !c->kept || d.iIntpDim != 1 ||
                    c->kept_ixdim != ri->ixdim || c->kept_interp != ri->iInterpolation ||
                    c->kept_start != ri->iStartSino || c->kept_step != ri->iStepSino ||
-                   c->kept_mult != ri->iMultiplex || c->kept_off != ri->iOffset || c->kept_views != views;
-    const size_t table_stride = (size_t)16 * ixdimp;
+                   c->kept_mult != ri->iMultiplex || c->kept_off != ri->iOffset || c->kept_views != views ||
+                   c->kept_pad != ref_table_pad();
+    const int tpad = ref_table_pad();
+    const size_t table_stride = (size_t)ref_table_stride(ixdimp, tpad);
     if (!c->out.ensure((size_t)ixdimp * ixdimp * sizeof(int))) {
         fail(ri, RV_ERR_DEVICE_OOM, "Out of CUDA device memory (slice)");
         return;
@@ -310,6 +313,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         fl.d = d;
         fl.ic = intcenter;
         fl.table_stride = (long long)table_stride;
+        fl.table_pad = tpad;
         if (!cuda_ok(launch_filter(fl, s), RV_ERR_LAUNCH, "filter kernel")) {
             ri->iStatus = RECONST_INFO_ERROR;
             return;
@@ -322,6 +326,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         c->kept_mult = ri->iMultiplex;
         c->kept_off = ri->iOffset;
         c->kept_views = views;
+        c->kept_pad = tpad;
     }
     // ---- geometry + back-projection ---------------------------------------------------------
     if (nv > 0) {
@@ -353,6 +358,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         bl.out = c->out.p;
         bl.out_slice_stride = (long long)ixdimp * ixdimp;
         bl.mode = RV_MODE_REF;
+        bl.table_pad = tpad;
         if (!cuda_ok(launch_backproject(bl, s), RV_ERR_LAUNCH, "back-projection kernel")) {
             ri->iStatus = RECONST_INFO_ERROR;
             return;
@@ -369,6 +375,10 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
                  RV_ERR_COPY_D2H, "slice copy") ||
         !cuda_ok(cudaStreamSynchronize(s), RV_ERR_LAUNCH, "slice")) {
         ri->iStatus = RECONST_INFO_ERROR;
+        return;
+    }
+    if (take_kernel_status(s)) {
+        fail(ri, RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
         return;
     }
     publish_fields(ri, c);

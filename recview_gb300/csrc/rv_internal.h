@@ -66,6 +66,7 @@ struct FilterLaunch {
     int ic;                   // (int)center
     long long table_stride;   // ints between table slots
     long long row_stride;     // elements between filtered rows
+    int table_pad;            // 1: 17 ints per detector pixel (see ref_table_pad())
 };
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
 
@@ -87,10 +88,16 @@ struct BackprojLaunch {
     long long out_slice_stride;  // elements per output slice
     int center_shift16;       // REF: 16 * integer centre offset added to foffset (R10)
     int mode;
-    int checked;              // 1: bounds-checked variant that counts window violations
-    unsigned int* status;     // device counter of violations (checked variant)
+    int table_pad;            // REF table layout (must match the filter launch)
+    unsigned int* status_counter;  // validation mode: window-violation counter (else null)
 };
 cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s);
+cudaError_t launch_bp_ref(const BackprojLaunch& p, cudaStream_t s);
+// REF table layout: 16 (dense) or 17 (padded) ints per detector pixel, and the slot stride.
+int ref_table_pad();
+long long ref_table_stride(int ixdimp, int pad);
+// status word written by kernels whose bounded waits ran out (0 = fine); read-and-clear
+unsigned int take_kernel_status(cudaStream_t s);
 
 // ---- normalisation (R1) written back as int16 rows ------------------------------------------
 struct NormLaunch {

@@ -251,11 +251,18 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
             int v[16];
 #pragma unroll
             for (int k = 0; k < 16; k++) v[k] = __float2int_rz(fadd(p0, fmul(p1p0, (float)k)));
-            int4* dst = reinterpret_cast<int4*>(tab + 16 * (size_t)j);
-            dst[0] = make_int4(v[0], v[1], v[2], v[3]);
-            dst[1] = make_int4(v[4], v[5], v[6], v[7]);
-            dst[2] = make_int4(v[8], v[9], v[10], v[11]);
-            dst[3] = make_int4(v[12], v[13], v[14], v[15]);
+            if (p.table_pad) {
+                // 17 words per detector pixel (the 17th unused): shared-memory bank spreading
+                int* dst = tab + 17 * (size_t)j;
+#pragma unroll
+                for (int k = 0; k < 16; k++) dst[k] = v[k];
+            } else {
+                int4* dst = reinterpret_cast<int4*>(tab + 16 * (size_t)j);
+                dst[0] = make_int4(v[0], v[1], v[2], v[3]);
+                dst[1] = make_int4(v[4], v[5], v[6], v[7]);
+                dst[2] = make_int4(v[8], v[9], v[10], v[11]);
+                dst[3] = make_int4(v[12], v[13], v[14], v[15]);
+            }
         }
     }
     if (p.rows) {
@@ -317,199 +324,9 @@ cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {
     return e;
 }
 
-// ---------------------------------------------------------------------------------------------
-// R8 (REF): pixel-tile back-projection with the reference's fixed-point table.
-//
-// CTA = 64x64 pixel tile of one slice, 256 threads, 4x4 pixels per thread (strided by 16 so a
-// warp covers an 8x4 pixel block per register -> 32 lanes read nearby table entries).
-// Views are processed in chunks of VC; for each view the CTA stages the window of the view's
-// int table that its tile can touch (<= 1456 ints) into shared memory with cp.async (zero-fill
-// outside [0, 16*ixdimp)), double-buffered so the next chunk streams in during compute.
-// Per pixel and view (source/general.cpp:2150-2156):
-//      fx  = fl(fl(ix*fcos) + fl(fl(iy*fsin) + foffset));   ix0 = (int)fx;   acc += igp[ix0]
-// The two products are per column / per row and are tabulated per chunk.  Truncation: when
-// every fx of the (tile, view) is >= 0 the exact floor comes from one round-toward-zero add of
-// 2^23 (FP32 pipe) whose bit pattern is the index; otherwise cvt.rzi (F2I) is used so that
-// fx in (-1, 0) still maps to entry 0 as in the reference.  Entries outside the table are zeros
-// in the window, which implements the reference's two range checks without a branch.
-// ---------------------------------------------------------------------------------------------
+// Back-projection tiling shared by the LIN kernel (the REF kernel lives in rv_bp_ref.cu).
 constexpr int BP_T = 64;        // tile edge
 constexpr int BP_THREADS = 256;
-constexpr int BP_WIN = 1456;    // ints per view window (>= 63*16*sqrt(2) + margins, 16B multiple)
-constexpr unsigned kMagicBits = 0x4B000000u;  // bit pattern of 2^23
-
-struct ViewMeta { int lo; int nwin4; int fast; int pad; };
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ int lds_s32(unsigned addr) {
-    int v;
-    asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(addr));
-    return v;
-}
-__device__ __forceinline__ void cp_async16(unsigned dst, const void* src, int src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
-
-template <int VC, bool CHECKED>
-__global__ void __launch_bounds__(BP_THREADS, 2) k_bp_ref(BackprojLaunch p) {
-    extern __shared__ __align__(16) int smi[];
-    int* win = smi;                                                   // [2][VC][BP_WIN]
-    float* xs = reinterpret_cast<float*>(win + 2 * VC * BP_WIN);      // [3][VC][64]
-    float* ys = xs + 3 * VC * 64;                                     // [3][VC][64]
-    ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * 64);   // [3][VC]
-
-    const int ixdimp = p.ixdimp;
-    const int tiles_x = (ixdimp + BP_T - 1) / BP_T;
-    const int X0 = (blockIdx.x % tiles_x) * BP_T;
-    const int Y0 = (blockIdx.x / tiles_x) * BP_T;
-    const int slice = blockIdx.y;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int tx = (warp & 1) * 8 + (lane & 7);
-    const int ty = (warp >> 1) * 4 + (lane >> 3);
-    const int* tab = p.table + (size_t)slice * p.slice_table_stride;
-    const int N16 = 16 * ixdimp;
-    const int nviews = p.nviews;
-    const int nchunks = (nviews + VC - 1) / VC;
-    unsigned viol = 0;
-
-    // per-view window + tabulated products for chunk c into meta/xs/ys slot ms
-    auto prepare = [&](int c, int ms) {
-        const int v0 = c * VC;
-        if (tid < VC && v0 + tid < nviews) {
-            const float4 g = __ldg(p.geom + v0 + tid);
-            float lo = 3.0e38f, hi = -3.0e38f;
-#pragma unroll
-            for (int cy = 0; cy < 2; cy++) {
-                const float fy = fadd(fmul((float)(Y0 + cy * (BP_T - 1)), g.y), g.z);
-#pragma unroll
-                for (int cx = 0; cx < 2; cx++) {
-                    const float fx = fadd(fmul((float)(X0 + cx * (BP_T - 1)), g.x), fy);
-                    lo = fminf(lo, fx);
-                    hi = fmaxf(hi, fx);
-                }
-            }
-            ViewMeta m;
-            const int ilo = (int)floorf(lo) - 2;
-            m.lo = ilo & ~3;
-            const int ihi = (int)floorf(hi) + 3;
-            int nwin = ihi - m.lo;
-            nwin = (nwin + 3) & ~3;
-            if (nwin > BP_WIN) nwin = BP_WIN;
-            m.nwin4 = nwin >> 2;
-            m.fast = (lo >= 2.0f) ? 1 : 0;
-            m.pad = 0;
-            meta[ms * VC + tid] = m;
-        }
-        for (int e = tid; e < VC * 128; e += BP_THREADS) {
-            const int vv = e >> 7, w = e & 127;
-            if (v0 + vv >= nviews) continue;
-            const float4 g = __ldg(p.geom + v0 + vv);
-            if (w < 64) {
-                const int x = X0 + (w >> 2) + 16 * (w & 3);
-                xs[(ms * VC + vv) * 64 + w] = fmul((float)x, g.x);
-            } else {
-                const int ww = w - 64;
-                const int y = Y0 + (ww >> 2) + 16 * (ww & 3);
-                ys[(ms * VC + vv) * 64 + ww] = fadd(fmul((float)y, g.y), g.z);
-            }
-        }
-    };
-    // cp.async of the windows of chunk c (meta slot ms) into window buffer wb
-    auto stage = [&](int c, int ms, int wb) {
-        const int v0 = c * VC;
-        for (int vv = 0; vv < VC; vv++) {
-            if (v0 + vv >= nviews) break;
-            const ViewMeta m = meta[ms * VC + vv];
-            const int* src = tab + (size_t)(v0 + vv) * p.table_stride;
-            int* dst = win + (wb * VC + vv) * BP_WIN;
-            for (int e = tid; e < m.nwin4; e += BP_THREADS) {
-                const int g = m.lo + 4 * e;
-                const bool in = (g >= 0) && (g + 4 <= N16);
-                cp_async16(smem_u32(dst + 4 * e), in ? (const void*)(src + g) : (const void*)src, in ? 16 : 0);
-            }
-        }
-    };
-
-    int acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[r][c] = 0;
-
-    prepare(0, 0);
-    if (nchunks > 1) prepare(1, 1);
-    __syncthreads();
-    stage(0, 0, 0);
-    cp_async_commit();
-
-    for (int k = 0; k < nchunks; k++) {
-        const int wb = k & 1, ms = k % 3;
-        if (k + 1 < nchunks) {
-            stage(k + 1, (k + 1) % 3, wb ^ 1);
-            cp_async_commit();
-        }
-        if (k + 2 < nchunks) prepare(k + 2, (k + 2) % 3);
-        if (k + 1 < nchunks) cp_async_wait<1>(); else cp_async_wait<0>();
-        __syncthreads();
-        const int nv = min(VC, nviews - k * VC);
-        for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[ms * VC + vv];
-            const float4 xa = *reinterpret_cast<const float4*>(xs + (ms * VC + vv) * 64 + tx * 4);
-            const float4 ya = *reinterpret_cast<const float4*>(ys + (ms * VC + vv) * 64 + ty * 4);
-            const float xv[4] = {xa.x, xa.y, xa.z, xa.w};
-            const float yv[4] = {ya.x, ya.y, ya.z, ya.w};
-            const unsigned wbase = smem_u32(win + (wb * VC + vv) * BP_WIN);
-            if (m.fast) {
-                const unsigned base = wbase - 4u * (unsigned)m.lo - 4u * kMagicBits;
-#pragma unroll
-                for (int r = 0; r < 4; r++)
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const float fx = fadd(xv[c], yv[r]);
-                        const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
-                        if (CHECKED) {
-                            const int idx = (int)(bits - kMagicBits) - m.lo;
-                            if (fx < 0.0f || idx < 0 || idx >= 4 * m.nwin4) { viol++; continue; }
-                        }
-                        acc[r][c] += lds_s32(base + 4u * bits);
-                    }
-            } else {
-                const unsigned base = wbase - 4u * (unsigned)m.lo;
-#pragma unroll
-                for (int r = 0; r < 4; r++)
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const float fx = fadd(xv[c], yv[r]);
-                        const int ix0 = __float2int_rz(fx);
-                        if (CHECKED) {
-                            const int idx = ix0 - m.lo;
-                            if (idx < 0 || idx >= 4 * m.nwin4) { viol++; continue; }
-                        }
-                        acc[r][c] += lds_s32(base + 4u * (unsigned)ix0);
-                    }
-            }
-        }
-        __syncthreads();
-    }
-    if (CHECKED && viol) atomicAdd(p.status, viol);
-
-    int* out = static_cast<int*>(p.out) + (size_t)slice * p.out_slice_stride;
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int y = Y0 + ty + 16 * r;
-        if (y >= ixdimp) continue;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const int x = X0 + tx + 16 * c;
-            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------------------------
 // R8' (LIN): the same tiling with true linear interpolation of the filtered row at the FP32
@@ -627,65 +444,12 @@ __global__ void __launch_bounds__(BP_THREADS, 2) k_bp_lin(BackprojLaunch p) {
     }
 }
 
-template <int VC>
-static size_t bp_ref_smem() {
-    return (size_t)2 * VC * BP_WIN * sizeof(int) + (size_t)2 * 3 * VC * 64 * sizeof(float) +
-           (size_t)3 * VC * sizeof(ViewMeta);
-}
-
-// Validation mode (RvSetCheckedBackprojection): the REF kernel is replaced by its bounds-checked
-// twin, which skips and counts every table index outside the staged window.
-static int g_checked = 0;
-static unsigned int* g_status = nullptr;
-static unsigned long long g_violations = 0;
-
-}  // namespace rv
-
-extern "C" int RvSetCheckedBackprojection(int enable) {
-    if (enable && !rv::g_status) {
-        if (cudaMalloc(&rv::g_status, sizeof(unsigned int)) != cudaSuccess) return RV_ERR_DEVICE_OOM;
-    }
-    rv::g_checked = enable ? 1 : 0;
-    rv::g_violations = 0;
-    return 0;
-}
-extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
-
-namespace rv {
-
-cudaError_t launch_backproject(const BackprojLaunch& pin, cudaStream_t s) {
-    BackprojLaunch p = pin;
-    if (g_checked && p.mode == RV_MODE_REF) {
-        p.checked = 1;
-        p.status = g_status;
-        cudaError_t e = cudaMemsetAsync(g_status, 0, sizeof(unsigned int), s);
-        if (e != cudaSuccess) return e;
-    }
+cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s) {
     if (p.nslices <= 0) return cudaSuccess;
     if (p.ixdimp > kMaxIxdimp) return cudaErrorInvalidValue;
+    if (p.mode == RV_MODE_REF) return launch_bp_ref(p, s);
     const int tiles = ((p.ixdimp + BP_T - 1) / BP_T) * ((p.ixdimp + BP_T - 1) / BP_T);
     dim3 grid(tiles, p.nslices);
-    cudaError_t e = cudaSuccess;
-    if (p.mode == RV_MODE_REF) {
-        constexpr int VC = 8;
-        const size_t smem = bp_ref_smem<VC>();
-        auto go = [&](auto kern) {
-            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return;
-            kern<<<grid, BP_THREADS, smem, s>>>(p);
-            e = cudaGetLastError();
-        };
-        if (p.checked && p.status) {
-            go(k_bp_ref<VC, true>);
-            unsigned int v = 0;
-            if (e == cudaSuccess) e = cudaMemcpyAsync(&v, p.status, sizeof(v), cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            g_violations += v;
-        } else {
-            go(k_bp_ref<VC, false>);
-        }
-        return e;
-    }
     constexpr int VC = 8;
     switch (p.mode) {
     case RV_MODE_LIN: k_bp_lin<VC, RV_MODE_LIN><<<grid, BP_THREADS, 0, s>>>(p); break;

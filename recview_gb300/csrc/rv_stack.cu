@@ -40,6 +40,8 @@ struct RvStack {
     int nbatches_last = 0;
     float t_filter = 0, t_bp = 0, t_total = 0;
     int launches = 0;
+    int tpad = 0;                   // REF table layout (ref_table_pad at creation)
+    long long tstride = 0;          // ints per table slot
 };
 
 static void stack_free(RvStack* st) {
@@ -141,7 +143,9 @@ extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
     // ---- batch size from the table budget ----------------------------------------------------
     size_t budget_mb = 8192;
     if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
-    const size_t per_slice = desc->mode == RV_MODE_REF ? (size_t)V * 16 * d.ixdimp * sizeof(int)
+    st->tpad = ref_table_pad();
+    st->tstride = ref_table_stride(d.ixdimp, st->tpad);
+    const size_t per_slice = desc->mode == RV_MODE_REF ? (size_t)V * st->tstride * sizeof(int)
                                                        : (size_t)V * d.ixdimp * (desc->mode == RV_MODE_LIN ? 4 : 2);
     size_t b = (budget_mb << 20) / (per_slice ? per_slice : 1);
     if (b < 1) b = 1;
@@ -213,7 +217,7 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
     cudaStream_t s = (cudaStream_t)stream;
     const Dims& d = st->d;
     const int S = st->desc.nslices, V = st->nviews, mode = st->desc.mode;
-    const long long tstride = 16LL * d.ixdimp;
+    const long long tstride = st->tstride;
     const size_t npix = (size_t)d.ixdimp * d.ixdimp;
     st->launches = 0;
     float tf = 0, tb = 0;
@@ -234,6 +238,7 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
         if (mode == RV_MODE_REF) {
             fl.table = static_cast<int*>(st->d_table);
             fl.table_stride = tstride;
+            fl.table_pad = st->tpad;
         } else if (mode == RV_MODE_LIN) {
             fl.rows = static_cast<float*>(st->d_table);
             fl.row_stride = d.ixdimp;
@@ -263,6 +268,7 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
                                      : (void*)(static_cast<float*>(d_out) + (size_t)s0 * npix);
         bl.out_slice_stride = (long long)npix;
         bl.mode = mode;
+        bl.table_pad = st->tpad;
         e = launch_backproject(bl, s);
         if (!cuda_ok(e, RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
         cudaEventRecord(st->ev[2], s);
@@ -278,6 +284,10 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
     cudaEventRecord(st->ev[5], s);
     cudaError_t e = cudaEventSynchronize(st->ev[5]);
     if (!cuda_ok(e, RV_ERR_LAUNCH, "stack run")) return RV_ERR_LAUNCH;
+    if (take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+        return RV_ERR_KERNEL_STATUS;
+    }
     float tt = 0;
     cudaEventElapsedTime(&tt, st->ev[4], st->ev[5]);
     st->t_filter = tf;

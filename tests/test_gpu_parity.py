@@ -157,9 +157,20 @@ def test_progress_callback_abort(gpu, oracle):
     assert np.array_equal(got, oracle.reconstruct(ri2))
 
 
+@pytest.fixture(params=[(0, 0), (0, 1), (1, 0), (1, 1), (2, 0), (2, 1)], ids=lambda v: f"variant{v[0]}pad{v[1]}")
+def bp_variant(request, gpu):
+    """Every back-projection variant and table layout; restores the default afterwards."""
+    L = rv.lib()
+    old_v, old_p = C.c_int(), C.c_int()
+    L.RvGetBackprojectionVariant(C.byref(old_v), C.byref(old_p))
+    assert L.RvSetBackprojectionVariant(*request.param) == 0
+    yield request.param
+    L.RvSetBackprojectionVariant(old_v.value, old_p.value)
+
+
 @pytest.mark.parametrize("W,V,cen,interp", [(512, 900, 255.5, 2), (200, 181, 10.4, 2), (200, 181, 180.6, 2),
                                             (96, 100, 50.25, 4), (1000, 400, 499.3, 2), (60, 64, 5.5, 5)])
-def test_window_bound_holds(gpu, oracle, W, V, cen, interp):
+def test_window_bound_holds(bp_variant, oracle, W, V, cen, interp):
     """The production kernel reads the staged table window without per-access checks; the
     checked twin counts any index outside the window, and must count none."""
     L = rv.lib()
@@ -171,6 +182,14 @@ def test_window_bound_holds(gpu, oracle, W, V, cen, interp):
     finally:
         L.RvSetCheckedBackprojection(0)
     assert np.array_equal(got, oracle.reconstruct(ri, threads=8))
+
+
+@pytest.mark.parametrize("case", SLICE_CASES[:8], ids=lambda c: f"W{c[1]}V{c[2]}c{c[3]}z{c[4]}")
+def test_variants_bit_exact(bp_variant, oracle, case):
+    seed, W, V, cen, interp, kind, flags, tilt = case
+    ri = fbp_case(seed, W, V, cen, interp, kind=kind, flags=flags, tilt=tilt, skip_every=13, oracle=oracle)
+    want = oracle.reconstruct(ri, threads=8)
+    assert np.array_equal(_gpu_slice(ri), want)
 
 
 # ---- normalisation (R1) ---------------------------------------------------------------------
