@@ -278,6 +278,22 @@ int RvStackLastTimings(const RvStack* st, float* ms3);
 /* Number of kernels launched by the last run. */
 int RvStackLastLaunchCount(const RvStack* st);
 
+/* Allocation-free variant of the one-slice reconstruction (no counterpart in the reference).
+ * For callers that cannot allocate device memory -- e.g. a plugin inside a host program that
+ * owns the device-memory pool, or code that must not synchronise the device through an
+ * allocation -- but can pass device buffers: d_sino holds nviews log-normalised int16 rows of
+ * ixdim samples (the SAMPLE views only, in order), fdeg[nviews] and fFilter[ndim] are host
+ * arrays, d_slice receives ixdimp^2 int32 values; results equal CudaReconstHost's bit for bit.
+ * Scratch (tables, geometry, FFT twiddles) lives in a fixed 64 MiB __device__ array that every
+ * GPU loading this library keeps until the process exits; a slice needing more (about
+ * nviews * 64 * ixdimp bytes) is rejected with RV_ERR_UNSUPPORTED.  The first call on a device
+ * resolves the array's device address on that device, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race.  Returns 0 or an RV_ERR_* code
+ * after the slice is complete on `stream`. */
+int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ixdim, int iInterpolation,
+                              double center, const float* fdeg, float fTiltAngle,
+                              const float* fFilter, int* d_slice, void* stream);
+
 /* Validation mode: while enabled, the REF back-projection runs a bounds-checked variant that
  * skips and counts every table index falling outside the window staged in shared memory (the
  * production kernel relies on the window bound instead of per-access checks).  Slower; for tests. */

@@ -187,6 +187,8 @@ PROTOTYPES = {
     "RvProbeThroughput": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "RvSetBackprojectionVariant": (C.c_int, [C.c_int, C.c_int]),
     "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
+    "RvReconstructSliceNoAlloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, c_float_p,
+                                            C.c_float, c_float_p, C.c_void_p, C.c_void_p]),
 }
 
 
