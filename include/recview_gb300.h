@@ -300,11 +300,25 @@ int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ixdim, int iI
 int RvSetCheckedBackprojection(int enable);
 unsigned long long RvGetWindowViolations(void);
 
+/* R9: the rescale CGazoDoc::DeconvBackProj applies to finished slices (source/gazoDoc.cpp:
+ * 3993-4021), on the device, in place on d_slices[nslices][ixdimp^2] (int32): per slice imin/imax
+ * (imax starts at 0), pixels outside the circle of radius min(ipintp*c/bin, ixdimp - ipintp*c/bin)
+ * (c = the user centre before the half-pixel/binning conversion) set to 0, others mapped to
+ * (v - imin) * 65534 / (imax - imin) in float.  Optional d_out16 receives the same values as
+ * uint16; minmax (host, 2*nslices) receives imin, imax per slice (imax before the +1 of a flat
+ * slice).  Synchronises `stream` before returning. */
+int RvRescaleSlices(int* d_slices, int nslices, int ixdimp, double center_user, int ipintp, int ibinning,
+                    unsigned short* d_out16, int* minmax, void* stream);
+
 /* Tuning of the REF back-projection (process-wide; affects stacks created and slices reconstructed
- * afterwards): variant 0 = 128x128 tile / 8 views per chunk, 1 = 64x64 / 8, 2 = 128x128 / 4;
- * pad = 1 stores 17 table words per detector pixel (fewer shared-memory bank conflicts). */
-int RvSetBackprojectionVariant(int variant, int pad);
-int RvGetBackprojectionVariant(int* variant, int* pad);
+ * afterwards).  format: 0 = the reference's 16-int table per detector pixel, 1 = the same padded
+ * to 17 words (fewer shared-memory bank conflicts), 2 = the float pair (p0, slope) per
+ * detector pixel, expanded by the kernel with the reference's operations (8x smaller tables,
+ * conflict-free lookups).  variant 0..4 selects tile shape / threads / views per chunk (default:
+ * format 0, variant 0, the fastest measured on GB300).  All
+ * combinations give bit-identical slices. */
+int RvSetBackprojectionVariant(int variant, int format);
+int RvGetBackprojectionVariant(int* variant, int* format);
 
 /* Device throughput probes used as roofline denominators for the back-projection, which is
  * bound by instruction issue rather than HBM or tensor cores: out[0] = FP32 FMA TFLOP/s,

@@ -185,6 +185,8 @@ PROTOTYPES = {
     "RvSetCheckedBackprojection": (C.c_int, [C.c_int]),
     "RvGetWindowViolations": (C.c_ulonglong, []),
     "RvProbeThroughput": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
+    "RvRescaleSlices": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
+                                  c_int_p, C.c_void_p]),
     "RvSetBackprojectionVariant": (C.c_int, [C.c_int, C.c_int]),
     "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
     "RvReconstructSliceNoAlloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, c_float_p,

@@ -25,7 +25,7 @@
 // [floor(min) - 2 (aligned down), floor(max) + 3).  The bounds-checked twin (CHECKED) counts any
 // index outside the window; tests run it on many geometries and require zero.
 //
-// Optional padded layout (table_pad): 17 words per detector pixel, so lanes whose indices differ
+// Optional padded layout (table_fmt): 17 words per detector pixel, so lanes whose indices differ
 // by ~16 (views near 0 or 90 degrees) fall into different shared-memory banks.
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -103,8 +103,8 @@ struct ViewMeta {
     int pad0, pad1, pad2;
 };
 
-template <int WX, int WY, int RX, int RY, int VC, int PAD, bool CHECKED>
-__global__ void __launch_bounds__(32 * WX * WY, 1) k_bp_ref(BackprojLaunch p) {
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, bool CHECKED>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p) {
     using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
     constexpr int NT = Cfg::NT, TX = Cfg::TX, TY = Cfg::TY, WIN = Cfg::WIN;
     extern __shared__ __align__(128) int smi[];
@@ -301,62 +301,293 @@ __global__ void __launch_bounds__(32 * WX * WY, 1) k_bp_ref(BackprojLaunch p) {
     }
 }
 
+// ---- pair-table variant ------------------------------------------------------------------------
+// The table holds, per detector pixel j, the float pair (p0, p1p0) from which the reference builds
+// its 16 ints (source/general.cpp:2130-2137).  Each update rebuilds its entry with the same float
+// operations, (int)(p0 + p1p0 * k), so results stay bit-identical while a warp's 32 lookups fall on
+// ~10 consecutive 8-byte pairs (no bank conflicts) and the table is 8x smaller.  With
+// y = fl_rz(fx + 2^23) = 2^23 + floor(fx):  fl = y - 2^23 = floor(fx),
+// z = fl_rz(fl/16 + 2^23) = 2^23 + j,  k = fl - 16 j  -- all exact in FP32 for 0 <= fx < 2^23.
+template <int WX, int WY, int RX, int RY, int VC>
+struct PairCfg {
+    static constexpr int NT = 32 * WX * WY;
+    static constexpr int GX = 8 * WX, GY = 4 * WY;
+    static constexpr int TX = GX * RX, TY = GY * RY;
+    // detector-pixel span of a tile: sqrt((TX-1)^2 + (TY-1)^2) + margins + even alignment
+    static constexpr int WINJ = ((isqrt_ceil((TX - 1) * (TX - 1) + (TY - 1) * (TY - 1)) + 8) + 3) / 4 * 4;
+    static constexpr size_t SMEM = (size_t)2 * VC * WINJ * 8 + (size_t)3 * VC * (TX + TY) * 4 + (size_t)3 * VC * 32 + 16;
+};
+
+template <int WX, int WY, int RX, int RY, int VC, int MINB, bool CHECKED>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p) {
+    using Cfg = PairCfg<WX, WY, RX, RY, VC>;
+    constexpr int NT = Cfg::NT, TX = Cfg::TX, TY = Cfg::TY, WINJ = Cfg::WINJ;
+    extern __shared__ __align__(128) int smi[];
+    float2* win = reinterpret_cast<float2*>(smi);                       // [2][VC][WINJ]
+    float* xs = reinterpret_cast<float*>(win + 2 * VC * WINJ);          // [3][VC][TX]
+    float* ys = xs + 3 * VC * TX;                                       // [3][VC][TY]
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * TY);     // [3][VC]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(meta + 3 * VC);        // [2]
+
+    const int ixdimp = p.ixdimp;
+    const int tiles_x = (ixdimp + TX - 1) / TX;
+    const int X0 = (blockIdx.x % tiles_x) * TX;
+    const int Y0 = (blockIdx.x / tiles_x) * TY;
+    const int slice = blockIdx.y;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = (warp % WX) * 8 + (lane & 7);
+    const int ty = (warp / WX) * 4 + (lane >> 3);
+    const float2* tab = reinterpret_cast<const float2*>(p.table + (size_t)slice * p.slice_table_stride);
+    const int npairs = (ixdimp + 1) & ~1;   // the filter writes a zero pair at j = ixdimp when odd
+    const int nviews = p.nviews;
+    const int nchunks = (nviews + VC - 1) / VC;
+    unsigned viol = 0;
+
+    if (tid == 0) {
+        mbar_init(smem_u32(&bars[0]), 1);
+        mbar_init(smem_u32(&bars[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    auto prepare = [&](int c, int ms) {
+        const int v0 = c * VC;
+        if (tid < VC && v0 + tid < nviews) {
+            const float4 g = __ldg(p.geom + v0 + tid);
+            float lo = 3.0e38f, hi = -3.0e38f;
+#pragma unroll
+            for (int cy = 0; cy < 2; cy++) {
+                const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), g.y), g.z);
+#pragma unroll
+                for (int cx = 0; cx < 2; cx++) {
+                    const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), g.x), fy);
+                    lo = fminf(lo, fx);
+                    hi = fmaxf(hi, fx);
+                }
+            }
+            const int ilo = (int)floorf(lo) - 2;       // index range [ilo, ihi)
+            const int ihi = (int)floorf(hi) + 3;
+            ViewMeta m;
+            m.w0 = (ilo >> 4) & ~1;                    // first pair (even, floor division)
+            const int jhi = (((ihi - 1) >> 4) + 2) & ~1;
+            m.nwin = min(jhi - m.w0, WINJ);
+            m.a = max(m.w0, 0);
+            m.b = min(m.w0 + m.nwin, npairs);
+            m.fast = (lo >= 2.0f) ? 1 : 0;
+            m.pad0 = m.pad1 = m.pad2 = 0;
+            meta[ms * VC + tid] = m;
+        }
+        for (int e = tid; e < VC * (TX + TY); e += NT) {
+            const int vv = e / (TX + TY), w = e - vv * (TX + TY);
+            if (v0 + vv >= nviews) continue;
+            const float4 g = __ldg(p.geom + v0 + vv);
+            if (w < TX) {
+                const int t = w / RX, c = w - t * RX;
+                xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
+            } else {
+                const int w2 = w - TX, t = w2 / RY, r = w2 - t * RY;
+                ys[(ms * VC + vv) * TY + w2] = faddr(fmulr((float)(Y0 + t + Cfg::GY * r), g.y), g.z);
+            }
+        }
+    };
+    auto stage = [&](int c, int ms, int wb) {
+        const int v0 = c * VC;
+        const int nv = min(VC, nviews - v0);
+        if (tid == 0) {
+            unsigned bytes = 0;
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[ms * VC + vv];
+                if (m.b > m.a) bytes += 8u * (unsigned)(m.b - m.a);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const unsigned bar = smem_u32(&bars[wb]);
+            mbar_arrive_expect_tx(bar, bytes);
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[ms * VC + vv];
+                if (m.b <= m.a) continue;
+                const float2* src = tab + (size_t)(v0 + vv) * (p.table_stride / 2) + m.a;
+                const unsigned dst = smem_u32(win + (wb * VC + vv) * WINJ + (m.a - m.w0));
+                tma_bulk_g2s(dst, src, 8u * (unsigned)(m.b - m.a), bar);
+            }
+        }
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[ms * VC + vv];
+            float4* w4 = reinterpret_cast<float4*>(win + (wb * VC + vv) * WINJ);   // 2 pairs per float4
+            const int za = (m.b > m.a) ? (m.a - m.w0) >> 1 : m.nwin >> 1;
+            const int zb = (m.b > m.a) ? (m.b - m.w0) >> 1 : m.nwin >> 1;
+            for (int e = tid; e < za; e += NT) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int e = zb + tid; e < ((m.nwin + 1) >> 1); e += NT) w4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+
+    int acc[RY][RX];
+#pragma unroll
+    for (int r = 0; r < RY; r++)
+#pragma unroll
+        for (int c = 0; c < RX; c++) acc[r][c] = 0;
+
+    prepare(0, 0);
+    if (nchunks > 1) prepare(1, 1);
+    __syncthreads();
+    stage(0, 0, 0);
+    for (int k = 0; k < nchunks; k++) {
+        const int wb = k & 1, ms = k % 3;
+        if (k + 1 < nchunks) stage(k + 1, (k + 1) % 3, wb ^ 1);
+        if (k + 2 < nchunks) prepare(k + 2, (k + 2) % 3);
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[wb]), (unsigned)(k >> 1) & 1u);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(&g_kernel_status, 1u);
+            mbar_wait_bounded(smem_u32(&bars[wb]), (unsigned)(k >> 1) & 1u);
+            if (k + 1 < nchunks) mbar_wait_bounded(smem_u32(&bars[wb ^ 1]), (unsigned)((k + 1) >> 1) & 1u);
+            return;
+        }
+        const int nv = min(VC, nviews - k * VC);
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[ms * VC + vv];
+            float xv[RX], yv[RY];
+#pragma unroll
+            for (int c4 = 0; c4 < RX; c4 += 4) {
+                const float4 t4 = *reinterpret_cast<const float4*>(xs + (ms * VC + vv) * TX + tx * RX + c4);
+                xv[c4] = t4.x; xv[c4 + 1] = t4.y; xv[c4 + 2] = t4.z; xv[c4 + 3] = t4.w;
+            }
+#pragma unroll
+            for (int r4 = 0; r4 < RY; r4 += 4) {
+                const float4 t4 = *reinterpret_cast<const float4*>(ys + (ms * VC + vv) * TY + ty * RY + r4);
+                yv[r4] = t4.x; yv[r4 + 1] = t4.y; yv[r4 + 2] = t4.z; yv[r4 + 3] = t4.w;
+            }
+            const float2* wv = win + (wb * VC + vv) * WINJ;
+            const unsigned wbase = smem_u32(wv) - 8u * (unsigned)m.w0;
+            if (m.fast) {
+                const unsigned base = wbase - 8u * kMagicBits;
+#pragma unroll
+                for (int r = 0; r < RY; r++)
+#pragma unroll
+                    for (int c = 0; c < RX; c++) {
+                        const float fx = faddr(xv[c], yv[r]);
+                        const float y = __fadd_rz(fx, 8388608.0f);
+                        const float fl = __fsub_rn(y, 8388608.0f);            // floor(fx)
+                        const float z = __fmaf_rz(fl, 0.0625f, 8388608.0f);   // 2^23 + j
+                        const float jf = __fsub_rn(z, 8388608.0f);
+                        const float kf = __fmaf_rn(-16.0f, jf, fl);            // k, exact
+                        const unsigned zb = __float_as_uint(z);
+                        if (CHECKED) {
+                            const int j = (int)(zb - kMagicBits);
+                            if (fx < 0.0f || j < m.w0 || j >= m.w0 + m.nwin) { viol++; continue; }
+                        }
+                        float2 pr;
+                        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(pr.x), "=f"(pr.y) : "r"(base + 8u * zb));
+                        acc[r][c] += __float2int_rz(faddr(pr.x, fmulr(pr.y, kf)));
+                    }
+            } else {
+#pragma unroll
+                for (int r = 0; r < RY; r++)
+#pragma unroll
+                    for (int c = 0; c < RX; c++) {
+                        const float fx = faddr(xv[c], yv[r]);
+                        const int ix = __float2int_rz(fx);        // the reference's (int)fx
+                        const int j = ix >> 4;                    // floor division
+                        const float kf = (float)(ix & 15);
+                        if (CHECKED) {
+                            if (j < m.w0 || j >= m.w0 + m.nwin) { viol++; continue; }
+                        }
+                        float2 pr;
+                        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(pr.x), "=f"(pr.y) : "r"(wbase + 8u * (unsigned)j));
+                        acc[r][c] += __float2int_rz(faddr(pr.x, fmulr(pr.y, kf)));
+                    }
+            }
+        }
+        __syncthreads();
+    }
+    if (CHECKED && viol) atomicAdd(p.status_counter, viol);
+
+    int* out = static_cast<int*>(p.out) + (size_t)slice * p.out_slice_stride;
+#pragma unroll
+    for (int r = 0; r < RY; r++) {
+        const int y = Y0 + ty + Cfg::GY * r;
+        if (y >= ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < RX; c++) {
+            const int x = X0 + tx + Cfg::GX * c;
+            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+        }
+    }
+}
+
 // ---- configuration ---------------------------------------------------------------------------
-// Variants (RV_BP_VARIANT, for tuning; the default is the measured best):
-//   0: 128x128 tile, 512 threads, 4x8 px/thread, 8 views/chunk
-//   1: 64x64 tile, 256 threads, 4x4 px/thread, 8 views/chunk
-//   2: 128x128 tile, 512 threads, 4x8 px/thread, 4 views/chunk
+// Table format (RvSetBackprojectionVariant's second argument, or RV_BP_FORMAT) and variant
+// (first argument, or RV_BP_VARIANT):
+//   int tables (format 0 dense / 1 padded), 32 px per thread unless noted:
+//     0: 128x128 tile, 512 threads, 8 views/chunk   1: 64x64, 256 threads, 16 px/thread
+//     2: 128x128, 512 threads, 4 views/chunk
+//     3: 64x64, 256 threads, 16 px/thread, 4 views/chunk, 4 CTAs/SM
+//     4: 128x64, 512 threads, 16 px/thread, 4 views/chunk, 2 CTAs/SM
+//   pair tables (format 2):
+//     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
+//     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
 static int env_int(const char* name, int dflt) {
     const char* e = getenv(name);
     return e ? atoi(e) : dflt;
 }
-static int g_variant = -1, g_pad = -1;
+static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
     if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 0);
-    if (g_pad < 0) g_pad = env_int("RV_BP_PAD", 0) ? 1 : 0;
+    if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
-int ref_table_pad() {
+int ref_table_fmt() {
     load_defaults();
-    return g_pad;
+    return g_fmt;
 }
-long long ref_table_stride(int ixdimp, int pad) {
-    return pad ? (((long long)17 * ixdimp + 15) & ~15LL) : 16LL * ixdimp;
+long long ref_table_stride(int ixdimp, int fmt) {
+    if (fmt == kTabPair) return 2LL * ((ixdimp + 1) & ~1);   // floats, pairs rounded to an even count
+    if (fmt == kTabInt17) return ((long long)17 * ixdimp + 15) & ~15LL;
+    return 16LL * ixdimp;
 }
 
 static int g_checked = 0;
 static unsigned int* g_counter = nullptr;
 static unsigned long long g_violations = 0;
 
-template <int WX, int WY, int RX, int RY, int VC, int PAD>
+template <typename K>
+static cudaError_t launch_k(K kern, dim3 grid, int nt, size_t smem, const BackprojLaunch& p, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, nt, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB>
 static cudaError_t go_bp(const BackprojLaunch& p, cudaStream_t s, bool checked) {
     using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
     const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
     dim3 grid(tiles, p.nslices);
-    cudaError_t e;
-    if (checked) {
-        auto kern = k_bp_ref<WX, WY, RX, RY, VC, PAD, true>;
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
-        if (e == cudaSuccess) {
-            kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(p);
-            e = cudaGetLastError();
-        }
-    } else {
-        auto kern = k_bp_ref<WX, WY, RX, RY, VC, PAD, false>;
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
-        if (e == cudaSuccess) {
-            kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(p);
-            e = cudaGetLastError();
-        }
-    }
-    return e;
+    if (checked) return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int MINB>
+static cudaError_t go_pair(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    using Cfg = PairCfg<WX, WY, RX, RY, VC>;
+    const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
+    dim3 grid(tiles, p.nslices);
+    if (checked) return launch_k(k_bp_pair<WX, WY, RX, RY, VC, MINB, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    return launch_k(k_bp_pair<WX, WY, RX, RY, VC, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
 template <int PAD>
 static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool checked, int variant) {
     switch (variant) {
-    case 1: return go_bp<2, 4, 4, 4, 8, PAD>(p, s, checked);
-    case 2: return go_bp<4, 4, 4, 8, 4, PAD>(p, s, checked);
-    default: return go_bp<4, 4, 4, 8, 8, PAD>(p, s, checked);
+    case 1: return go_bp<2, 4, 4, 4, 8, PAD, 1>(p, s, checked);
+    case 2: return go_bp<4, 4, 4, 8, 4, PAD, 1>(p, s, checked);
+    case 3: return go_bp<2, 4, 4, 4, 4, PAD, 4>(p, s, checked);
+    case 4: return go_bp<4, 4, 4, 4, 4, PAD, 2>(p, s, checked);
+    default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
+    }
+}
+
+static cudaError_t dispatch_pair(const BackprojLaunch& p, cudaStream_t s, bool checked, int variant) {
+    switch (variant) {
+    case 1: return go_pair<2, 4, 4, 8, 16, 2>(p, s, checked);
+    case 2: case 4: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
+    case 3: return go_pair<2, 4, 4, 4, 8, 4>(p, s, checked);
+    default: return go_pair<4, 4, 4, 8, 16, 1>(p, s, checked);
     }
 }
 
@@ -370,7 +601,10 @@ cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
         cudaError_t e = cudaMemsetAsync(g_counter, 0, sizeof(unsigned int), s);
         if (e != cudaSuccess) return e;
     }
-    cudaError_t e = p.table_pad ? dispatch_bp<1>(p, s, checked, variant) : dispatch_bp<0>(p, s, checked, variant);
+    cudaError_t e;
+    if (p.table_fmt == kTabPair) e = dispatch_pair(p, s, checked, variant);
+    else if (p.table_fmt == kTabInt17) e = dispatch_bp<1>(p, s, checked, variant);
+    else e = dispatch_bp<0>(p, s, checked, variant);
     if (checked && e == cudaSuccess) {
         unsigned int v = 0;
         e = cudaMemcpyAsync(&v, g_counter, sizeof(v), cudaMemcpyDeviceToHost, s);
@@ -400,15 +634,15 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 }
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
-extern "C" int RvSetBackprojectionVariant(int variant, int pad) {
-    if (variant < 0 || variant > 2 || pad < 0 || pad > 1) return RV_ERR_BAD_ARGUMENT;
+extern "C" int RvSetBackprojectionVariant(int variant, int format) {
+    if (variant < 0 || variant > 4 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
-    rv::g_pad = pad;
+    rv::g_fmt = format;
     return 0;
 }
-extern "C" int RvGetBackprojectionVariant(int* variant, int* pad) {
+extern "C" int RvGetBackprojectionVariant(int* variant, int* format) {
     rv::load_defaults();
     if (variant) *variant = rv::g_variant;
-    if (pad) *pad = rv::g_pad;
+    if (format) *format = rv::g_fmt;
     return 0;
 }

@@ -125,7 +125,7 @@ struct RiContext {
     // filtered views kept for RQFLAGS_SINOGRAMKEPT (source/cudaReconstHost.cpp:658)
     bool kept = false;
     int kept_ixdim = 0, kept_interp = 0, kept_start = 0, kept_step = 0, kept_mult = 0, kept_off = 0;
-    int kept_pad = 0;
+    int kept_fmt = 0;
     std::vector<int> kept_views;
 
     bool stage(size_t need) {
@@ -262,9 +262,9 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
                    c->kept_ixdim != ri->ixdim || c->kept_interp != ri->iInterpolation ||
                    c->kept_start != ri->iStartSino || c->kept_step != ri->iStepSino ||
                    c->kept_mult != ri->iMultiplex || c->kept_off != ri->iOffset || c->kept_views != views ||
-                   c->kept_pad != ref_table_pad();
-    const int tpad = ref_table_pad();
-    const size_t table_stride = (size_t)ref_table_stride(ixdimp, tpad);
+                   c->kept_fmt != ref_table_fmt();
+    const int tfmt = ref_table_fmt();
+    const size_t table_stride = (size_t)ref_table_stride(ixdimp, tfmt);
     if (!c->out.ensure((size_t)ixdimp * ixdimp * sizeof(int))) {
         fail(ri, RV_ERR_DEVICE_OOM, "Out of CUDA device memory (slice)");
         return;
@@ -313,7 +313,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         fl.d = d;
         fl.ic = intcenter;
         fl.table_stride = (long long)table_stride;
-        fl.table_pad = tpad;
+        fl.table_fmt = tfmt;
         if (!cuda_ok(launch_filter(fl, s), RV_ERR_LAUNCH, "filter kernel")) {
             ri->iStatus = RECONST_INFO_ERROR;
             return;
@@ -326,7 +326,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         c->kept_mult = ri->iMultiplex;
         c->kept_off = ri->iOffset;
         c->kept_views = views;
-        c->kept_pad = tpad;
+        c->kept_fmt = tfmt;
     }
     // ---- geometry + back-projection ---------------------------------------------------------
     if (nv > 0) {
@@ -358,7 +358,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         bl.out = c->out.p;
         bl.out_slice_stride = (long long)ixdimp * ixdimp;
         bl.mode = RV_MODE_REF;
-        bl.table_pad = tpad;
+        bl.table_fmt = tfmt;
         if (!cuda_ok(launch_backproject(bl, s), RV_ERR_LAUNCH, "back-projection kernel")) {
             ri->iStatus = RECONST_INFO_ERROR;
             return;

@@ -66,7 +66,7 @@ struct FilterLaunch {
     int ic;                   // (int)center
     long long table_stride;   // ints between table slots
     long long row_stride;     // elements between filtered rows
-    int table_pad;            // 1: 17 ints per detector pixel (see ref_table_pad())
+    int table_fmt;            // REF table format, see ref_table_fmt()
 };
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
 
@@ -88,14 +88,19 @@ struct BackprojLaunch {
     long long out_slice_stride;  // elements per output slice
     int center_shift16;       // REF: 16 * integer centre offset added to foffset (R10)
     int mode;
-    int table_pad;            // REF table layout (must match the filter launch)
+    int table_fmt;            // REF table layout (must match the filter launch)
     unsigned int* status_counter;  // validation mode: window-violation counter (else null)
 };
 cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s);
 cudaError_t launch_bp_ref(const BackprojLaunch& p, cudaStream_t s);
-// REF table layout: 16 (dense) or 17 (padded) ints per detector pixel, and the slot stride.
-int ref_table_pad();
-long long ref_table_stride(int ixdimp, int pad);
+// REF table format per detector pixel j, and the slot stride in 4-byte words:
+//   kTabInt16: the reference's 16 ints igp[16j+k]          (64 B per pixel)
+//   kTabInt17: the same with one unused word after each 16  (68 B, fewer bank conflicts)
+//   kTabPair:  the float pair (p0, p1p0) the 16 ints are made from (8 B); the back-projection
+//              evaluates (int)(p0 + p1p0*k) itself with the reference's float operations
+enum { kTabInt16 = 0, kTabInt17 = 1, kTabPair = 2 };
+int ref_table_fmt();
+long long ref_table_stride(int ixdimp, int fmt);
 // status word written by kernels whose bounded waits ran out (0 = fine); read-and-clear
 unsigned int take_kernel_status(cudaStream_t s);
 

@@ -248,10 +248,14 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
                 const float qn = fmul(buf[rbase - j - 1].x, inv_n);
                 p1p0 = fmul(fmul(fsub(qn, qj), 0.0625f), 100.0f);  // (q1-q0)/16*100
             }
+            if (p.table_fmt == kTabPair) {
+                reinterpret_cast<float2*>(tab)[j] = make_float2(p0, p1p0);
+                continue;
+            }
             int v[16];
 #pragma unroll
             for (int k = 0; k < 16; k++) v[k] = __float2int_rz(fadd(p0, fmul(p1p0, (float)k)));
-            if (p.table_pad) {
+            if (p.table_fmt == kTabInt17) {
                 // 17 words per detector pixel (the 17th unused): shared-memory bank spreading
                 int* dst = tab + 17 * (size_t)j;
 #pragma unroll
@@ -264,6 +268,9 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
                 dst[3] = make_int4(v[12], v[13], v[14], v[15]);
             }
         }
+        // pair tables are copied in 16-byte units: an odd row ends with a zero pair
+        if (p.table_fmt == kTabPair && (ixdimp & 1) && tid == 0)
+            reinterpret_cast<float2*>(tab)[ixdimp] = make_float2(0.0f, 0.0f);
     }
     if (p.rows) {
         float* row = p.rows + (size_t)job.dst * p.row_stride;

@@ -69,7 +69,7 @@ extern "C" int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ix
         set_error(RV_ERR_UNSUPPORTED, "RvReconstructSliceNoAlloc: ixdim*zoom beyond 16384");
         return RV_ERR_UNSUPPORTED;
     }
-    const int pad = ref_table_pad();
+    const int pad = ref_table_fmt();
     const long long tstride = ref_table_stride(d.ixdimp, pad);
     // scratch layout: twiddles | filter | row jobs | geometry | tables
     const size_t o_tw = 0;
@@ -123,7 +123,7 @@ extern "C" int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ix
     fl.d = d;
     fl.ic = (int)center;
     fl.table_stride = tstride;
-    fl.table_pad = pad;
+    fl.table_fmt = pad;
     if (!cuda_ok(launch_filter(fl, s), RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
     BackprojLaunch bl{};
     bl.table = reinterpret_cast<const int*>(base + o_tab);
@@ -136,7 +136,7 @@ extern "C" int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ix
     bl.out = d_slice;
     bl.out_slice_stride = (long long)d.ixdimp * d.ixdimp;
     bl.mode = RV_MODE_REF;
-    bl.table_pad = pad;
+    bl.table_fmt = pad;
     if (!cuda_ok(launch_backproject(bl, s), RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
     if (!cuda_ok(cudaStreamSynchronize(s), RV_ERR_LAUNCH, "no-alloc slice")) return RV_ERR_LAUNCH;
     if (take_kernel_status(s)) {

@@ -40,7 +40,7 @@ struct RvStack {
     int nbatches_last = 0;
     float t_filter = 0, t_bp = 0, t_total = 0;
     int launches = 0;
-    int tpad = 0;                   // REF table layout (ref_table_pad at creation)
+    int tfmt = 0;                   // REF table layout (ref_table_fmt at creation)
     long long tstride = 0;          // ints per table slot
 };
 
@@ -143,8 +143,8 @@ extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
     // ---- batch size from the table budget ----------------------------------------------------
     size_t budget_mb = 8192;
     if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
-    st->tpad = ref_table_pad();
-    st->tstride = ref_table_stride(d.ixdimp, st->tpad);
+    st->tfmt = ref_table_fmt();
+    st->tstride = ref_table_stride(d.ixdimp, st->tfmt);
     const size_t per_slice = desc->mode == RV_MODE_REF ? (size_t)V * st->tstride * sizeof(int)
                                                        : (size_t)V * d.ixdimp * (desc->mode == RV_MODE_LIN ? 4 : 2);
     size_t b = (budget_mb << 20) / (per_slice ? per_slice : 1);
@@ -238,7 +238,7 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
         if (mode == RV_MODE_REF) {
             fl.table = static_cast<int*>(st->d_table);
             fl.table_stride = tstride;
-            fl.table_pad = st->tpad;
+            fl.table_fmt = st->tfmt;
         } else if (mode == RV_MODE_LIN) {
             fl.rows = static_cast<float*>(st->d_table);
             fl.row_stride = d.ixdimp;
@@ -268,7 +268,7 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
                                      : (void*)(static_cast<float*>(d_out) + (size_t)s0 * npix);
         bl.out_slice_stride = (long long)npix;
         bl.mode = mode;
-        bl.table_pad = st->tpad;
+        bl.table_fmt = st->tfmt;
         e = launch_backproject(bl, s);
         if (!cuda_ok(e, RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
         cudaEventRecord(st->ev[2], s);

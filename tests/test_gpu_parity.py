@@ -157,9 +157,9 @@ def test_progress_callback_abort(gpu, oracle):
     assert np.array_equal(got, oracle.reconstruct(ri2))
 
 
-@pytest.fixture(params=[(0, 0), (0, 1), (1, 0), (1, 1), (2, 0), (2, 1)], ids=lambda v: f"variant{v[0]}pad{v[1]}")
+@pytest.fixture(params=[(v, f) for f in (0, 1, 2) for v in (0, 1, 2, 3, 4)], ids=lambda v: f"variant{v[0]}fmt{v[1]}")
 def bp_variant(request, gpu):
-    """Every back-projection variant and table layout; restores the default afterwards."""
+    """Every back-projection variant and table format; restores the default afterwards."""
     L = rv.lib()
     old_v, old_p = C.c_int(), C.c_int()
     L.RvGetBackprojectionVariant(C.byref(old_v), C.byref(old_p))
@@ -272,3 +272,27 @@ def test_stack_lin_modes_vs_fp64(gpu, oracle, mode, tol):
         ref64 = oracle.lin64(rs)
         err = rel_l2(got[s][circle], ref64[circle])
         assert err < tol, (mode, s, err)
+
+
+# ---- R9 rescale -------------------------------------------------------------------------------
+@pytest.mark.parametrize("W,V,cen,interp,binning", [(256, 300, 131.3, 2, 1), (128, 120, 60.4, 3, 1),
+                                                    (200, 181, 99.0, 2, 2)])
+def test_rescale_bit_exact(gpu, oracle, W, V, cen, interp, binning):
+    torch = pytest.importorskip("torch")
+    ri = fbp_case(95, W, V, cen, interp, oracle=oracle)
+    sl = oracle.reconstruct(ri)
+    d = rv.dims(W, interp)
+    center_user = cen * binning - 0.5          # ri->center = (c + 0.5) / binning
+    want, imin, imax = oracle.rescale(sl, d.ixdimp, center_user, d.iIntpDim, binning)
+    dev = torch.from_numpy(np.stack([sl, sl[::-1].copy()])).cuda()
+    out16 = torch.zeros(dev.shape, dtype=torch.int16, device="cuda")
+    mm = np.zeros(4, np.int32)
+    rc = rv.lib().RvRescaleSlices(C.c_void_p(dev.data_ptr()), 2, d.ixdimp, center_user, d.iIntpDim, binning,
+                                  C.c_void_p(out16.data_ptr()), mm.ctypes.data_as(C.POINTER(C.c_int)), None)
+    assert rc == 0, rv.last_error()
+    got = dev.cpu().numpy()
+    assert np.array_equal(got[0], want)
+    assert (mm[0], mm[1]) == (imin, imax)
+    want2, _, _ = oracle.rescale(sl[::-1], d.ixdimp, center_user, d.iIntpDim, binning)
+    assert np.array_equal(got[1], want2)
+    assert np.array_equal(out16.cpu().numpy().view(np.uint16)[0].astype(np.int32), want)
