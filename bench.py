@@ -242,6 +242,9 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     build_lib()
     build_oracle()
     torch.cuda.set_device(local_rank)
+    _v, _f = C.c_int(), C.c_int()
+    rv.lib().RvGetBackprojectionVariant(C.byref(_v), C.byref(_f))
+    bp_variant, bp_format = _v.value, _f.value
     dev = torch.device("cuda", local_rank)
     L = rv.lib()
     S = args.slices
@@ -343,7 +346,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "config": {"workload": WORKLOAD, "detector": W_DET, "views": nviews, "slices_per_gpu": S,
                        "output": f"{st.ixdimp}x{st.ixdimp} int32 per slice", "filter": "shepp-logan",
                        "mode": args.mode, "centre": round(center, 4), "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (raw 472 MB, tables 8 GB per batch)"},
+                       "l2": "inputs larger than L2 (raw 472 MB, tables 15 GB)",
+                       "bp_variant": bp_variant, "table_format": bp_format},
             "slices_per_s": S * world * 1e3 / ms,
             "updates_per_s": total_updates / (ms * 1e-3),
             "stage_ms": {"filter": filt_ms, "backprojection": bp_ms},

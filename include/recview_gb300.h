@@ -310,12 +310,30 @@ unsigned long long RvGetWindowViolations(void);
 int RvRescaleSlices(int* d_slices, int nslices, int ixdimp, double center_user, int ipintp, int ibinning,
                     unsigned short* d_out16, int* minmax, void* stream);
 
+/* R11: the reference's automatic centre estimate, CGazoDoc::GetAxis (source/gazoDoc.cpp:4036-4626),
+ * from frames the caller has read: the first sample frame (0 deg), the sample frame nearest
+ * 180 deg minus one step, and a flat, each iydim rows of ixdim uint16 (host).  iAxisOffset > 0
+ * selects the offset-CT branch.  pCenter/pGrad receive the applied line centre(iy) = c + g*iy
+ * (the user-centre convention of the reference: ri->center = (c + 0.5) / binning); pOverall
+ * (may be NULL) the overall SSD centre.  Results equal the reference's. */
+int RvGetAxis(const unsigned short* sample0, const unsigned short* sample1, const unsigned short* flat,
+              int ixdim, int iydim, int iAxisOffset, double* pCenter, double* pGrad, double* pOverall);
+
+/* R11: the axis-scan sweep (source/gazoDoc.cpp:1994-2024) with a score: one slice (nviews
+ * log-normalised int16 rows of ixdim, host) reconstructed at ncent trial centres (ri->center
+ * convention), scores[i] = total variation of trial i inside the circle r < 0.45 ixdimp (this
+ * library's criterion: lowest = sharpest; the reference leaves the choice to a person), and
+ * best_centre = a parabola through the lowest score and its neighbours (equal steps). */
+int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInterpolation, const float* fdeg,
+                  float fTiltAngle, const float* fFilter, const double* centres, int ncent,
+                  double* scores, double* best_centre);
+
 /* Tuning of the REF back-projection (process-wide; affects stacks created and slices reconstructed
  * afterwards).  format: 0 = the reference's 16-int table per detector pixel, 1 = the same padded
  * to 17 words (fewer shared-memory bank conflicts), 2 = the float pair (p0, slope) per
  * detector pixel, expanded by the kernel with the reference's operations (8x smaller tables,
  * conflict-free lookups).  variant 0..4 selects tile shape / threads / views per chunk (default:
- * format 0, variant 0, the fastest measured on GB300).  All
+ * format 0, variant 3, the fastest measured on GB300).  All
  * combinations give bit-identical slices. */
 int RvSetBackprojectionVariant(int variant, int format);
 int RvGetBackprojectionVariant(int* variant, int* format);

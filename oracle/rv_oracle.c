@@ -654,3 +654,153 @@ int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
     free(buf); free(fre);
     return 0;
 }
+
+/* ---------------------------------------------------------------- R11 ------------------- */
+static short rvo_d2s_x64(double v) {
+    /* (short)(double) as the reference's x64 build performs it: via a 32-bit conversion whose
+     * out-of-range / NaN result is 0x80000000 (low 16 bits 0). */
+    if (!(v > -2147483649.0 && v < 2147483648.0)) return 0;
+    return (short)(int)v;
+}
+
+int rvo_get_axis(const unsigned short* s0in, const unsigned short* s1in, const unsigned short* inc0,
+                 int ixdim, int iydim, int iAxisOffset, double* pCenter, double* pGrad, double* pOverall) {
+    /* CGazoDoc::GetAxis after the frame reads (source/gazoDoc.cpp:4379-4626) */
+    const int ixydim = ixdim * iydim;
+    const int tail = 2 * ixdim + 16;
+    int* S0 = (int*)calloc((size_t)ixydim + tail, sizeof(int));
+    int* S1 = (int*)calloc((size_t)ixydim + tail, sizeof(int));
+    const int ixdimh = ixdim / 5 > 100 ? ixdim / 5 : 100;
+    const int istep = iydim < 40 ? 1 : iydim / 40;
+    const int icdim = (int)ceil(iydim / (double)istep);
+    double* sdiff = (double*)calloc((size_t)ixdimh * 2, sizeof(double));
+    double* center = (double*)calloc((size_t)icdim, sizeof(double));
+    double* sdifftotal = (double*)calloc((size_t)ixdimh * 2, sizeof(double));
+    int* ndifftotal = (int*)calloc((size_t)ixdimh * 2, sizeof(int));
+    if (!S0 || !S1 || !sdiff || !center || !sdifftotal || !ndifftotal) {
+        free(S0); free(S1); free(sdiff); free(center); free(sdifftotal); free(ndifftotal);
+        return RV_ERR_HOST_ALLOC;
+    }
+    for (int j = 0; j < ixydim; j++) {
+        S0[j] = rvo_d2s_x64(log((double)inc0[j] / (double)s0in[j]) * RV_LOG_SCALE);
+        S1[j] = rvo_d2s_x64(log((double)inc0[j] / (double)s1in[j]) * RV_LOG_SCALE);
+    }
+    for (int k = 0; k < iydim; k += istep) {
+        const int icidx = k / istep;
+        float minDiff = SHRT_MAX;
+        int minIdx = 0;
+        const int kix = k * ixdim;
+        int ixCenter2;
+        if (iAxisOffset) {
+            const int scan = (iAxisOffset < ixdim / 2) ? iAxisOffset / 2 : (ixdim - iAxisOffset) / 2;
+            for (int js = -ixdimh; js < ixdimh; js++) {
+                const int idx = js + ixdimh, j = js + iAxisOffset;
+                sdiff[idx] = 0;
+                if (abs(js) > scan) continue;
+                int nd = 0;
+                for (int i = -scan; i <= scan; i++) {
+                    const int d = S1[j - i + kix] - S0[j + i + kix];
+                    sdiff[idx] += (double)d * d;
+                    nd++;
+                    sdifftotal[idx] += (double)d * d;
+                    ndifftotal[idx]++;
+                }
+                if (nd == 0) continue;
+                sdiff[idx] /= nd;
+                if (sdiff[idx] < minDiff) { minDiff = (float)sdiff[idx]; minIdx = js; }
+            }
+            ixCenter2 = (minIdx + iAxisOffset) * 2;
+        } else {
+            for (int j = -ixdimh; j < ixdimh; j++) {
+                const int idx = j + ixdimh;
+                sdiff[idx] = 0;
+                int nd = 0;
+                const int ifrom = j >= 0 ? 0 : -j;
+                const int ito = j >= 0 ? ixdim - j : ixdim;
+                for (int i = ifrom; i < ito; i++) {
+                    const int d = S1[ixdim - 1 - i + kix] - S0[i + j + kix];
+                    sdiff[idx] += (double)d * d;
+                    nd++;
+                    sdifftotal[idx] += (double)d * d;
+                    ndifftotal[idx]++;
+                }
+                if (nd == 0) continue;
+                sdiff[idx] /= nd;
+                if (sdiff[idx] < minDiff) { minDiff = (float)sdiff[idx]; minIdx = j; }
+            }
+            ixCenter2 = minIdx + ixdim - 1;
+        }
+        center[icidx] = 0;
+        if ((minIdx == -ixdimh) || (minIdx == ixdimh - 1)) {
+            center[icidx] = ixCenter2 / 2.;
+        } else {
+            const double dy1 = sdiff[minIdx + ixdimh];
+            double dy0 = sdiff[minIdx - 1 + ixdimh];
+            const double dy2 = sdiff[minIdx + 1 + ixdimh];
+            if (dy2 == dy0) center[icidx] = (double)(ixCenter2 / 2.);
+            else {
+                dy0 = (dy1 - dy0) / (dy2 - dy0);
+                center[icidx] = (4 * dy0 * ixCenter2 - (ixCenter2 * 2 - 1)) / (4 * dy0 - 2) / 2;
+            }
+        }
+        center[icidx] -= 0.5;
+    }
+    double minDifftotal = SHRT_MAX;
+    int idifftotal = 0;
+    for (int j = -ixdimh; j < ixdimh; j++) {
+        const int idx = j + ixdimh;
+        if (ndifftotal[idx] == 0) continue;
+        sdifftotal[idx] /= ndifftotal[idx];
+        if (sdifftotal[idx] < minDifftotal) { minDifftotal = sdifftotal[idx]; idifftotal = j; }
+    }
+    const int ixCenter2total = iAxisOffset ? (idifftotal + iAxisOffset) * 2 : idifftotal + ixdim - 1;
+    double dcentertotal = ixCenter2total / 2.;
+    if ((idifftotal > -ixdimh) && (idifftotal < ixdimh - 1)) {
+        const double dy1 = sdifftotal[idifftotal + ixdimh];
+        double dy0 = sdifftotal[idifftotal - 1 + ixdimh];
+        const double dy2 = sdifftotal[idifftotal + 1 + ixdimh];
+        if (dy2 != dy0) {
+            dy0 = (dy1 - dy0) / (dy2 - dy0);
+            dcentertotal = (4 * dy0 * ixCenter2total - (ixCenter2total * 2 - 1)) / (4 * dy0 - 2) / 2;
+        }
+    }
+    dcentertotal -= 0.5;
+    const double cavg = dcentertotal, csig = 1;
+    int isig1 = 0, isig2 = 0, nsig = 0;
+    double sigc = 0, sigcx = 0;
+    for (int k = 0; k < iydim; k += istep) {
+        const int icidx = k / istep;
+        if (fabs(cavg - center[icidx]) > csig * 3) continue;
+        isig1 += k;
+        isig2 = (int)((unsigned)isig2 + (unsigned)k * (unsigned)k);   /* int arithmetic wraps */
+        sigc += center[icidx];
+        sigcx += k * center[icidx];
+        nsig++;
+    }
+    const int den = (int)((unsigned)nsig * (unsigned)isig2 - (unsigned)isig1 * (unsigned)isig1);
+    double coeffb = (isig2 * sigc - isig1 * sigcx) / den;
+    double coeffa = (sigc - nsig * coeffb) / isig1;
+    if (nsig < iydim / istep / 2) { isig1 = 1; coeffb = dcentertotal; coeffa = 0; }
+    else isig1 = 0;
+    if ((coeffb < 0) || isig1) { *pCenter = dcentertotal; *pGrad = 0; }
+    else { *pCenter = coeffb; *pGrad = coeffa; }
+    if (pOverall) *pOverall = dcentertotal;
+    free(S0); free(S1); free(sdiff); free(center); free(sdifftotal); free(ndifftotal);
+    return 0;
+}
+
+double rvo_tv_score(const int* slice, int ixdimp) {
+    /* project-defined sharpness score of a centre sweep: total variation inside r < 0.45 ixdimp */
+    const double h = ixdimp / 2.0, r2 = (0.45 * ixdimp) * (0.45 * ixdimp);
+    double acc = 0.0;
+    for (int y = 0; y < ixdimp - 1; y++)
+        for (int x = 0; x < ixdimp - 1; x++) {
+            const double dx = x - h, dy = y - h;
+            if (dx * dx + dy * dy >= r2) continue;
+            const double v = slice[(size_t)y * ixdimp + x];
+            const double gx = slice[(size_t)y * ixdimp + x + 1] - v;
+            const double gy = slice[(size_t)(y + 1) * ixdimp + x] - v;
+            acc += sqrt(gx * gx + gy * gy);
+        }
+    return acc;
+}

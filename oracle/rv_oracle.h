@@ -75,6 +75,14 @@ void rvo_rescale(int* slice, int ixdimp, double center_user, int ipintp, int ibi
  * int32 reference (x BACKPROJ_SCALE) so the two are directly comparable. */
 int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out);
 
+/* R11: CGazoDoc::GetAxis after the frame reads (source/gazoDoc.cpp:4379-4626): 0-degree frame,
+ * ~180-degree frame and flat, ixdim x iydim each; returns the applied centre/gradient and the
+ * overall SSD centre. */
+int rvo_get_axis(const unsigned short* s0, const unsigned short* s1, const unsigned short* flat,
+                 int ixdim, int iydim, int iAxisOffset, double* pCenter, double* pGrad, double* pOverall);
+/* Project-defined centre-sweep score: total variation inside the circle r < 0.45 ixdimp. */
+double rvo_tv_score(const int* slice, int ixdimp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -187,6 +187,10 @@ PROTOTYPES = {
     "RvProbeThroughput": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "RvRescaleSlices": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
                                   c_int_p, C.c_void_p]),
+    "RvGetAxis": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                            C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "RvCentreSweep": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, c_float_p, C.c_float, c_float_p,
+                                C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "RvSetBackprojectionVariant": (C.c_int, [C.c_int, C.c_int]),
     "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
     "RvReconstructSliceNoAlloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, c_float_p,

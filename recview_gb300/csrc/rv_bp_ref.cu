@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
     auto prepare = [&](int c, int ms) {
         const int v0 = c * VC;
         if (tid < VC && v0 + tid < nviews) {
-            const float4 g = __ldg(p.geom + v0 + tid);
+            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + tid);
             float lo = 3.0e38f, hi = -3.0e38f;
 #pragma unroll
             for (int cy = 0; cy < 2; cy++) {
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
         for (int e = tid; e < VC * (TX + TY); e += NT) {
             const int vv = e / (TX + TY), w = e - vv * (TX + TY);
             if (v0 + vv >= nviews) continue;
-            const float4 g = __ldg(p.geom + v0 + vv);
+            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + vv);
             if (w < TX) {
                 const int t = w / RX, c = w - t * RX;          // xs[t*RX + c] = column of (tx=t, c)
                 xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
     auto prepare = [&](int c, int ms) {
         const int v0 = c * VC;
         if (tid < VC && v0 + tid < nviews) {
-            const float4 g = __ldg(p.geom + v0 + tid);
+            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + tid);
             float lo = 3.0e38f, hi = -3.0e38f;
 #pragma unroll
             for (int cy = 0; cy < 2; cy++) {
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
         for (int e = tid; e < VC * (TX + TY); e += NT) {
             const int vv = e / (TX + TY), w = e - vv * (TX + TY);
             if (v0 + vv >= nviews) continue;
-            const float4 g = __ldg(p.geom + v0 + vv);
+            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + vv);
             if (w < TX) {
                 const int t = w / RX, c = w - t * RX;
                 xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
@@ -528,7 +528,7 @@ static int env_int(const char* name, int dflt) {
 }
 static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
-    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 0);
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 3);
     if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
 int ref_table_fmt() {

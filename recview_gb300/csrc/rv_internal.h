@@ -46,7 +46,7 @@ struct RowJob {
     float t0;        // raw mode: flat interpolation weight (source/general.cpp:2443-2447)
     int dst;         // output slot (view-major within a slice: slice * nviews + v)
     int zero;        // 1: the row is all zero (SKIP frame)
-    int pad;
+    int ic;          // integer centre of this row when FilterLaunch::ic_per_job is set
 };
 
 struct FilterLaunch {
@@ -64,6 +64,7 @@ struct FilterLaunch {
     int mode;
     Dims d;
     int ic;                   // (int)center
+    int ic_per_job;           // 1: take the integer centre from each RowJob (centre sweeps)
     long long table_stride;   // ints between table slots
     long long row_stride;     // elements between filtered rows
     int table_fmt;            // REF table format, see ref_table_fmt()
@@ -77,6 +78,7 @@ struct BackprojLaunch {
     const void* rows16;       // LIN_F16/BF16 rows
     const float* row_scale;
     const float4* geom;       // per view {fcos, fsin, foffset, 0} (REF units: x16)
+    long long geom_slice_stride;  // float4s between the geometry of consecutive slices (0: shared)
     int nviews;               // views per slice
     int nslices;
     int ixdimp;

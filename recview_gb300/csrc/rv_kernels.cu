@@ -114,8 +114,9 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
     // ---- R5: placement with edge padding and integer zoom (source/general.cpp:2105-2126) ------
     {
         const int z = p.d.iIntpDim;
-        const int idx0 = (0 - p.ic) * z + (half - 1);
-        const int idx1 = (W - 1 - p.ic) * z + (half - 1) + 1;
+        const int ic = p.ic_per_job ? job.ic : p.ic;
+        const int idx0 = (0 - ic) * z + (half - 1);
+        const int idx1 = (W - 1 - ic) * z + (half - 1) + 1;
         for (int m = tid; m < n; m += NT) {
             float v;
             if (m < idx0) v = strip[0];
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(BP_THREADS, 2) k_bp_lin(BackprojLaunch p) {
     for (int v0 = 0; v0 < nviews; v0 += VC) {
         const int nv = min(VC, nviews - v0);
         if (tid < nv) {
-            const float4 g = __ldg(p.geom + v0 + tid);
+            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + tid);
             float lo = 3.0e38f;
 #pragma unroll
             for (int cy = 0; cy < 2; cy++)
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(BP_THREADS, 2) k_bp_lin(BackprojLaunch p) {
         for (int e = tid; e < VC * 128; e += BP_THREADS) {
             const int vv = e >> 7, w = e & 127;
             if (vv >= nv) continue;
-            const float4 g = __ldg(p.geom + v0 + vv);
+            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + vv);
             if (w < 64) xs[vv][w] = (float)(X0 + (w >> 2) + 16 * (w & 3)) * g.x;
             else {
                 const int ww = w - 64;

@@ -7,7 +7,7 @@
 //   rows     [batch * V * ixdimp]        f32/f16/bf16 LIN: filtered rows x100 (+ per-row scale)
 //   out      [nslices * ixdimp^2]        int32 (REF) / f32 (LIN)
 // Slices are processed in batches so the tables stay within a device-memory budget
-// (RV_TABLE_BUDGET_MB, default 8192).
+// (RV_TABLE_BUDGET_MB, default 32768).
 #include <cuda_runtime.h>
 #include <stdlib.h>
 #include <string.h>
@@ -141,7 +141,7 @@ extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
     }
     st->filt.assign(desc->fFilter, desc->fFilter + d.ndim);
     // ---- batch size from the table budget ----------------------------------------------------
-    size_t budget_mb = 8192;
+    size_t budget_mb = 32768;
     if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
     st->tfmt = ref_table_fmt();
     st->tstride = ref_table_stride(d.ixdimp, st->tfmt);

@@ -108,6 +108,19 @@ def main() -> None:
         out[f"{name}_fexp"] = fexp
         out[f"{name}_out"] = r
         out[f"{name}_params"] = np.array([flags, iflag])
+    # GetAxis (centre estimate from the 0 / ~180 degree frames and a flat)
+    U16P = C.POINTER(C.c_ushort)
+    ref.rvref_get_axis.argtypes = [U16P, U16P, U16P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]
+    for name, seed, W, S, V, cen, off in (("axis_a", 11, 160, 48, 120, 81.3, 0), ("axis_b", 12, 128, 40, 90, 58.7, 0),
+                                          ("axis_off", 13, 160, 24, 120, 110.4, 110)):
+        raw, bInc, fdeg, fexp, _ = phantom.raw_stack(seed, W, V, S, cen, n_ellipsoids=10)
+        s0, s1, fl = (np.ascontiguousarray(raw[i]) for i in (1, V, 0))
+        a, b = C.c_double(), C.c_double()
+        ref.rvref_get_axis(s0.ctypes.data_as(U16P), s1.ctypes.data_as(U16P), fl.ctypes.data_as(U16P), W, S, off,
+                           C.byref(a), C.byref(b))
+        out[f"{name}_frames"] = np.stack([s0, s1, fl])
+        out[f"{name}_params"] = np.array([off, a.value, b.value])
     dst = Path(__file__).with_name("golden.npz")
     np.savez_compressed(dst, **out)
     print(f"wrote {dst} ({dst.stat().st_size} bytes, {len(out)} arrays)")

@@ -30,6 +30,11 @@ class Oracle:
         L.rvo_reconstruct_lin64.argtypes = [RIP, C.POINTER(C.c_double)]
         L.rvo_rescale.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_double, C.c_int, C.c_int,
                                   C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        U16P = C.POINTER(C.c_ushort)
+        DP = C.POINTER(C.c_double)
+        L.rvo_get_axis.argtypes = [U16P, U16P, U16P, C.c_int, C.c_int, C.c_int, DP, DP, DP]
+        L.rvo_tv_score.argtypes = [C.POINTER(C.c_int), C.c_int]
+        L.rvo_tv_score.restype = C.c_double
 
     def set_filter(self, kind, ndim, cutoff=0.5, order=2.0):
         t = np.zeros(ndim, np.float32)
@@ -64,6 +69,18 @@ class Oracle:
         self.L.rvo_reconstruct_lin64(C.byref(ri.ri), out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
+    def get_axis(self, s0, s1, flat, offset=0):
+        U16P = C.POINTER(C.c_ushort)
+        a, b, o = C.c_double(), C.c_double(), C.c_double()
+        s0, s1, flat = (np.ascontiguousarray(x, np.uint16) for x in (s0, s1, flat))
+        assert self.L.rvo_get_axis(s0.ctypes.data_as(U16P), s1.ctypes.data_as(U16P), flat.ctypes.data_as(U16P),
+                                   s0.shape[1], s0.shape[0], offset, C.byref(a), C.byref(b), C.byref(o)) == 0
+        return a.value, b.value, o.value
+
+    def tv_score(self, slice_):
+        s = np.ascontiguousarray(slice_, np.int32)
+        return self.L.rvo_tv_score(s.ctypes.data_as(C.POINTER(C.c_int)), s.shape[0])
+
     def rescale(self, slice_, ixdimp, center_user, ipintp=1, ibinning=1):
         s = np.ascontiguousarray(slice_, np.int32).copy()
         imin, imax = C.c_int(), C.c_int()
@@ -81,6 +98,9 @@ def ref_lib():
     L.rvref_fbp.argtypes = [RIP]
     L.rvref_gen_sinogram.argtypes = [RIP]
     L.rvref_fft.argtypes = [C.c_int, C.c_int, F32P, F32P]
+    U16P = C.POINTER(C.c_ushort)
+    L.rvref_get_axis.argtypes = [U16P, U16P, U16P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]
     return L
 
 

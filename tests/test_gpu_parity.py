@@ -296,3 +296,36 @@ def test_rescale_bit_exact(gpu, oracle, W, V, cen, interp, binning):
     want2, _, _ = oracle.rescale(sl[::-1], d.ixdimp, center_user, d.iIntpDim, binning)
     assert np.array_equal(got[1], want2)
     assert np.array_equal(out16.cpu().numpy().view(np.uint16)[0].astype(np.int32), want)
+
+
+# ---- R11 centre methods -----------------------------------------------------------------------
+@pytest.mark.parametrize("seed,W,S,V,cen,off", [(1, 256, 48, 180, 131.3, 0), (3, 300, 100, 360, 140.25, 0),
+                                                (4, 160, 30, 100, 120.2, 120), (6, 2048, 64, 60, 1030.6, 0)])
+def test_get_axis_matches_oracle(gpu, oracle, seed, W, S, V, cen, off):
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(seed, W, V, S, cen, n_ellipsoids=12)
+    s0, s1, fl = (np.ascontiguousarray(raw[i]) for i in (1, V, 0))
+    want = oracle.get_axis(s0, s1, fl, off)
+    a, b, o = C.c_double(), C.c_double(), C.c_double()
+    rc = rv.lib().RvGetAxis(s0.ctypes.data, s1.ctypes.data, fl.ctypes.data, W, S, off, C.byref(a), C.byref(b), C.byref(o))
+    assert rc == 0, rv.last_error()
+    assert (a.value, b.value, o.value) == want
+
+
+@pytest.mark.parametrize("seed,W,V,cen", [(7, 256, 300, 131.3), (8, 512, 600, 247.8)])
+def test_centre_sweep(gpu, oracle, seed, W, V, cen):
+    sino, fdeg = phantom.sinogram_2d(seed, W, V, cen)
+    F = oracle.set_filter(abi.FILT_SHEPP, rv.dims(W).ndim)
+    centres = np.round(cen) + np.arange(-4.0, 4.01, 0.5)
+    scores = np.zeros(len(centres))
+    best = C.c_double()
+    rc = rv.lib().RvCentreSweep(sino.ctypes.data, V, W, 2, fdeg.ctypes.data_as(C.POINTER(C.c_float)), 0.0,
+                                F.ctypes.data_as(C.POINTER(C.c_float)),
+                                centres.ctypes.data_as(C.POINTER(C.c_double)), len(centres),
+                                scores.ctypes.data_as(C.POINTER(C.c_double)), C.byref(best))
+    assert rc == 0, rv.last_error()
+    bInc = np.ones(V, np.int8)
+    for i in (0, int(np.argmin(scores)), len(centres) - 1):
+        ri = ReconInfo(sino, fdeg, bInc, center=float(centres[i]), fFilter=F)
+        want = oracle.tv_score(oracle.reconstruct(ri))
+        assert abs(scores[i] - want) <= 1e-9 * want
+    assert abs(best.value - cen) <= 0.25, (best.value, cen)

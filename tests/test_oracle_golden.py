@@ -69,3 +69,11 @@ def test_oracle_threads_equal_single(oracle):
     one = oracle.reconstruct(ri, threads=1)
     many = oracle.reconstruct(ri, threads=5)
     assert np.array_equal(one, many)
+
+
+@pytest.mark.parametrize("name", ["axis_a", "axis_b", "axis_off"])
+def test_get_axis_bit_exact(golden, oracle, name):
+    s0, s1, fl = golden[f"{name}_frames"]
+    off, c, g = golden[f"{name}_params"]
+    got = oracle.get_axis(s0, s1, fl, int(off))
+    assert got[0] == c and got[1] == g

@@ -53,3 +53,17 @@ def test_normalisation_random(oracle, flags, drift):
             REF.rvref_gen_sinogram(C.byref(ri.ri))
         outs.append(r)
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("seed,W,S,V,cen,off", [(1, 256, 48, 180, 131.3, 0), (2, 200, 40, 90, 97.8, 0),
+                                                (3, 300, 100, 360, 140.25, 0), (4, 160, 30, 100, 120.2, 120),
+                                                (5, 160, 30, 100, 40.7, 40)])
+def test_get_axis_random(oracle, seed, W, S, V, cen, off):
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(seed, W, V, S, cen, n_ellipsoids=12)
+    s0, s1, fl = (np.ascontiguousarray(raw[i]) for i in (1, V, 0))
+    a, b = C.c_double(), C.c_double()
+    U16P = C.POINTER(C.c_ushort)
+    REF.rvref_get_axis(s0.ctypes.data_as(U16P), s1.ctypes.data_as(U16P), fl.ctypes.data_as(U16P), W, S, off,
+                       C.byref(a), C.byref(b))
+    got = oracle.get_axis(s0, s1, fl, off)
+    assert (got[0], got[1]) == (a.value, b.value)
