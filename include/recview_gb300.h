@@ -310,6 +310,25 @@ unsigned long long RvGetWindowViolations(void);
 int RvRescaleSlices(int* d_slices, int nslices, int ixdimp, double center_user, int ipintp, int ibinning,
                     unsigned short* d_out16, int* minmax, void* stream);
 
+/* ---- batched queue (no reference counterpart; replaces the sequential queue loop of
+ * source/DlgQueue.cpp:363-470 / CGazoDoc::BatchReconst, source/gazoDoc.cpp:1938-1993) --------
+ * Datasets of uneven detector width, view count, centre and zoom are added as stack descriptions
+ * with device buffers (raw frames in, int32 slices out).  RvQueueRun groups their slices into
+ * waves whose tables fit a device-memory pool (RV_TABLE_BUDGET_MB, default 32768), runs each
+ * wave as one filter launch per dataset plus one persistent back-projection kernel that takes
+ * tiles of every dataset from a device work list, captures the whole sequence in a CUDA graph on
+ * the first run and replays the graph afterwards.  REF mode only; results equal RvStackRunDevice's.
+ * RvQueueAutotune (optional, before the first run) times the tile-shape variants of the
+ * persistent kernel on this queue and keeps the fastest. */
+typedef struct RvQueue RvQueue;
+int RvQueueCreate(RvQueue** out);
+int RvQueueAdd(RvQueue* q, const RvStackDesc* desc, const void* d_raw, void* d_out);
+int RvQueueAutotune(RvQueue* q, void* stream, int* chosen_variant);
+int RvQueueRun(RvQueue* q, void* stream);
+float RvQueueLastMs(const RvQueue* q);        /* device time of the last run */
+double RvQueueUpdates(const RvQueue* q);      /* pixel-view updates of one run */
+void RvQueueDestroy(RvQueue* q);
+
 /* R11: the reference's automatic centre estimate, CGazoDoc::GetAxis (source/gazoDoc.cpp:4036-4626),
  * from frames the caller has read: the first sample frame (0 deg), the sample frame nearest
  * 180 deg minus one step, and a flat, each iydim rows of ixdim uint16 (host).  iAxisOffset > 0
@@ -332,7 +351,7 @@ int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInterpolation, 
  * afterwards).  format: 0 = the reference's 16-int table per detector pixel, 1 = the same padded
  * to 17 words (fewer shared-memory bank conflicts), 2 = the float pair (p0, slope) per
  * detector pixel, expanded by the kernel with the reference's operations (8x smaller tables,
- * conflict-free lookups).  variant 0..4 selects tile shape / threads / views per chunk (default:
+ * conflict-free lookups).  variant 0..5 selects tile shape / threads / views per chunk (default:
  * format 0, variant 3, the fastest measured on GB300).  All
  * combinations give bit-identical slices. */
 int RvSetBackprojectionVariant(int variant, int format);

@@ -191,6 +191,13 @@ PROTOTYPES = {
                             C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "RvCentreSweep": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, c_float_p, C.c_float, c_float_p,
                                 C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "RvQueueCreate": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "RvQueueAdd": (C.c_int, [C.c_void_p, C.POINTER(RvStackDesc), C.c_void_p, C.c_void_p]),
+    "RvQueueAutotune": (C.c_int, [C.c_void_p, C.c_void_p, c_int_p]),
+    "RvQueueRun": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "RvQueueLastMs": (C.c_float, [C.c_void_p]),
+    "RvQueueUpdates": (C.c_double, [C.c_void_p]),
+    "RvQueueDestroy": (None, [C.c_void_p]),
     "RvSetBackprojectionVariant": (C.c_int, [C.c_int, C.c_int]),
     "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
     "RvReconstructSliceNoAlloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, c_float_p,

@@ -103,42 +103,34 @@ struct ViewMeta {
     int pad0, pad1, pad2;
 };
 
-template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, bool CHECKED>
-__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p) {
+// One tile of one slice.  ph[b] counts the completed phases of mbarrier b, so a persistent CTA
+// can run many tiles on the same barriers.  Returns false when a bounded wait ran out.
+template <int WX, int WY, int RX, int RY, int VC, int PAD, bool CHECKED>
+__device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned (&ph)[2], unsigned* status_counter) {
     using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
     constexpr int NT = Cfg::NT, TX = Cfg::TX, TY = Cfg::TY, WIN = Cfg::WIN;
-    extern __shared__ __align__(128) int smi[];
     int* win = smi;                                                     // [2][VC][WIN]
     float* xs = reinterpret_cast<float*>(win + 2 * VC * WIN);           // [3][VC][TX]
     float* ys = xs + 3 * VC * TX;                                       // [3][VC][TY]
     ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * TY);     // [3][VC]
     uint64_t* bars = reinterpret_cast<uint64_t*>(meta + 3 * VC);        // [2]
 
-    const int ixdimp = p.ixdimp;
-    const int tiles_x = (ixdimp + TX - 1) / TX;
-    const int X0 = (blockIdx.x % tiles_x) * TX;
-    const int Y0 = (blockIdx.x / tiles_x) * TY;
-    const int slice = blockIdx.y;
+    const int ixdimp = J.ixdimp;
+    const int X0 = J.X0, Y0 = J.Y0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % WX) * 8 + (lane & 7);
     const int ty = (warp / WX) * 4 + (lane >> 3);
-    const int* tab = p.table + (size_t)slice * p.slice_table_stride;
+    const int* tab = J.table;
     const int nstore = PAD ? ((17 * ixdimp + 3) & ~3) : 16 * ixdimp;   // storage words per table row
-    const int nviews = p.nviews;
+    const int nviews = J.nviews;
     const int nchunks = (nviews + VC - 1) / VC;
     unsigned viol = 0;
-
-    if (tid == 0) {
-        mbar_init(smem_u32(&bars[0]), 1);
-        mbar_init(smem_u32(&bars[1]), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
 
     // window bounds and tabulated products of chunk c into meta/xs/ys slot ms
     auto prepare = [&](int c, int ms) {
         const int v0 = c * VC;
         if (tid < VC && v0 + tid < nviews) {
-            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + tid);
+            const float4 g = __ldg(J.geom + v0 + tid);
             float lo = 3.0e38f, hi = -3.0e38f;
 #pragma unroll
             for (int cy = 0; cy < 2; cy++) {
@@ -166,13 +158,20 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
             m.a = max(m.w0, 0);
             m.b = min(m.w0 + m.nwin, nstore);
             m.fast = (lo >= 2.0f) ? 1 : 0;
-            m.pad0 = m.pad1 = m.pad2 = 0;
+            m.pad1 = (m.a != m.w0 || m.b != m.w0 + m.nwin) ? 1 : 0;   // needs zero-fill
+            m.pad2 = 0;
+            // byte offset that turns the index bits into a shared-memory address (fast/slow path)
+            {   // unsigned arithmetic: the offset is a 32-bit wrap-around quantity
+                const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
+                const unsigned off = 0u - 4u * (unsigned)m.w0 - (m.fast ? 4u * mag : 0u);
+                m.pad0 = (int)off;
+            }
             meta[ms * VC + tid] = m;
         }
         for (int e = tid; e < VC * (TX + TY); e += NT) {
             const int vv = e / (TX + TY), w = e - vv * (TX + TY);
             if (v0 + vv >= nviews) continue;
-            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + vv);
+            const float4 g = __ldg(J.geom + v0 + vv);
             if (w < TX) {
                 const int t = w / RX, c = w - t * RX;          // xs[t*RX + c] = column of (tx=t, c)
                 xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
@@ -198,13 +197,14 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
             for (int vv = 0; vv < nv; vv++) {
                 const ViewMeta m = meta[ms * VC + vv];
                 if (m.b <= m.a) continue;
-                const int* src = tab + (size_t)(v0 + vv) * p.table_stride + m.a;
+                const int* src = tab + (size_t)(v0 + vv) * J.table_stride + m.a;
                 const unsigned dst = smem_u32(win + (wb * VC + vv) * WIN + (m.a - m.w0));
                 tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
             }
         }
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[ms * VC + vv];
+            if (!m.pad1) continue;   // window entirely inside the table: nothing to zero
             int4* w4 = reinterpret_cast<int4*>(win + (wb * VC + vv) * WIN);
             const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;   // [0, za) zero
             const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;   // [zb, nwin) zero
@@ -228,15 +228,16 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
         const int wb = k & 1, ms = k % 3;
         if (k + 1 < nchunks) stage(k + 1, (k + 1) % 3, wb ^ 1);
         if (k + 2 < nchunks) prepare(k + 2, (k + 2) % 3);
-        const bool ok = mbar_wait_bounded(smem_u32(&bars[wb]), (unsigned)(k >> 1) & 1u);
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[wb]), ph[wb] & 1u);
         if (__syncthreads_or(!ok)) {
             // a bulk copy did not complete in time: report, give the copies a bounded last
             // chance to land, and leave without touching the output
             if (tid == 0) atomicOr(&g_kernel_status, 1u);
-            mbar_wait_bounded(smem_u32(&bars[wb]), (unsigned)(k >> 1) & 1u);
-            if (k + 1 < nchunks) mbar_wait_bounded(smem_u32(&bars[wb ^ 1]), (unsigned)((k + 1) >> 1) & 1u);
-            return;
+            mbar_wait_bounded(smem_u32(&bars[wb]), ph[wb] & 1u);
+            if (k + 1 < nchunks) mbar_wait_bounded(smem_u32(&bars[wb ^ 1]), ph[wb ^ 1] & 1u);
+            return false;
         }
+        ph[wb]++;
         const int nv = min(VC, nviews - k * VC);
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[ms * VC + vv];
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
             const unsigned wbase = smem_u32(win + (wb * VC + vv) * WIN) - 4u * (unsigned)m.w0;
             if (m.fast) {
                 // index v = bits - 2^23 pattern; PAD: storage = v + (v >> 4)
-                const unsigned base = PAD ? wbase - 4u * (kMagicBits + (kMagicBits >> 4)) : wbase - 4u * kMagicBits;
+                const unsigned base = smem_u32(win + (wb * VC + vv) * WIN) + (unsigned)m.pad0;
 #pragma unroll
                 for (int r = 0; r < RY; r++)
 #pragma unroll
@@ -286,9 +287,9 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
         }
         __syncthreads();
     }
-    if (CHECKED && viol) atomicAdd(p.status_counter, viol);
+    if (CHECKED && viol) atomicAdd(status_counter, viol);
 
-    int* out = static_cast<int*>(p.out) + (size_t)slice * p.out_slice_stride;
+    int* out = J.out;
 #pragma unroll
     for (int r = 0; r < RY; r++) {
         const int y = Y0 + ty + Cfg::GY * r;
@@ -298,6 +299,58 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
             const int x = X0 + tx + Cfg::GX * c;
             if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
         }
+    }
+    __syncthreads();   // the next tile of a persistent CTA reuses the shared buffers
+    return true;
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int PAD>
+__device__ __forceinline__ void bp_init_barriers(int* smi) {
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + 2 * VC * Cfg::WIN + 3 * VC * (Cfg::TX + Cfg::TY) + 3 * VC * 8);
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bars[0]), 1);
+        mbar_init(smem_u32(&bars[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+}
+
+// Grid form: blockIdx.x = tile, blockIdx.y = slice.
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, bool CHECKED>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p) {
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    extern __shared__ __align__(128) int smi[];
+    bp_init_barriers<WX, WY, RX, RY, VC, PAD>(smi);
+    const int tiles_x = (p.ixdimp + Cfg::TX - 1) / Cfg::TX;
+    TileJob J;
+    J.table = p.table + (size_t)blockIdx.y * p.slice_table_stride;
+    J.geom = p.geom + (size_t)blockIdx.y * p.geom_slice_stride;
+    J.out = static_cast<int*>(p.out) + (size_t)blockIdx.y * p.out_slice_stride;
+    J.table_stride = p.table_stride;
+    J.nviews = p.nviews;
+    J.ixdimp = p.ixdimp;
+    J.X0 = (blockIdx.x % tiles_x) * Cfg::TX;
+    J.Y0 = (blockIdx.x / tiles_x) * Cfg::TY;
+    unsigned ph[2] = {0u, 0u};
+    bp_ref_tile<WX, WY, RX, RY, VC, PAD, CHECKED>(J, smi, ph, p.status_counter);
+}
+
+// Persistent form: each CTA takes tiles from a device work list (uneven datasets) until it is
+// exhausted; *counter must be zero at launch.
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_persistent(const TileJob* jobs, int njobs,
+                                                                          unsigned* counter) {
+    extern __shared__ __align__(128) int smi[];
+    __shared__ int s_item;
+    bp_init_barriers<WX, WY, RX, RY, VC, PAD>(smi);
+    unsigned ph[2] = {0u, 0u};
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= njobs) break;
+        if (!bp_ref_tile<WX, WY, RX, RY, VC, PAD, false>(jobs[it], smi, ph, nullptr)) return;
     }
 }
 
@@ -519,6 +572,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //     2: 128x128, 512 threads, 4 views/chunk
 //     3: 64x64, 256 threads, 16 px/thread, 4 views/chunk, 4 CTAs/SM
 //     4: 128x64, 512 threads, 16 px/thread, 4 views/chunk, 2 CTAs/SM
+//     5: 64x128, 256 threads, 32 px/thread, 4 views/chunk, 2 CTAs/SM
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -578,6 +632,7 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 2: return go_bp<4, 4, 4, 8, 4, PAD, 1>(p, s, checked);
     case 3: return go_bp<2, 4, 4, 4, 4, PAD, 4>(p, s, checked);
     case 4: return go_bp<4, 4, 4, 4, 4, PAD, 2>(p, s, checked);
+    case 5: return go_bp<2, 4, 4, 8, 4, PAD, 2>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -585,10 +640,65 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
 static cudaError_t dispatch_pair(const BackprojLaunch& p, cudaStream_t s, bool checked, int variant) {
     switch (variant) {
     case 1: return go_pair<2, 4, 4, 8, 16, 2>(p, s, checked);
-    case 2: case 4: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
+    case 2: case 4: case 5: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
     case 3: return go_pair<2, 4, 4, 4, 8, 4>(p, s, checked);
     default: return go_pair<4, 4, 4, 8, 16, 1>(p, s, checked);
     }
+}
+
+// Persistent launcher for the batched queue: the tile shape of the selected int-table variant
+// (variants 0/2 -> 128x128, 4 -> 128x64, else 64x64), one grid of (SMs x resident CTAs).
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB>
+static cudaError_t go_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    auto kern = k_bp_ref_persistent<WX, WY, RX, RY, VC, PAD, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::NT, Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int grid = sms * per_sm;
+    if (grid > njobs) grid = njobs;
+    if (grid < 1) return cudaSuccess;
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(jobs, njobs, counter);
+    return cudaGetLastError();
+}
+
+static void persistent_shape(int variant, int* tx, int* ty) {
+    switch (variant) {
+    case 0: case 2: *tx = 128; *ty = 128; break;
+    case 4: *tx = 128; *ty = 64; break;
+    case 5: *tx = 64; *ty = 128; break;
+    default: *tx = 64; *ty = 64; break;
+    }
+}
+
+void persistent_tile_xy(int variant, int* tx, int* ty) { persistent_shape(variant, tx, ty); }
+
+template <int PAD>
+static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s, int variant) {
+    switch (variant) {
+    case 0: return go_persistent<4, 4, 4, 8, 8, PAD, 1>(jobs, njobs, counter, s);
+    case 2: return go_persistent<4, 4, 4, 8, 4, PAD, 1>(jobs, njobs, counter, s);
+    case 4: return go_persistent<4, 4, 4, 4, 4, PAD, 2>(jobs, njobs, counter, s);
+    case 5: return go_persistent<2, 4, 4, 8, 4, PAD, 2>(jobs, njobs, counter, s);
+    case 1: return go_persistent<2, 4, 4, 4, 8, PAD, 1>(jobs, njobs, counter, s);
+    default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
+    }
+}
+
+cudaError_t launch_bp_ref_persistent(const TileJob* d_jobs, int njobs, unsigned* d_counter, int table_fmt,
+                                     int variant, cudaStream_t s) {
+    if (table_fmt == kTabPair) return cudaErrorInvalidValue;   // queue tables are int tables
+    return table_fmt == kTabInt17 ? dispatch_persistent<1>(d_jobs, njobs, d_counter, s, variant)
+                                  : dispatch_persistent<0>(d_jobs, njobs, d_counter, s, variant);
+}
+int default_variant() {
+    load_defaults();
+    return g_variant;
 }
 
 cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
@@ -635,7 +745,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 4 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 5 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;

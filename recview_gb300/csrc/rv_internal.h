@@ -94,6 +94,20 @@ struct BackprojLaunch {
     unsigned int* status_counter;  // validation mode: window-violation counter (else null)
 };
 cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s);
+
+// One tile of one slice for the persistent REF back-projection (batched queue).
+struct TileJob {
+    const int* table;         // the slice's tables (view-major, table_stride ints per view)
+    const float4* geom;       // the slice's per-view geometry
+    int* out;                 // the slice (ixdimp^2 int32)
+    long long table_stride;
+    int nviews, ixdimp, X0, Y0;
+};
+// tile shape of the persistent kernel of an int-table variant (0..4), and the default variant
+void persistent_tile_xy(int variant, int* tx, int* ty);
+int default_variant();
+cudaError_t launch_bp_ref_persistent(const TileJob* d_jobs, int njobs, unsigned* d_counter, int table_fmt,
+                                     int variant, cudaStream_t s);
 cudaError_t launch_bp_ref(const BackprojLaunch& p, cudaStream_t s);
 // REF table format per detector pixel j, and the slot stride in 4-byte words:
 //   kTabInt16: the reference's 16 ints igp[16j+k]          (64 B per pixel)

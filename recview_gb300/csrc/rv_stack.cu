@@ -52,7 +52,7 @@ static void stack_free(RvStack* st) {
         if (e) cudaEventDestroy(e);
 }
 
-extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
+static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_tables) {
     if (!desc || !out || !desc->bInc || !desc->fdeg || !desc->fFilter || desc->nframes < 1 || desc->nslices < 1 ||
         desc->ixdim < 4 || (!desc->input_is_sinogram && !desc->fexp) || desc->mode < RV_MODE_REF ||
         desc->mode > RV_MODE_LIN_BF16) {
@@ -172,7 +172,7 @@ extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
               cuda_ok(cudaMalloc(&st->d_geom, (size_t)V * sizeof(float4)), RV_ERR_DEVICE_OOM, "geometry") &&
               cuda_ok(cudaMalloc(&st->d_filt, (size_t)d.ndim * sizeof(float)), RV_ERR_DEVICE_OOM, "filter") &&
               cuda_ok(cudaMalloc(&st->d_tw, tw.size() * sizeof(float2)), RV_ERR_DEVICE_OOM, "twiddles") &&
-              cuda_ok(cudaMalloc(&st->d_table, per_slice * st->batch), RV_ERR_DEVICE_OOM, "tables") &&
+              (!alloc_tables || cuda_ok(cudaMalloc(&st->d_table, per_slice * st->batch), RV_ERR_DEVICE_OOM, "tables")) &&
               cuda_ok(cudaMalloc(&st->d_scale, (size_t)st->batch * V * sizeof(float)), RV_ERR_DEVICE_OOM, "scales");
     if (ok) {
         const std::vector<float4>& g = desc->mode == RV_MODE_REF ? st->geom_ref : st->geom_lin;
@@ -192,6 +192,8 @@ extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) {
     *out = st;
     return 0;
 }
+
+extern "C" int RvStackCreate(const RvStackDesc* desc, RvStack** out) { return stack_create(desc, out, true); }
 
 extern "C" void RvStackDestroy(RvStack* st) {
     if (!st) return;
@@ -337,3 +339,292 @@ extern "C" int RvStackLastTimings(const RvStack* st, float* ms3) {
 }
 
 extern "C" int RvStackLastLaunchCount(const RvStack* st) { return st ? st->launches : 0; }
+
+// =============================================================================================
+// Batched queue (no reference counterpart; replaces the sequential item loop of
+// source/DlgQueue.cpp:363-470 and CGazoDoc::BatchReconst, source/gazoDoc.cpp:1938-1993).
+// Datasets of uneven width, view count, centre and zoom are added as stacks; RvQueueRun groups
+// (dataset, slice) pairs into waves whose int tables fit a device-memory pool, and each wave is
+// one filter launch per dataset plus ONE persistent back-projection launch that takes 64x64 (or
+// the tuned shape) tiles from a device work list until it is empty.  The whole sequence is
+// captured once into a CUDA graph and replayed on later runs.
+// =============================================================================================
+struct RvQueueItem {
+    RvStack* st;
+    const void* d_raw;
+    void* d_out;
+};
+
+struct RvQueue {
+    std::vector<RvQueueItem> items;
+    int fmt = kTabInt16;
+    int variant = -1;
+    bool built = false;
+    struct FilterPart { FilterLaunch fl; };
+    struct Wave { std::vector<FilterLaunch> filters; int tile_begin = 0, ntiles = 0; };
+    std::vector<Wave> waves;
+    void* d_rowjobs = nullptr;
+    void* d_tiles = nullptr;
+    void* d_pool = nullptr;
+    unsigned* d_counters = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev[2] = {};
+    float last_ms = 0;
+    size_t total_tiles = 0;
+    double total_updates = 0;
+    void release_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        void* b[] = {d_rowjobs, d_tiles, d_pool, d_counters};
+        for (void* p : b)
+            if (p) cudaFree(p);
+        d_rowjobs = d_tiles = d_pool = nullptr;
+        d_counters = nullptr;
+        waves.clear();
+        built = false;
+    }
+};
+
+extern "C" int RvQueueCreate(RvQueue** out) {
+    if (!out) return RV_ERR_BAD_ARGUMENT;
+    RvQueue* q = new RvQueue();
+    const int f = ref_table_fmt();
+    q->fmt = (f == kTabInt17) ? kTabInt17 : kTabInt16;
+    q->variant = default_variant();
+    if (!cuda_ok(cudaEventCreate(&q->ev[0]), RV_ERR_LAUNCH, "event") ||
+        !cuda_ok(cudaEventCreate(&q->ev[1]), RV_ERR_LAUNCH, "event")) {
+        delete q;
+        return RV_ERR_LAUNCH;
+    }
+    *out = q;
+    return 0;
+}
+
+extern "C" int RvQueueAdd(RvQueue* q, const RvStackDesc* desc, const void* d_raw, void* d_out) {
+    if (!q || !desc || !d_raw || !d_out) {
+        set_error(RV_ERR_BAD_ARGUMENT, "RvQueueAdd: NULL argument");
+        return RV_ERR_BAD_ARGUMENT;
+    }
+    if (desc->mode != RV_MODE_REF) {
+        set_error(RV_ERR_UNSUPPORTED, "RvQueueAdd: the queue runs the reference-semantics mode only");
+        return RV_ERR_UNSUPPORTED;
+    }
+    RvStack* st = nullptr;   // the queue keeps its own table pool: no per-stack tables
+    const int rc = stack_create(desc, &st, false);
+    if (rc) return rc;
+    q->items.push_back({st, d_raw, d_out});
+    q->release_plan();
+    return 0;
+}
+
+static int queue_build(RvQueue* q, cudaStream_t s) {
+    q->release_plan();
+    q->total_updates = 0;
+    int tx = 64, ty = 64;
+    persistent_tile_xy(q->variant, &tx, &ty);
+    size_t budget_mb = 32768;
+    if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
+    const size_t pool_words_max = (budget_mb << 20) / 4;
+    // ---- waves of (item, slice range) whose tables fit the pool ---------------------------
+    struct Part { int item, s0, s1; size_t off; };
+    std::vector<std::vector<Part>> wparts(1);
+    size_t used = 0, pool_words = 0;
+    for (int it = 0; it < (int)q->items.size(); it++) {
+        RvStack* st = q->items[it].st;
+        const size_t per_slice = (size_t)st->nviews * (size_t)ref_table_stride(st->d.ixdimp, q->fmt);
+        if (per_slice > pool_words_max) {
+            set_error(RV_ERR_UNSUPPORTED, "RvQueueRun: one slice's tables exceed the table budget");
+            return RV_ERR_UNSUPPORTED;
+        }
+        int s = 0;
+        while (s < st->desc.nslices) {
+            if (used + per_slice > pool_words_max) {
+                wparts.emplace_back();
+                used = 0;
+            }
+            int n = (int)((pool_words_max - used) / per_slice);
+            if (n > st->desc.nslices - s) n = st->desc.nslices - s;
+            wparts.back().push_back({it, s, s + n, used});
+            used += per_slice * n;
+            if (used > pool_words) pool_words = used;
+            s += n;
+        }
+    }
+    // ---- row jobs, filter launches and tile work lists --------------------------------------
+    std::vector<RowJob> rowjobs;
+    std::vector<TileJob> tiles;
+    std::vector<size_t> rj_begin;   // per filter launch: start index into rowjobs
+    for (auto& parts : wparts) {
+        RvQueue::Wave w;
+        w.tile_begin = (int)tiles.size();
+        for (const Part& pt : parts) {
+            RvStack* st = q->items[pt.item].st;
+            const int V = st->nviews;
+            const long long ts = ref_table_stride(st->d.ixdimp, q->fmt);
+            const size_t npix = (size_t)st->d.ixdimp * st->d.ixdimp;
+            rj_begin.push_back(rowjobs.size());
+            for (int sl = pt.s0; sl < pt.s1; sl++)
+                for (int v = 0; v < V; v++) {
+                    RowJob j = st->jobs[(size_t)sl * V + v];
+                    j.dst = (sl - pt.s0) * V + v;
+                    rowjobs.push_back(j);
+                }
+            FilterLaunch fl{};
+            fl.src = q->items[pt.item].d_raw;
+            fl.raw = st->desc.input_is_sinogram ? 0 : 1;
+            fl.pixmin = (st->desc.iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit : RV_SINOGRAM_PIXEL_MIN16bit;
+            fl.njobs = (pt.s1 - pt.s0) * V;
+            fl.filt = static_cast<const float*>(st->d_filt);
+            fl.tw = static_cast<const float2*>(st->d_tw);
+            fl.table = reinterpret_cast<int*>((size_t)pt.off * 4);   // pool offset, rebased below
+            fl.mode = RV_MODE_REF;
+            fl.d = st->d;
+            fl.ic = (int)st->desc.center;
+            fl.table_stride = ts;
+            fl.table_fmt = q->fmt;
+            w.filters.push_back(fl);
+            const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
+            for (int sl = pt.s0; sl < pt.s1; sl++)
+                for (int t = 0; t < ntx * nty; t++) {
+                    TileJob J{};
+                    J.table = reinterpret_cast<const int*>((pt.off + (size_t)(sl - pt.s0) * V * ts) * 4);
+                    J.geom = static_cast<const float4*>(st->d_geom);
+                    J.out = static_cast<int*>(q->items[pt.item].d_out) + (size_t)sl * npix;
+                    J.table_stride = ts;
+                    J.nviews = V;
+                    J.ixdimp = st->d.ixdimp;
+                    J.X0 = (t % ntx) * tx;
+                    J.Y0 = (t / ntx) * ty;
+                    tiles.push_back(J);
+                }
+            q->total_updates += (double)(pt.s1 - pt.s0) * V * npix;
+        }
+        w.ntiles = (int)tiles.size() - w.tile_begin;
+        q->waves.push_back(std::move(w));
+    }
+    q->total_tiles = tiles.size();
+    if (!cuda_ok(cudaMalloc(&q->d_pool, pool_words * 4 + 16), RV_ERR_DEVICE_OOM, "table pool") ||
+        !cuda_ok(cudaMalloc(&q->d_rowjobs, rowjobs.size() * sizeof(RowJob) + 16), RV_ERR_DEVICE_OOM, "row jobs") ||
+        !cuda_ok(cudaMalloc(&q->d_tiles, tiles.size() * sizeof(TileJob) + 16), RV_ERR_DEVICE_OOM, "tiles") ||
+        !cuda_ok(cudaMalloc((void**)&q->d_counters, q->waves.size() * sizeof(unsigned)), RV_ERR_DEVICE_OOM, "counters"))
+        return RvGetLastError();
+    // rebase pool offsets to device addresses
+    int* pool = static_cast<int*>(q->d_pool);
+    for (TileJob& J : tiles) J.table = pool + reinterpret_cast<size_t>(J.table) / 4;
+    size_t fi = 0;
+    for (auto& w : q->waves)
+        for (FilterLaunch& fl : w.filters) {
+            fl.table = pool + reinterpret_cast<size_t>(fl.table) / 4;
+            fl.jobs = static_cast<const RowJob*>(q->d_rowjobs) + rj_begin[fi++];
+        }
+    if (!cuda_ok(cudaMemcpy(q->d_rowjobs, rowjobs.data(), rowjobs.size() * sizeof(RowJob), cudaMemcpyHostToDevice),
+                 RV_ERR_COPY_H2D, "row jobs") ||
+        !cuda_ok(cudaMemcpy(q->d_tiles, tiles.data(), tiles.size() * sizeof(TileJob), cudaMemcpyHostToDevice),
+                 RV_ERR_COPY_H2D, "tiles"))
+        return RvGetLastError();
+    (void)s;
+    q->built = true;
+    return 0;
+}
+
+static int queue_launch(RvQueue* q, cudaStream_t s) {
+    const TileJob* tiles = static_cast<const TileJob*>(q->d_tiles);
+    for (size_t w = 0; w < q->waves.size(); w++) {
+        RvQueue::Wave& wv = q->waves[w];
+        if (!cuda_ok(cudaMemsetAsync(q->d_counters + w, 0, sizeof(unsigned), s), RV_ERR_MEMSET, "counter"))
+            return RV_ERR_MEMSET;
+        for (const FilterLaunch& fl : wv.filters)
+            if (!cuda_ok(launch_filter(fl, s), RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
+        if (!cuda_ok(launch_bp_ref_persistent(tiles + wv.tile_begin, wv.ntiles, q->d_counters + w, q->fmt,
+                                              q->variant, s),
+                     RV_ERR_LAUNCH, "persistent back-projection"))
+            return RV_ERR_LAUNCH;
+    }
+    return 0;
+}
+
+extern "C" int RvQueueRun(RvQueue* q, void* stream) {
+    if (!q) return RV_ERR_BAD_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStream_t cap = nullptr;
+    int rc = 0;
+    if (!q->built) {
+        if ((rc = queue_build(q, s))) return rc;
+        // capture the whole sequence once (on a private stream: the legacy stream cannot capture)
+        if (!cuda_ok(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), RV_ERR_STREAM, "capture stream"))
+            return RV_ERR_STREAM;
+        if (!cuda_ok(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), RV_ERR_LAUNCH, "graph capture")) {
+            cudaStreamDestroy(cap);
+            return RV_ERR_LAUNCH;
+        }
+        rc = queue_launch(q, cap);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (!cuda_ok(e, RV_ERR_LAUNCH, "graph capture") ||
+            !cuda_ok(cudaGraphInstantiate(&q->exec, g, 0), RV_ERR_LAUNCH, "graph instantiate")) {
+            if (g) cudaGraphDestroy(g);
+            return RV_ERR_LAUNCH;
+        }
+        q->graph = g;
+    }
+    cudaEventRecord(q->ev[0], s);
+    if (!cuda_ok(cudaGraphLaunch(q->exec, s), RV_ERR_LAUNCH, "graph launch")) return RV_ERR_LAUNCH;
+    cudaEventRecord(q->ev[1], s);
+    if (!cuda_ok(cudaEventSynchronize(q->ev[1]), RV_ERR_LAUNCH, "queue run")) return RV_ERR_LAUNCH;
+    cudaEventElapsedTime(&q->last_ms, q->ev[0], q->ev[1]);
+    if (take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+        return RV_ERR_KERNEL_STATUS;
+    }
+    return 0;
+}
+
+extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
+    // times every int-table variant's persistent kernel on the whole queue (graph-free runs) and
+    // keeps the fastest for the captured graph
+    if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int cands[] = {3, 0, 4, 5};
+    float best = 3.0e38f;
+    int bestv = q->variant;
+    for (int v : cands) {
+        q->variant = v;
+        int rc = queue_build(q, s);
+        if (rc) return rc;
+        if ((rc = queue_launch(q, s))) return rc;   // warm-up
+        cudaEventRecord(q->ev[0], s);
+        if ((rc = queue_launch(q, s))) return rc;
+        cudaEventRecord(q->ev[1], s);
+        cudaEventSynchronize(q->ev[1]);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, q->ev[0], q->ev[1]);
+        if (ms < best) {
+            best = ms;
+            bestv = v;
+        }
+    }
+    q->variant = bestv;
+    q->release_plan();
+    if (chosen) *chosen = bestv;
+    return 0;
+}
+
+extern "C" float RvQueueLastMs(const RvQueue* q) { return q ? q->last_ms : 0.0f; }
+extern "C" double RvQueueUpdates(const RvQueue* q) { return q ? q->total_updates : 0.0; }
+
+extern "C" void RvQueueDestroy(RvQueue* q) {
+    if (!q) return;
+    q->release_plan();
+    for (RvQueueItem& it : q->items) RvStackDestroy(it.st);
+    for (cudaEvent_t& e : q->ev)
+        if (e) cudaEventDestroy(e);
+    delete q;
+}
