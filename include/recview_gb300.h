@@ -310,6 +310,22 @@ unsigned long long RvGetWindowViolations(void);
 int RvRescaleSlices(int* d_slices, int nslices, int ixdimp, double center_user, int ipintp, int ibinning,
                     unsigned short* d_out16, int* minmax, void* stream);
 
+/* ---- output files (R9 / next-row TIFF output) -------------------------------------------------
+ * RecView's per-slice 16-bit TIFF (WriteTifMonochrome16, source/general.cpp:1313-1470), byte for
+ * byte: slice = the rescaled int values (RvRescaleSlices), negatives stored as 0; artist NULL
+ * gives the reference's "SP-uCT, gazoView".  RvTiff16Bytes returns the file size and fills out
+ * when cap is large enough (negative RV_ERR_* on bad arguments). */
+long long RvTiff16Bytes(const int* slice, int height, int width, const char* description, const char* artist,
+                        unsigned char* out, long long cap);
+int RvWriteTiff16(const char* path, const int* slice, int height, int width, const char* description,
+                  const char* artist);
+/* The physical scale of the rescaled values (pixelBase/pixelDiv, source/gazoDoc.cpp:3997-4006) and
+ * the ImageDescription string BatchReconst writes (source/gazoDoc.cpp:1985-1988). */
+int RvPixelScale(int nSinogr, double pixelWidth, int iBinning, int ipintp, int imin, int imax, int zernike,
+                 float* pixelBase, float* pixelDiv);
+int RvImageDescription(char* out, int cap, int nSinogr, double pixelWidth, float pixelDiv, float pixelBase,
+                       double centre, int filterKind);
+
 /* ---- batched queue (no reference counterpart; replaces the sequential queue loop of
  * source/DlgQueue.cpp:363-470 / CGazoDoc::BatchReconst, source/gazoDoc.cpp:1938-1993) --------
  * Datasets of uneven detector width, view count, centre and zoom are added as stack descriptions

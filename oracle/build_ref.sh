@@ -12,6 +12,7 @@
 #   source/general.cpp:2377-2532                  GenerateSinogramThread
 #   source/gazoDoc.cpp:3748-3812                  body of CGazoDoc::SetFilter
 #   source/gazoDoc.cpp:4379-4627                  computational part of CGazoDoc::GetAxis
+#   source/general.cpp:1313-1470                  WriteTifMonochrome16 (16-bit TIFF writer)
 #   oracle/ref_wrap/libm_pin.cpp                  correctly rounded cosf/sinf for the twiddles
 #
 # The extracted ranges are checked against SHA-256 sums so a different checkout fails loudly
@@ -40,6 +41,7 @@ check() {  # file first last sha256
 check general.cpp 2020 2163 0363b3ff22cd95c6b3c1aa74a56ec5eb8c6fd5e225459306ffdbaa97adf2ff28
 check general.cpp 2377 2532 2f41a4c98ee29e23f3a3dc7d8e5ddc1289e70dd46e097b141a26bd4c4a033981
 check gazoDoc.cpp 3748 3812 74de08b2b13fbf43c047b1fdca2bff6aae955307240a1aed58a8024175e90a3d
+check general.cpp 1313 1470 80bb671236c506c654d4f1f620d23d219fa28b59a121d4f25384e6f6054c2c56
 check gazoDoc.cpp 4379 4627 fcf94fb4d8af6e867fe5ecef64c6d776047c3b5bea9ea73fa5fd83c00b407774
 
 CXX="${CXX:-g++}"
@@ -57,6 +59,8 @@ cd "$OUT/obj"   # empty directory: quote includes of the piped units resolve via
     | "$CXX" "${FLAGS[@]}" -x c++ -c - -o filter.o
 { cat "$HERE/ref_wrap/axis_head.inc"; sed -n 4379,4627p "$SRC/gazoDoc.cpp"; cat "$HERE/ref_wrap/axis_tail.inc"; } \
     | "$CXX" "${FLAGS[@]}" -x c++ -c - -o axis.o
+{ cat "$HERE/ref_wrap/tif_head.inc"; sed -n 1313,1470p "$SRC/general.cpp"; cat "$HERE/ref_wrap/tif_tail.inc"; } \
+    | "$CXX" "${FLAGS[@]}" -x c++ -c - -o tif.o
 "$CXX" "${FLAGS[@]}" -fno-builtin -c "$HERE/ref_wrap/libm_pin.cpp" -o libm_pin.o
-"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o axis.o libm_pin.o -lm
+"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o axis.o tif.o libm_pin.o -lm
 echo "build_ref: $OUT/librvref.so"

@@ -191,6 +191,13 @@ PROTOTYPES = {
                             C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "RvCentreSweep": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, c_float_p, C.c_float, c_float_p,
                                 C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "RvTiff16Bytes": (C.c_longlong, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p, C.c_void_p,
+                                     C.c_longlong]),
+    "RvWriteTiff16": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p]),
+    "RvPixelScale": (C.c_int, [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, c_float_p,
+                               c_float_p]),
+    "RvImageDescription": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_float, C.c_float, C.c_double,
+                                     C.c_int]),
     "RvQueueCreate": (C.c_int, [C.POINTER(C.c_void_p)]),
     "RvQueueAdd": (C.c_int, [C.c_void_p, C.POINTER(RvStackDesc), C.c_void_p, C.c_void_p]),
     "RvQueueAutotune": (C.c_int, [C.c_void_p, C.c_void_p, c_int_p]),

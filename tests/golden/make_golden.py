@@ -121,6 +121,18 @@ def main() -> None:
                            C.byref(a), C.byref(b))
         out[f"{name}_frames"] = np.stack([s0, s1, fl])
         out[f"{name}_params"] = np.array([off, a.value, b.value])
+    # 16-bit TIFF files
+    ref.rvref_write_tif16.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int]
+    rng = np.random.default_rng(5)
+    for name, h, w, desc, art in (("tif_a", 7, 9, b"1800\t3.250000\t0.1\t0.2\t1023.5\t6\t55.111697\t0.461227 ",
+                                   b"SP-uCT, gazoView"), ("tif_b", 4, 5, b"ab", b"")):
+        img = rng.integers(-100, 70000, (h, w)).astype(np.int32)
+        buf = np.zeros(1 << 16, np.uint8)
+        n = ref.rvref_write_tif16(img.ctypes.data, h, w, desc, art, buf.ctypes.data, buf.size)
+        out[f"{name}_img"] = img
+        out[f"{name}_desc"] = np.frombuffer(desc, np.uint8)
+        out[f"{name}_artist"] = np.frombuffer(art, np.uint8)
+        out[f"{name}_bytes"] = buf[:n].copy()
     dst = Path(__file__).with_name("golden.npz")
     np.savez_compressed(dst, **out)
     print(f"wrote {dst} ({dst.stat().st_size} bytes, {len(out)} arrays)")

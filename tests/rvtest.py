@@ -101,6 +101,7 @@ def ref_lib():
     U16P = C.POINTER(C.c_ushort)
     L.rvref_get_axis.argtypes = [U16P, U16P, U16P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]
+    L.rvref_write_tif16.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int]
     return L
 
 
