@@ -234,9 +234,8 @@ def run_reference(args, rank: int, world: int):
 # ------------------------------------------------------------------------------ GPU side ---
 def run_ours(args, rank: int, world: int, local_rank: int):
     import torch
-    import torch.distributed as dist
     import recview_gb300 as rv
-    from recview_gb300 import abi
+    from recview_gb300 import abi, replicas
     from recview_gb300.build import build_lib, build_oracle
 
     build_lib()
@@ -259,16 +258,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        tt = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        return float(tt.item())
+    barrier, max_over_ranks = replicas.barrier, replicas.max_over_ranks
 
     for _ in range(args.warmup):
         st.run_device(raw.data_ptr(), out.data_ptr(), sh)
