@@ -378,6 +378,47 @@ int RvGetBackprojectionVariant(int* variant, int* format);
  * out[1] = float->int32 conversions in G/s, both measured on the current device. */
 int RvProbeThroughput(double* out, int n);
 
+/* ---- Offset-CT (360-degree scan with the rotation axis near one edge of the frame) ----------
+ * Replaces the offset-CT tail of CGazoDoc::GenerateSinogram (source/gazoDoc.cpp:3535-3665):
+ * every SAMPLE view i below nof = GetSinogramYdim(TRUE) (the first frame beyond 180 degrees,
+ * source/gazoDoc.cpp:2967-2978) is joined with the first later SAMPLE frame at least 180 degrees
+ * on into one row of width = iXdim / binning samples: the view's own samples on the axis side,
+ * the partner mirrored about the axis (linear interpolation for the sub-pixel axis position) on
+ * the other, crossfaded over the overlap, exactly as the reference rounds them.  Non-SAMPLE views
+ * give zero rows.  The stitched rows are then reconstructed like any sinogram with ixdim =
+ * width, iLenSinogr = nof + 1 and ri->center = RvOffsetCtReconCenter(...)
+ * (CGazoDoc::DeconvBackProj, source/gazoDoc.cpp:3832-3836,3935). */
+typedef struct RvOffsetCtDesc {
+    int iRawSinoXdim;      /* frame width before binning (rq->iRawSinoXdim) */
+    int iXdim;             /* stitched width before binning (rq->iXdim; RecView sets 2*iRawSinoXdim) */
+    int iInterpolation;    /* rq->iInterpolation: binning 4 / 2 / 1 for 0 / 1 / other values */
+    int iTrimWidth;        /* rq->iTrimWidth */
+    int iLenSinogr;        /* frames including the dark frame (CGazoDoc::iLenSinogr) */
+    int iMultiplex;        /* detector rows (slices) per frame */
+    double center;         /* rotation centre passed to GenerateSinogram (frame pixels, user convention) */
+    double deltaCent;      /* centre change per detector row (GenerateSinogram's deltaCent) */
+    const char* bInc;      /* [iLenSinogr] RV_BINC_* flags (host) */
+    const float* fdeg;     /* [iLenSinogr] angles in degrees (host) */
+} RvOffsetCtDesc;
+
+/* Sizes: nof stitched views, ixlen = iRawSinoXdim / binning samples per input row, width samples
+ * per output row.  Returns 0, 21051 (no frame beyond 180 degrees, as the reference) or
+ * RV_ERR_BAD_ARGUMENT. */
+int RvOffsetCtDims(const RvOffsetCtDesc* desc, int* nof, int* ixlen, int* width);
+/* ri->center for the reconstruction of stitched rows of one detector row whose centre (user
+ * convention, frame pixels) is layer_center. */
+double RvOffsetCtReconCenter(const RvOffsetCtDesc* desc, double layer_center);
+/* Device buffers: d_sino = iLenSinogr * iMultiplex rows of ixlen normalised int16 samples (row
+ * i*iMultiplex + j = frame i, detector row j, the reference's iSinogr order); d_out = nof *
+ * iMultiplex rows of width samples, all written.  Asynchronous on stream (NULL = legacy default
+ * stream).  Returns 0, 21051 / 21052 (no frame beyond 180 degrees / a view without a partner,
+ * as the reference), RV_ERR_BAD_ARGUMENT (also when a row would be read or written outside its
+ * bounds, which the reference leaves undefined), or a CUDA error code. */
+int RvOffsetCtStitchDevice(const RvOffsetCtDesc* desc, const short* d_sino, short* d_out, void* stream);
+/* The reference's host form: iSinogr[i*iMultiplex + j] rows in, ofSinogr[i*iMultiplex + j] rows
+ * (width samples each, i < nof) out; synchronous.  Same return codes. */
+int RvOffsetCtStitchHost(const RvOffsetCtDesc* desc, short* const* iSinogr, short* const* ofSinogr);
+
 #ifdef __cplusplus
 }
 #endif

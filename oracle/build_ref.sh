@@ -4,7 +4,7 @@
 # TEST INFRASTRUCTURE ONLY: the library is the parity pin for the oracle restatement
 # (oracle/rv_oracle.c) and is used by tests and fixture generation in the container that has
 # the reference checkout.  Nothing is copied into the repository: whole files are compiled by
-# path, and the three function bodies below are spliced between small wrapper heads/tails
+# path, and the function bodies below are spliced between small wrapper heads/tails
 # (oracle/ref_wrap) through a pipe straight into the compiler.  Outputs go to oracle/_ref only.
 #
 #   source/cfft.cpp, source/ccmplx.cpp             compiled by path
@@ -13,6 +13,7 @@
 #   source/gazoDoc.cpp:3748-3812                  body of CGazoDoc::SetFilter
 #   source/gazoDoc.cpp:4379-4627                  computational part of CGazoDoc::GetAxis
 #   source/general.cpp:1313-1470                  WriteTifMonochrome16 (16-bit TIFF writer)
+#   source/gazoDoc.cpp:2967-2978, 3535-3666        GetSinogramYdim + offset-CT stitching tail
 #   oracle/ref_wrap/libm_pin.cpp                  correctly rounded cosf/sinf for the twiddles
 #
 # The extracted ranges are checked against SHA-256 sums so a different checkout fails loudly
@@ -43,6 +44,8 @@ check general.cpp 2377 2532 2f41a4c98ee29e23f3a3dc7d8e5ddc1289e70dd46e097b141a26
 check gazoDoc.cpp 3748 3812 74de08b2b13fbf43c047b1fdca2bff6aae955307240a1aed58a8024175e90a3d
 check general.cpp 1313 1470 80bb671236c506c654d4f1f620d23d219fa28b59a121d4f25384e6f6054c2c56
 check gazoDoc.cpp 4379 4627 fcf94fb4d8af6e867fe5ecef64c6d776047c3b5bea9ea73fa5fd83c00b407774
+check gazoDoc.cpp 2967 2978 d0d0a88882e1b0a605ad40cbe58e122756669c99033dbdf55af4b2aceb72b678
+check gazoDoc.cpp 3535 3666 20e3f0e0c127d19e8d899301a4ddfc030737579b554f0435a85014666a383e8b
 
 CXX="${CXX:-g++}"
 # -ffp-contract=off: the reference's x64 build rounds every float operation separately.
@@ -61,6 +64,9 @@ cd "$OUT/obj"   # empty directory: quote includes of the piped units resolve via
     | "$CXX" "${FLAGS[@]}" -x c++ -c - -o axis.o
 { cat "$HERE/ref_wrap/tif_head.inc"; sed -n 1313,1470p "$SRC/general.cpp"; cat "$HERE/ref_wrap/tif_tail.inc"; } \
     | "$CXX" "${FLAGS[@]}" -x c++ -c - -o tif.o
+{ cat "$HERE/ref_wrap/ofct_head.inc"; sed -n 2967,2978p "$SRC/gazoDoc.cpp"; cat "$HERE/ref_wrap/ofct_mid.inc"; \
+  sed -n 3535,3666p "$SRC/gazoDoc.cpp"; cat "$HERE/ref_wrap/ofct_tail.inc"; } \
+    | "$CXX" "${FLAGS[@]}" -x c++ -c - -o ofct.o
 "$CXX" "${FLAGS[@]}" -fno-builtin -c "$HERE/ref_wrap/libm_pin.cpp" -o libm_pin.o
-"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o axis.o tif.o libm_pin.o -lm
+"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o axis.o tif.o ofct.o libm_pin.o -lm
 echo "build_ref: $OUT/librvref.so"

@@ -804,3 +804,111 @@ double rvo_tv_score(const int* slice, int ixdimp) {
         }
     return acc;
 }
+
+/* ------------------------------------------------------------ offset-CT sinogram stitching ---- */
+int rvo_offset_ct_views(const float* fdeg, int iLenSinogr) {
+    /* CGazoDoc::GetSinogramYdim(TRUE), source/gazoDoc.cpp:2967-2978: index of the first frame
+     * whose angle exceeds 180 degrees (the dark frame, last, is not examined); -1 if none */
+    if (!fdeg) return -1;
+    for (int i = 0; i + 1 < iLenSinogr; i++)
+        if (fdeg[i] > 180.) return i;
+    return -1;
+}
+
+/* (short)(a + (b - a) t): the mirrored-sample interpolation of source/gazoDoc.cpp:3590-3650,
+ * int difference promoted to double, one product, one sum, truncation toward zero */
+static short oct_mix(int a, int b, double t) {
+    const double prod = (double)(b - a) * t;
+    return (short)((double)a + prod);
+}
+
+/* crossfade of source/gazoDoc.cpp:3597,3614,3635,3652: (short)(r*v + (1-r)*s) */
+static short oct_fade(double r, short v, short s) {
+    const double x = r * (double)v;
+    const double y = (1. - r) * (double)s;
+    return (short)(x + y);
+}
+
+int rvo_offset_ct_stitch(const short* sino, long long sino_stride, short* of, long long of_stride,
+                         const char* bInc, const float* fdeg, int iLenSinogr, int iMultiplex,
+                         double center, double deltaCent, int iInterpolation, int iTrimWidth,
+                         int iRawSinoXdim, int iXdim) {
+    /* The offset-CT tail of CGazoDoc::GenerateSinogram (source/gazoDoc.cpp:3535-3665), on
+     * already normalised int16 rows sino[(i*iMultiplex + j) * sino_stride + x], x < ixlen.
+     * Output rows of[(i*iMultiplex + j) * of_stride + x], x < width, for i < nof.  Returns 0,
+     * the reference's 21051 (no frame beyond 180 degrees) / 21052 (no partner frame), or -1 when
+     * a row would read or write outside its bounds (undefined in the reference). */
+    const int B = (iInterpolation == 0) ? 4 : ((iInterpolation == 1) ? 2 : 1);   /* :2987 */
+    const int F = iRawSinoXdim, T = iTrimWidth;
+    const int ixlen = F / B;                                                      /* :3002-3004 */
+    const int width = iXdim / B;                                                  /* :3001 */
+    const int nof = rvo_offset_ct_views(fdeg, iLenSinogr);
+    if (nof < 0) return 21051;
+    for (long long r = 0; r < (long long)nof * iMultiplex; r++) memset(of + r * of_stride, 0, sizeof(short) * width);
+    const double cen = center + 0.5;   /* HALFPIXEL_OFFSET */
+    int partner = nof;
+    for (int i = 0; i < nof; i++) {
+        if (!(bInc[i] & RV_BINC_SAMPLE)) continue;
+        const double th = fdeg[i];
+        /* the first later SAMPLE frame at least 180 degrees on; the search index only advances */
+        while ((fdeg[partner] - th < 180) || !(bInc[partner] & RV_BINC_SAMPLE))
+            if (++partner >= iLenSinogr - 1) return 21052;
+        for (int j = 0; j < iMultiplex; j++) {
+            const short* s1 = sino + (long long)(i * iMultiplex + j) * sino_stride;
+            const short* s2 = sino + (long long)(partner * iMultiplex + j) * sino_stride;
+            short* o = of + (long long)(i * iMultiplex + j) * of_stride;
+#define OCT_PUT(pos, val) do { const int p_ = (pos); if (p_ < 0 || p_ >= width) return -1; o[p_] = (val); } while (0)
+#define OCT_CHK1(k) do { if ((k) < 0 || (k) >= ixlen) return -1; } while (0)
+            short held = 0;   /* the value repeated where the mirrored sample is missing */
+            if (cen > F / 2.) {
+                /* axis in the right half: own samples left of the overlap, mirrored partner right */
+                const double fc = (cen + deltaCent * j * B + T) / B;
+                const int ic = (int)fc;
+                const double dc = fc - ic;
+                const int g = F / B - 1 - ic;          /* half width of the crossfade */
+                const int o0 = T / B;
+                for (int k = o0; k <= ic - g; k++) { OCT_CHK1(k); OCT_PUT(k - o0, s1[k]); }
+                const int kend = (2 * F - T) / B;
+                for (int k = ic - g + 1; k < kend; k++) {
+                    const int m = 2 * ic - k;
+                    int ok;
+                    if (dc < 0.5) {
+                        ok = (m >= 0) && (m < ixlen - 1);
+                        if (ok) held = oct_mix(s2[m + 1], s2[m], 1 - 2 * dc);
+                    } else {
+                        ok = (m >= 1) && (m < ixlen);
+                        if (ok) held = oct_mix(s2[m - 1], s2[m], 2 - 2 * dc);
+                    }
+                    if (ok && k <= ic + g) {
+                        OCT_CHK1(k);
+                        held = oct_fade((double)(k - (ic - g)) / (g * 2 + 1), held, s1[k]);
+                    }
+                    OCT_PUT(k - o0, held);
+                }
+            } else {
+                /* axis in the left half: own samples right of the overlap, mirrored partner left */
+                const double fc = (cen + deltaCent * j * B) / B;
+                const int ic = (int)(fc + 0.5);
+                const double dc = fc - (int)fc;
+                const int g = ic;
+                const int sh = (F - T) / B;
+                for (int k = (F - 1 - T) / B; k >= ic + g; k--) { OCT_CHK1(k); OCT_PUT(k + sh, s1[k]); }
+                const int kmin = (dc < 0.5) ? 2 * ic + 1 - F / B : 2 * ic - F / B;
+                for (int k = ic + g - 1; k >= kmin; k--) {
+                    const int m = (dc < 0.5) ? 2 * ic - k : 2 * ic - 1 - k;
+                    if ((m >= 0) && (m < ixlen - 1)) {
+                        held = oct_mix(s2[m], s2[m + 1], (dc < 0.5) ? 2 * dc : 2 * dc - 1);
+                        if (k >= ic - g) {
+                            OCT_CHK1(k);
+                            held = oct_fade((double)((ic + g) - k) / (g * 2 + 1), held, s1[k]);
+                        }
+                    }
+                    OCT_PUT(k + sh, held);
+                }
+            }
+#undef OCT_PUT
+#undef OCT_CHK1
+        }
+    }
+    return 0;
+}

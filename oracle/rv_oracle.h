@@ -83,6 +83,16 @@ int rvo_get_axis(const unsigned short* s0, const unsigned short* s1, const unsig
 /* Project-defined centre-sweep score: total variation inside the circle r < 0.45 ixdimp. */
 double rvo_tv_score(const int* slice, int ixdimp);
 
+/* Offset-CT (360-degree scan, axis near a detector edge): GetSinogramYdim(TRUE)
+ * (source/gazoDoc.cpp:2967-2978) and the stitching tail of CGazoDoc::GenerateSinogram
+ * (source/gazoDoc.cpp:3535-3665) on contiguous int16 rows.  Returns 0, 21051, 21052, or -1 for a
+ * configuration whose rows would be read or written out of bounds. */
+int rvo_offset_ct_views(const float* fdeg, int iLenSinogr);
+int rvo_offset_ct_stitch(const short* sino, long long sino_stride, short* of, long long of_stride,
+                         const char* bInc, const float* fdeg, int iLenSinogr, int iMultiplex,
+                         double center, double deltaCent, int iInterpolation, int iTrimWidth,
+                         int iRawSinoXdim, int iXdim);
+
 #ifdef __cplusplus
 }
 #endif

@@ -109,6 +109,21 @@ class RvStackDesc(C.Structure):
     ]
 
 
+class RvOffsetCtDesc(C.Structure):
+    _fields_ = [
+        ("iRawSinoXdim", C.c_int),
+        ("iXdim", C.c_int),
+        ("iInterpolation", C.c_int),
+        ("iTrimWidth", C.c_int),
+        ("iLenSinogr", C.c_int),
+        ("iMultiplex", C.c_int),
+        ("center", C.c_double),
+        ("deltaCent", C.c_double),
+        ("bInc", C.POINTER(C.c_char)),
+        ("fdeg", c_float_p),
+    ]
+
+
 # constants (include/recview_gb300.h)
 LOG_SCALE = 3000
 BACKPROJ_SCALE = 100
@@ -209,6 +224,10 @@ PROTOTYPES = {
     "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
     "RvReconstructSliceNoAlloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, c_float_p,
                                             C.c_float, c_float_p, C.c_void_p, C.c_void_p]),
+    "RvOffsetCtDims": (C.c_int, [C.POINTER(RvOffsetCtDesc), c_int_p, c_int_p, c_int_p]),
+    "RvOffsetCtReconCenter": (C.c_double, [C.POINTER(RvOffsetCtDesc), C.c_double]),
+    "RvOffsetCtStitchDevice": (C.c_int, [C.POINTER(RvOffsetCtDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "RvOffsetCtStitchHost": (C.c_int, [C.POINTER(RvOffsetCtDesc), C.c_void_p, C.c_void_p]),
 }
 
 

@@ -148,3 +148,36 @@ def raw_stack(seed: int, ixdim: int, nviews: int, nslices: int, center: float,
             raw[f] = sample(flat).astype(np.uint16)
     raw[nframes] = np.clip(np.rint(dark), 0, 65535).astype(np.uint16)
     return raw, bInc, fdeg, fexp, p
+
+
+def offset_ct_sinogram(seed: int, ixfrm: int, nviews360: int, nslices: int, center: float,
+                       n_ellipsoids: int = 20, nflat_before: int = 1, nflat_after: int = 1,
+                       noise_frac: float = 0.003):
+    """Normalised int16 rows of a 360-degree offset-CT scan (rotation axis near a frame edge).
+
+    The frame has ixfrm samples and the axis sits at `center` (frame pixels); the object fills a
+    disc of radius ~ixfrm around the axis, so each frame sees one half of it and the partner frame
+    180 degrees later the other.  Returns (sino[nframes+1, nslices, ixfrm] int16 with a zero dark
+    frame last, bInc, fdeg) with flats before and after the samples, angles 360 v / nviews360.
+    """
+    rng = np.random.default_rng(seed)
+    ells3 = random_ellipsoids(rng, n_ellipsoids)
+    ns = nviews360 + 1
+    nframes = nflat_before + ns + nflat_after
+    bInc = np.zeros(nframes, dtype=np.int8)
+    bInc[nflat_before:nflat_before + ns] = 1
+    fdeg = np.zeros(nframes, dtype=np.float32)
+    ang = (np.arange(ns, dtype=np.float64) * (360.0 / nviews360)).astype(np.float32)
+    fdeg[nflat_before:nflat_before + ns] = ang
+    fdeg[nflat_before + ns:] = 360.0
+    # field half-width = ixfrm: the stitched row is twice the frame
+    t = (np.arange(ixfrm, dtype=np.float64) - center) / float(ixfrm)
+    theta = np.deg2rad(ang.astype(np.float64))
+    ys = (np.arange(nslices) - (nslices - 1) / 2.0) / (max(nslices, 2) / 2.0) * 0.5
+    sino = np.zeros((nframes + 1, nslices, ixfrm), dtype=np.int16)
+    for k, y in enumerate(ys):
+        p = line_integrals(ellipsoid_slice(ells3, y), theta, t)
+        if noise_frac > 0:
+            p = p + rng.normal(0.0, noise_frac * max(np.abs(p).max(), 1e-12), p.shape)
+        sino[nflat_before:nflat_before + ns, k] = np.clip(np.rint(p * LOG_SCALE), -32768, 32767)
+    return sino, bInc, fdeg

@@ -37,6 +37,19 @@ FBP_CASES = [
     ("odd37", 37, 45, 17.8, 2, abi.FILT_SHEPP, 0.5, 0, 0.0),
 ]
 
+# (name, seed, frame width, iInterpolation, trim, slices, views over 360, centre, centre gradient, edit)
+OCT_CASES = [
+    ("oct_right_lo", 31, 64, 2, 0, 2, 40, 50.8, 0.0, ""),
+    ("oct_right_hi", 32, 64, 2, 0, 2, 40, 52.3, 0.15, ""),
+    ("oct_left_lo", 33, 64, 2, 0, 2, 40, 9.6, 0.0, ""),
+    ("oct_left_hi", 34, 64, 2, 0, 3, 40, 11.2, -0.2, ""),
+    ("oct_bin2", 35, 96, 1, 0, 2, 36, 80.1, 0.0, ""),
+    ("oct_trim", 36, 64, 2, 2, 2, 40, 49.4, 0.0, ""),
+    ("oct_skip", 37, 48, 2, 0, 1, 30, 39.7, 0.0, "skip"),
+    ("oct_e21051", 38, 32, 2, 0, 1, 20, 26.0, 0.0, "no180"),
+    ("oct_e21052", 39, 32, 2, 0, 1, 20, 26.0, 0.0, "nopartner"),
+]
+
 
 def main() -> None:
     ref_path = build_ref()
@@ -133,6 +146,32 @@ def main() -> None:
         out[f"{name}_desc"] = np.frombuffer(desc, np.uint8)
         out[f"{name}_artist"] = np.frombuffer(art, np.uint8)
         out[f"{name}_bytes"] = buf[:n].copy()
+    # offset-CT stitching (360-degree frames, axis near an edge)
+    SP = C.POINTER(C.c_short)
+    ref.rvref_offset_ct.argtypes = [SP, C.c_longlong, SP, C.c_longlong, C.c_char_p, F32P, C.c_int, C.c_int,
+                                    C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int]
+    for name, seed, F, interp, T, M, V, cen, dcent, knock in OCT_CASES:
+        B = 4 if interp == 0 else (2 if interp == 1 else 1)
+        ixlen = F // B
+        sino, bInc, fdeg = phantom.offset_ct_sinogram(seed, ixlen, V, M, cen / B, n_ellipsoids=6)
+        if knock == "skip":
+            bInc[[3, 7, V // 2 + 2]] = 0
+        elif knock == "no180":
+            fdeg[fdeg > 180] = 180.0
+        elif knock == "nopartner":
+            bInc[V - 1:V + 2] = 0
+        nf = sino.shape[0]
+        rows = np.ascontiguousarray(sino.reshape(nf * M, ixlen))
+        width = (2 * F) // B
+        nof = max(1, int(np.argmax(fdeg[:nf - 1] > 180)))
+        res = np.zeros((nof * M, width), np.int16)
+        rc = ref.rvref_offset_ct(rows.ctypes.data_as(SP), ixlen, res.ctypes.data_as(SP), width, bInc.tobytes(),
+                                 fdeg.ctypes.data_as(F32P), nf, M, cen, dcent, interp, T, F, 2 * F)
+        out[f"{name}_rows"] = rows
+        out[f"{name}_binc"] = bInc
+        out[f"{name}_fdeg"] = fdeg
+        out[f"{name}_params"] = np.array([F, 2 * F, interp, T, M, cen, dcent, rc])
+        out[f"{name}_out"] = res
     dst = Path(__file__).with_name("golden.npz")
     np.savez_compressed(dst, **out)
     print(f"wrote {dst} ({dst.stat().st_size} bytes, {len(out)} arrays)")

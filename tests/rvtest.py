@@ -16,6 +16,23 @@ F32P = C.POINTER(C.c_float)
 RIP = C.POINTER(abi.RECONST_INFO)
 
 
+SP = C.POINTER(C.c_short)
+OCT_ARGTYPES = [SP, C.c_longlong, SP, C.c_longlong, C.c_char_p, F32P, C.c_int, C.c_int, C.c_double, C.c_double,
+                C.c_int, C.c_int, C.c_int, C.c_int]
+
+
+def oct_call(fn, rows, ixlen, bInc, fdeg, M, center, dcent, interp, trim, F, iXdim, nof):
+    """Runs an offset-CT stitcher with the (oracle / reference) C signature: (rc, rows out)."""
+    B = 4 if interp == 0 else (2 if interp == 1 else 1)
+    width = iXdim // B
+    rows = np.ascontiguousarray(rows, np.int16)
+    fdeg = np.ascontiguousarray(fdeg, np.float32)
+    out = np.full((max(nof, 1) * M, width), 0x5A5A, np.int16)
+    rc = fn(rows.ctypes.data_as(SP), ixlen, out.ctypes.data_as(SP), width, np.asarray(bInc, np.int8).tobytes(),
+            fdeg.ctypes.data_as(F32P), len(fdeg), M, center, dcent, interp, trim, F, iXdim)
+    return rc, out[:nof * M] if nof > 0 else out[:0]
+
+
 class Oracle:
     def __init__(self):
         self.L = C.CDLL(str(build_oracle()))
@@ -35,6 +52,8 @@ class Oracle:
         L.rvo_get_axis.argtypes = [U16P, U16P, U16P, C.c_int, C.c_int, C.c_int, DP, DP, DP]
         L.rvo_tv_score.argtypes = [C.POINTER(C.c_int), C.c_int]
         L.rvo_tv_score.restype = C.c_double
+        L.rvo_offset_ct_stitch.argtypes = OCT_ARGTYPES
+        L.rvo_offset_ct_views.argtypes = [F32P, C.c_int]
 
     def set_filter(self, kind, ndim, cutoff=0.5, order=2.0):
         t = np.zeros(ndim, np.float32)
@@ -81,6 +100,15 @@ class Oracle:
         s = np.ascontiguousarray(slice_, np.int32)
         return self.L.rvo_tv_score(s.ctypes.data_as(C.POINTER(C.c_int)), s.shape[0])
 
+    def offset_ct_views(self, fdeg):
+        f = np.ascontiguousarray(fdeg, np.float32)
+        return self.L.rvo_offset_ct_views(f.ctypes.data_as(F32P), len(f))
+
+    def offset_ct(self, rows, ixlen, bInc, fdeg, M, center, dcent, interp=2, trim=0, F=None, iXdim=None):
+        F = F if F is not None else ixlen
+        return oct_call(self.L.rvo_offset_ct_stitch, rows, ixlen, bInc, fdeg, M, center, dcent, interp, trim, F,
+                        iXdim if iXdim is not None else 2 * F, self.offset_ct_views(fdeg))
+
     def rescale(self, slice_, ixdimp, center_user, ipintp=1, ibinning=1):
         s = np.ascontiguousarray(slice_, np.int32).copy()
         imin, imax = C.c_int(), C.c_int()
@@ -102,6 +130,7 @@ def ref_lib():
     L.rvref_get_axis.argtypes = [U16P, U16P, U16P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]
     L.rvref_write_tif16.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int]
+    L.rvref_offset_ct.argtypes = OCT_ARGTYPES
     return L
 
 
@@ -124,3 +153,25 @@ def rel_l2(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oct_random_case(rng: np.random.Generator, trial: int) -> dict:
+    """A random offset-CT stitching case (frames, flags, centre, binning, trim, rows per frame)."""
+    F = int(rng.choice([32, 48, 64, 97, 128]))
+    interp = int(rng.choice([2, 2, 1, 0, 3]))
+    B = 4 if interp == 0 else (2 if interp == 1 else 1)
+    T = int(rng.choice([0, 0, 0, 2, 4, 8]))
+    M = int(rng.integers(1, 4))
+    V = int(rng.choice([40, 60, 61]))
+    right = rng.random() < 0.5
+    c = F - rng.uniform(2, F / 3) if right else rng.uniform(1, F / 3)
+    if rng.random() < 0.3:
+        c = float(np.round(c * 4) / 4)          # quarter-pixel centres hit the dc = 0 / 0.5 edges
+    dcent = float(rng.choice([0.0, 0.0, rng.uniform(-0.5, 0.5)]))
+    ixlen = F // B
+    sino, bInc, fdeg = phantom.offset_ct_sinogram(trial, ixlen, V, M, c / B, n_ellipsoids=5)
+    if rng.random() < 0.3:
+        bInc[rng.integers(2, V, 3)] = 0
+    nf = sino.shape[0]
+    return dict(rows=np.ascontiguousarray(sino.reshape(nf * M, ixlen)), ixlen=ixlen, bInc=bInc, fdeg=fdeg, M=M,
+                center=float(c), dcent=dcent, interp=interp, trim=T, F=F, iXdim=2 * F)
