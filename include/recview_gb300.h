@@ -367,9 +367,9 @@ int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInterpolation, 
  * afterwards).  format: 0 = the reference's 16-int table per detector pixel, 1 = the same padded
  * to 17 words (fewer shared-memory bank conflicts), 2 = the float pair (p0, slope) per
  * detector pixel, expanded by the kernel with the reference's operations (8x smaller tables,
- * conflict-free lookups).  variant 0..5 selects tile shape / threads / views per chunk (default:
- * format 0, variant 3, the fastest measured on GB300).  All
- * combinations give bit-identical slices. */
+ * conflict-free lookups).  variant 0..8 selects tile shape / threads / views per chunk, and
+ * whether the per-view coordinate products are tabulated in shared memory (0-5) or formed in
+ * registers (6-8) (default: format 0, variant 6).  All combinations give bit-identical slices. */
 int RvSetBackprojectionVariant(int variant, int format);
 int RvGetBackprojectionVariant(int* variant, int* format);
 

@@ -83,7 +83,7 @@ constexpr int isqrt_ceil(int n) {
     return r;
 }
 
-template <int WX, int WY, int RX, int RY, int VC, int PAD>
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int OTF = 0>
 struct BpCfg {
     static constexpr int NT = 32 * WX * WY;
     static constexpr int GX = 8 * WX, GY = 4 * WY;        // thread grid of the tile
@@ -92,28 +92,37 @@ struct BpCfg {
     // table-index span of a tile: 16*sqrt((TX-1)^2 + (TY-1)^2) + margins + alignment
     static constexpr int SPAN = 16 * isqrt_ceil((TX - 1) * (TX - 1) + (TY - 1) * (TY - 1)) + 2 + 3 + ALIGN + 16;
     static constexpr int WIN = PAD ? ((SPAN * 17 / 16 + 17 + 15) / 16) * 16 : ((SPAN + 15) / 16) * 16;
-    static constexpr size_t SMEM = (size_t)2 * VC * WIN * 4 + (size_t)3 * VC * (TX + TY) * 4 + (size_t)3 * VC * 32 + 16;
+    // shared layout in words: windows [2][VC][WIN], tabulated products [3][VC][TX+TY] (absent
+    // when OTF: the products are formed in registers), view records [3][VC][8], 2 mbarriers
+    static constexpr int XY_WORDS = OTF ? 0 : 3 * VC * (TX + TY);
+    static constexpr int META_OFF = 2 * VC * WIN + XY_WORDS;
+    static constexpr int BAR_OFF = META_OFF + 3 * VC * 8;
+    static constexpr size_t SMEM = (size_t)BAR_OFF * 4 + 16;
 };
 
+// Per-view record; the first 16 bytes are all the inner loop reads (one 128-bit load).
 struct ViewMeta {
-    int w0;      // window start in table-storage words
-    int nwin;    // window length in storage words (multiple of 4)
-    int a, b;    // in-table part [a, b) of the window (storage words, multiples of 4)
-    int fast;    // 1: every fx of the tile is >= 0 (exact floor by the 2^23 add)
-    int pad0, pad1, pad2;
+    float gc, gs, go;   // fcos, fsin, foffset of the view
+    unsigned off;       // byte offset from the window base to entry 0 (bit 0: fast path)
+    int w0;             // window start in table-storage words
+    int nwin;           // window length in storage words (multiple of 4)
+    int a, b;           // in-table part [a, b) of the window (storage words, multiples of 4)
 };
 
 // One tile of one slice.  ph[b] counts the completed phases of mbarrier b, so a persistent CTA
 // can run many tiles on the same barriers.  Returns false when a bounded wait ran out.
-template <int WX, int WY, int RX, int RY, int VC, int PAD, bool CHECKED>
+// OTF = 1 forms the per-view column/row products in registers (12 FP32 operations per view per
+// thread) instead of reading them from shared memory, which frees the shared-memory pipe -- the
+// kernel's binding resource -- for the table gathers.  Both forms round identically.
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int OTF, bool CHECKED>
 __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned (&ph)[2], unsigned* status_counter) {
-    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD, OTF>;
     constexpr int NT = Cfg::NT, TX = Cfg::TX, TY = Cfg::TY, WIN = Cfg::WIN;
     int* win = smi;                                                     // [2][VC][WIN]
-    float* xs = reinterpret_cast<float*>(win + 2 * VC * WIN);           // [3][VC][TX]
+    float* xs = reinterpret_cast<float*>(win + 2 * VC * WIN);           // [3][VC][TX]   (OTF: unused)
     float* ys = xs + 3 * VC * TX;                                       // [3][VC][TY]
-    ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * TY);     // [3][VC]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(meta + 3 * VC);        // [2]
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(smi + Cfg::META_OFF);  // [3][VC]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);   // [2]
 
     const int ixdimp = J.ixdimp;
     const int X0 = J.X0, Y0 = J.Y0;
@@ -125,8 +134,13 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
     const int nviews = J.nviews;
     const int nchunks = (nviews + VC - 1) / VC;
     unsigned viol = 0;
+    float colf[RX], rowf[RY];   // OTF: pixel coordinates as floats (exact: < 2^24)
+#pragma unroll
+    for (int c = 0; c < RX; c++) colf[c] = (float)(X0 + tx + Cfg::GX * c);
+#pragma unroll
+    for (int r = 0; r < RY; r++) rowf[r] = (float)(Y0 + ty + Cfg::GY * r);
 
-    // window bounds and tabulated products of chunk c into meta/xs/ys slot ms
+    // window bounds (and, unless OTF, tabulated products) of chunk c into meta/xs/ys slot ms
     auto prepare = [&](int c, int ms) {
         const int v0 = c * VC;
         if (tid < VC && v0 + tid < nviews) {
@@ -157,27 +171,28 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
             }
             m.a = max(m.w0, 0);
             m.b = min(m.w0 + m.nwin, nstore);
-            m.fast = (lo >= 2.0f) ? 1 : 0;
-            m.pad1 = (m.a != m.w0 || m.b != m.w0 + m.nwin) ? 1 : 0;   // needs zero-fill
-            m.pad2 = 0;
-            // byte offset that turns the index bits into a shared-memory address (fast/slow path)
-            {   // unsigned arithmetic: the offset is a 32-bit wrap-around quantity
-                const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
-                const unsigned off = 0u - 4u * (unsigned)m.w0 - (m.fast ? 4u * mag : 0u);
-                m.pad0 = (int)off;
-            }
+            const bool fast = lo >= 2.0f;
+            m.gc = g.x;
+            m.gs = g.y;
+            m.go = g.z;
+            // byte offset that turns the index bits into a shared-memory address (fast path: the
+            // 2^23 pattern is folded in); unsigned wrap-around arithmetic, bit 0 flags the path
+            const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
+            m.off = (0u - 4u * (unsigned)m.w0 - (fast ? 4u * mag : 0u)) | (fast ? 1u : 0u);
             meta[ms * VC + tid] = m;
         }
-        for (int e = tid; e < VC * (TX + TY); e += NT) {
-            const int vv = e / (TX + TY), w = e - vv * (TX + TY);
-            if (v0 + vv >= nviews) continue;
-            const float4 g = __ldg(J.geom + v0 + vv);
-            if (w < TX) {
-                const int t = w / RX, c = w - t * RX;          // xs[t*RX + c] = column of (tx=t, c)
-                xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
-            } else {
-                const int w2 = w - TX, t = w2 / RY, r = w2 - t * RY;
-                ys[(ms * VC + vv) * TY + w2] = faddr(fmulr((float)(Y0 + t + Cfg::GY * r), g.y), g.z);
+        if (!OTF) {
+            for (int e = tid; e < VC * (TX + TY); e += NT) {
+                const int vv = e / (TX + TY), w = e - vv * (TX + TY);
+                if (v0 + vv >= nviews) continue;
+                const float4 g = __ldg(J.geom + v0 + vv);
+                if (w < TX) {
+                    const int t = w / RX, c = w - t * RX;          // xs[t*RX + c] = column of (tx=t, c)
+                    xs[(ms * VC + vv) * TX + w] = fmulr((float)(X0 + t + Cfg::GX * c), g.x);
+                } else {
+                    const int w2 = w - TX, t = w2 / RY, r = w2 - t * RY;
+                    ys[(ms * VC + vv) * TY + w2] = faddr(fmulr((float)(Y0 + t + Cfg::GY * r), g.y), g.z);
+                }
             }
         }
     };
@@ -204,7 +219,7 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
         }
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[ms * VC + vv];
-            if (!m.pad1) continue;   // window entirely inside the table: nothing to zero
+            if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;   // inside the table: nothing to zero
             int4* w4 = reinterpret_cast<int4*>(win + (wb * VC + vv) * WIN);
             const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;   // [0, za) zero
             const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;   // [zb, nwin) zero
@@ -240,22 +255,34 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
         ph[wb]++;
         const int nv = min(VC, nviews - k * VC);
         for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[ms * VC + vv];
+            const float4 g = *reinterpret_cast<const float4*>(&meta[ms * VC + vv]);
             float xv[RX], yv[RY];
+            if (OTF) {
 #pragma unroll
-            for (int c4 = 0; c4 < RX; c4 += 4) {
-                const float4 t4 = *reinterpret_cast<const float4*>(xs + (ms * VC + vv) * TX + tx * RX + c4);
-                xv[c4] = t4.x; xv[c4 + 1] = t4.y; xv[c4 + 2] = t4.z; xv[c4 + 3] = t4.w;
-            }
+                for (int c = 0; c < RX; c++) xv[c] = fmulr(colf[c], g.x);
 #pragma unroll
-            for (int r4 = 0; r4 < RY; r4 += 4) {
-                const float4 t4 = *reinterpret_cast<const float4*>(ys + (ms * VC + vv) * TY + ty * RY + r4);
-                yv[r4] = t4.x; yv[r4 + 1] = t4.y; yv[r4 + 2] = t4.z; yv[r4 + 3] = t4.w;
+                for (int r = 0; r < RY; r++) yv[r] = faddr(fmulr(rowf[r], g.y), g.z);
+            } else {
+#pragma unroll
+                for (int c4 = 0; c4 < RX; c4 += 4) {
+                    const float4 t4 = *reinterpret_cast<const float4*>(xs + (ms * VC + vv) * TX + tx * RX + c4);
+                    xv[c4] = t4.x; xv[c4 + 1] = t4.y; xv[c4 + 2] = t4.z; xv[c4 + 3] = t4.w;
+                }
+#pragma unroll
+                for (int r4 = 0; r4 < RY; r4 += 4) {
+                    const float4 t4 = *reinterpret_cast<const float4*>(ys + (ms * VC + vv) * TY + ty * RY + r4);
+                    yv[r4] = t4.x; yv[r4 + 1] = t4.y; yv[r4 + 2] = t4.z; yv[r4 + 3] = t4.w;
+                }
             }
-            const unsigned wbase = smem_u32(win + (wb * VC + vv) * WIN) - 4u * (unsigned)m.w0;
-            if (m.fast) {
+            const unsigned offb = __float_as_uint(g.w);
+            const unsigned base = smem_u32(win + (wb * VC + vv) * WIN) + (offb & ~3u);
+            int cw0 = 0, cnw = 0;
+            if (CHECKED) {
+                cw0 = meta[ms * VC + vv].w0;
+                cnw = meta[ms * VC + vv].nwin;
+            }
+            if (offb & 1u) {
                 // index v = bits - 2^23 pattern; PAD: storage = v + (v >> 4)
-                const unsigned base = smem_u32(win + (wb * VC + vv) * WIN) + (unsigned)m.pad0;
 #pragma unroll
                 for (int r = 0; r < RY; r++)
 #pragma unroll
@@ -266,7 +293,7 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
                         if (CHECKED) {
                             const int v = (int)(bits - kMagicBits);
                             const int sw = PAD ? v + (v >> 4) : v;
-                            if (fx < 0.0f || sw < m.w0 || sw >= m.w0 + m.nwin) { viol++; continue; }
+                            if (fx < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
                         }
                         acc[r][c] += lds_s32(base + 4u * st);
                     }
@@ -279,9 +306,9 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
                         const int v = __float2int_rz(fx);
                         const int sw = PAD ? v + (v >> 4) : v;
                         if (CHECKED) {
-                            if (sw < m.w0 || sw >= m.w0 + m.nwin) { viol++; continue; }
+                            if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
                         }
-                        acc[r][c] += lds_s32(wbase + 4u * (unsigned)sw);
+                        acc[r][c] += lds_s32(base + 4u * (unsigned)sw);
                     }
             }
         }
@@ -304,10 +331,10 @@ __device__ __forceinline__ bool bp_ref_tile(const TileJob& J, int* smi, unsigned
     return true;
 }
 
-template <int WX, int WY, int RX, int RY, int VC, int PAD>
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int OTF>
 __device__ __forceinline__ void bp_init_barriers(int* smi) {
-    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + 2 * VC * Cfg::WIN + 3 * VC * (Cfg::TX + Cfg::TY) + 3 * VC * 8);
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD, OTF>;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);
     if (threadIdx.x == 0) {
         mbar_init(smem_u32(&bars[0]), 1);
         mbar_init(smem_u32(&bars[1]), 1);
@@ -316,11 +343,11 @@ __device__ __forceinline__ void bp_init_barriers(int* smi) {
 }
 
 // Grid form: blockIdx.x = tile, blockIdx.y = slice.
-template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, bool CHECKED>
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, int OTF, bool CHECKED>
 __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p) {
-    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD, OTF>;
     extern __shared__ __align__(128) int smi[];
-    bp_init_barriers<WX, WY, RX, RY, VC, PAD>(smi);
+    bp_init_barriers<WX, WY, RX, RY, VC, PAD, OTF>(smi);
     const int tiles_x = (p.ixdimp + Cfg::TX - 1) / Cfg::TX;
     TileJob J;
     J.table = p.table + (size_t)blockIdx.y * p.slice_table_stride;
@@ -332,17 +359,17 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref(BackprojLaunch p)
     J.X0 = (blockIdx.x % tiles_x) * Cfg::TX;
     J.Y0 = (blockIdx.x / tiles_x) * Cfg::TY;
     unsigned ph[2] = {0u, 0u};
-    bp_ref_tile<WX, WY, RX, RY, VC, PAD, CHECKED>(J, smi, ph, p.status_counter);
+    bp_ref_tile<WX, WY, RX, RY, VC, PAD, OTF, CHECKED>(J, smi, ph, p.status_counter);
 }
 
 // Persistent form: each CTA takes tiles from a device work list (uneven datasets) until it is
 // exhausted; *counter must be zero at launch.
-template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB>
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, int OTF>
 __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_persistent(const TileJob* jobs, int njobs,
                                                                           unsigned* counter) {
     extern __shared__ __align__(128) int smi[];
     __shared__ int s_item;
-    bp_init_barriers<WX, WY, RX, RY, VC, PAD>(smi);
+    bp_init_barriers<WX, WY, RX, RY, VC, PAD, OTF>(smi);
     unsigned ph[2] = {0u, 0u};
     for (;;) {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
@@ -350,7 +377,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_persistent(const 
         const int it = s_item;
         __syncthreads();
         if (it >= njobs) break;
-        if (!bp_ref_tile<WX, WY, RX, RY, VC, PAD, false>(jobs[it], smi, ph, nullptr)) return;
+        if (!bp_ref_tile<WX, WY, RX, RY, VC, PAD, OTF, false>(jobs[it], smi, ph, nullptr)) return;
     }
 }
 
@@ -361,6 +388,15 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_persistent(const 
 // ~10 consecutive 8-byte pairs (no bank conflicts) and the table is 8x smaller.  With
 // y = fl_rz(fx + 2^23) = 2^23 + floor(fx):  fl = y - 2^23 = floor(fx),
 // z = fl_rz(fl/16 + 2^23) = 2^23 + j,  k = fl - 16 j  -- all exact in FP32 for 0 <= fx < 2^23.
+// Per-view record of the pair-table kernel.
+struct PairMeta {
+    int w0;      // window start (pair index)
+    int nwin;    // window length in pairs
+    int a, b;    // in-table part [a, b) of the window
+    int fast;    // 1: every fx of the tile is >= 0
+    int pad0, pad1, pad2;
+};
+
 template <int WX, int WY, int RX, int RY, int VC>
 struct PairCfg {
     static constexpr int NT = 32 * WX * WY;
@@ -379,7 +415,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
     float2* win = reinterpret_cast<float2*>(smi);                       // [2][VC][WINJ]
     float* xs = reinterpret_cast<float*>(win + 2 * VC * WINJ);          // [3][VC][TX]
     float* ys = xs + 3 * VC * TX;                                       // [3][VC][TY]
-    ViewMeta* meta = reinterpret_cast<ViewMeta*>(ys + 3 * VC * TY);     // [3][VC]
+    PairMeta* meta = reinterpret_cast<PairMeta*>(ys + 3 * VC * TY);     // [3][VC]
     uint64_t* bars = reinterpret_cast<uint64_t*>(meta + 3 * VC);        // [2]
 
     const int ixdimp = p.ixdimp;
@@ -418,7 +454,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
             }
             const int ilo = (int)floorf(lo) - 2;       // index range [ilo, ihi)
             const int ihi = (int)floorf(hi) + 3;
-            ViewMeta m;
+            PairMeta m;
             m.w0 = (ilo >> 4) & ~1;                    // first pair (even, floor division)
             const int jhi = (((ihi - 1) >> 4) + 2) & ~1;
             m.nwin = min(jhi - m.w0, WINJ);
@@ -447,14 +483,14 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
         if (tid == 0) {
             unsigned bytes = 0;
             for (int vv = 0; vv < nv; vv++) {
-                const ViewMeta m = meta[ms * VC + vv];
+                const PairMeta m = meta[ms * VC + vv];
                 if (m.b > m.a) bytes += 8u * (unsigned)(m.b - m.a);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             const unsigned bar = smem_u32(&bars[wb]);
             mbar_arrive_expect_tx(bar, bytes);
             for (int vv = 0; vv < nv; vv++) {
-                const ViewMeta m = meta[ms * VC + vv];
+                const PairMeta m = meta[ms * VC + vv];
                 if (m.b <= m.a) continue;
                 const float2* src = tab + (size_t)(v0 + vv) * (p.table_stride / 2) + m.a;
                 const unsigned dst = smem_u32(win + (wb * VC + vv) * WINJ + (m.a - m.w0));
@@ -462,7 +498,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
             }
         }
         for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[ms * VC + vv];
+            const PairMeta m = meta[ms * VC + vv];
             float4* w4 = reinterpret_cast<float4*>(win + (wb * VC + vv) * WINJ);   // 2 pairs per float4
             const int za = (m.b > m.a) ? (m.a - m.w0) >> 1 : m.nwin >> 1;
             const int zb = (m.b > m.a) ? (m.b - m.w0) >> 1 : m.nwin >> 1;
@@ -494,7 +530,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
         }
         const int nv = min(VC, nviews - k * VC);
         for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[ms * VC + vv];
+            const PairMeta m = meta[ms * VC + vv];
             float xv[RX], yv[RY];
 #pragma unroll
             for (int c4 = 0; c4 < RX; c4 += 4) {
@@ -573,6 +609,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //     3: 64x64, 256 threads, 16 px/thread, 4 views/chunk, 4 CTAs/SM
 //     4: 128x64, 512 threads, 16 px/thread, 4 views/chunk, 2 CTAs/SM
 //     5: 64x128, 256 threads, 32 px/thread, 4 views/chunk, 2 CTAs/SM
+//     6, 7, 8: variants 3, 0, 4 with the column/row products formed in registers (OTF)
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -582,7 +619,7 @@ static int env_int(const char* name, int dflt) {
 }
 static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
-    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 3);
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 6);
     if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
 int ref_table_fmt() {
@@ -607,13 +644,14 @@ static cudaError_t launch_k(K kern, dim3 grid, int nt, size_t smem, const Backpr
     return cudaGetLastError();
 }
 
-template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB>
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, int OTF = 0>
 static cudaError_t go_bp(const BackprojLaunch& p, cudaStream_t s, bool checked) {
-    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD, OTF>;
     const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
     dim3 grid(tiles, p.nslices);
-    if (checked) return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
-    return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    if (checked)
+        return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, OTF, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, OTF, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
 template <int WX, int WY, int RX, int RY, int VC, int MINB>
@@ -633,6 +671,9 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 3: return go_bp<2, 4, 4, 4, 4, PAD, 4>(p, s, checked);
     case 4: return go_bp<4, 4, 4, 4, 4, PAD, 2>(p, s, checked);
     case 5: return go_bp<2, 4, 4, 8, 4, PAD, 2>(p, s, checked);
+    case 6: return go_bp<2, 4, 4, 4, 4, PAD, 4, 1>(p, s, checked);
+    case 7: return go_bp<4, 4, 4, 8, 8, PAD, 1, 1>(p, s, checked);
+    case 8: return go_bp<4, 4, 4, 4, 4, PAD, 2, 1>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -640,18 +681,18 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
 static cudaError_t dispatch_pair(const BackprojLaunch& p, cudaStream_t s, bool checked, int variant) {
     switch (variant) {
     case 1: return go_pair<2, 4, 4, 8, 16, 2>(p, s, checked);
-    case 2: case 4: case 5: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
-    case 3: return go_pair<2, 4, 4, 4, 8, 4>(p, s, checked);
+    case 2: case 4: case 5: case 8: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
+    case 3: case 6: return go_pair<2, 4, 4, 4, 8, 4>(p, s, checked);
     default: return go_pair<4, 4, 4, 8, 16, 1>(p, s, checked);
     }
 }
 
 // Persistent launcher for the batched queue: the tile shape of the selected int-table variant
 // (variants 0/2 -> 128x128, 4 -> 128x64, else 64x64), one grid of (SMs x resident CTAs).
-template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB>
+template <int WX, int WY, int RX, int RY, int VC, int PAD, int MINB, int OTF = 0>
 static cudaError_t go_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
-    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD>;
-    auto kern = k_bp_ref_persistent<WX, WY, RX, RY, VC, PAD, MINB>;
+    using Cfg = BpCfg<WX, WY, RX, RY, VC, PAD, OTF>;
+    auto kern = k_bp_ref_persistent<WX, WY, RX, RY, VC, PAD, MINB, OTF>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
@@ -669,8 +710,8 @@ static cudaError_t go_persistent(const TileJob* jobs, int njobs, unsigned* count
 
 static void persistent_shape(int variant, int* tx, int* ty) {
     switch (variant) {
-    case 0: case 2: *tx = 128; *ty = 128; break;
-    case 4: *tx = 128; *ty = 64; break;
+    case 0: case 2: case 7: *tx = 128; *ty = 128; break;
+    case 4: case 8: *tx = 128; *ty = 64; break;
     case 5: *tx = 64; *ty = 128; break;
     default: *tx = 64; *ty = 64; break;
     }
@@ -686,6 +727,9 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 4: return go_persistent<4, 4, 4, 4, 4, PAD, 2>(jobs, njobs, counter, s);
     case 5: return go_persistent<2, 4, 4, 8, 4, PAD, 2>(jobs, njobs, counter, s);
     case 1: return go_persistent<2, 4, 4, 4, 8, PAD, 1>(jobs, njobs, counter, s);
+    case 6: return go_persistent<2, 4, 4, 4, 4, PAD, 4, 1>(jobs, njobs, counter, s);
+    case 7: return go_persistent<4, 4, 4, 8, 8, PAD, 1, 1>(jobs, njobs, counter, s);
+    case 8: return go_persistent<4, 4, 4, 4, 4, PAD, 2, 1>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
 }
@@ -745,7 +789,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 5 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 8 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;
