@@ -40,6 +40,8 @@ struct RvStack {
     int nbatches_last = 0;
     float t_filter = 0, t_bp = 0, t_total = 0;
     int launches = 0;
+    cudaStream_t cs_in = nullptr, cs_out = nullptr;   // RunHost copy streams
+    std::vector<cudaEvent_t> pev;   // RunHost pipeline events
     int tfmt = 0;                   // REF table layout (ref_table_fmt at creation)
     long long tstride = 0;          // ints per table slot
 };
@@ -50,6 +52,10 @@ static void stack_free(RvStack* st) {
         if (p) cudaFree(p);
     for (cudaEvent_t& e : st->ev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : st->pev)
+        if (e) cudaEventDestroy(e);
+    if (st->cs_in) cudaStreamDestroy(st->cs_in);
+    if (st->cs_out) cudaStreamDestroy(st->cs_out);
 }
 
 static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_tables) {
@@ -211,70 +217,83 @@ extern "C" size_t RvStackInputBytes(const RvStack* st) {
 extern "C" int RvStackNumViews(const RvStack* st) { return st ? st->nviews : 0; }
 extern "C" int RvStackOutputDim(const RvStack* st) { return st ? st->d.ixdimp : 0; }
 
+// Filter + back-projection of slices [s0, s0 + nb) (nb <= batch) on stream s; ev_a/ev_b/ev_c
+// (may be null) bracket the two kernels.
+static int run_slices(RvStack* st, const void* d_raw, void* d_out, int s0, int nb, cudaStream_t s, cudaEvent_t ev_a,
+                      cudaEvent_t ev_b, cudaEvent_t ev_c) {
+    const Dims& d = st->d;
+    const int V = st->nviews, mode = st->desc.mode;
+    const long long tstride = st->tstride;
+    const size_t npix = (size_t)d.ixdimp * d.ixdimp;
+    FilterLaunch fl{};
+    fl.src = d_raw;
+    fl.raw = st->desc.input_is_sinogram ? 0 : 1;
+    fl.pixmin = (st->desc.iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit : RV_SINOGRAM_PIXEL_MIN16bit;
+    fl.jobs = static_cast<const RowJob*>(st->d_jobs) + (size_t)s0 * V;
+    fl.njobs = nb * V;
+    fl.filt = static_cast<const float*>(st->d_filt);
+    fl.tw = static_cast<const float2*>(st->d_tw);
+    fl.mode = mode;
+    fl.d = d;
+    fl.ic = (int)st->desc.center;
+    if (mode == RV_MODE_REF) {
+        fl.table = static_cast<int*>(st->d_table);
+        fl.table_stride = tstride;
+        fl.table_fmt = st->tfmt;
+    } else if (mode == RV_MODE_LIN) {
+        fl.rows = static_cast<float*>(st->d_table);
+        fl.row_stride = d.ixdimp;
+    } else {
+        fl.rows16 = st->d_table;
+        fl.row_scale = static_cast<float*>(st->d_scale);
+        fl.row_stride = d.ixdimp;
+    }
+    // jobs of slice s write table slot (s mod batch): rebase so the first slice of this call
+    // lands where its jobs point
+    if (ev_a) cudaEventRecord(ev_a, s);
+    cudaError_t e = launch_filter(fl, s);
+    if (!cuda_ok(e, RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
+    if (ev_b) cudaEventRecord(ev_b, s);
+    BackprojLaunch bl{};
+    const size_t slot0 = (size_t)(s0 % st->batch);
+    bl.table = static_cast<const int*>(st->d_table) + slot0 * (size_t)(tstride * V);
+    bl.rows = static_cast<const float*>(st->d_table) + slot0 * (size_t)d.ixdimp * V;
+    bl.rows16 = static_cast<const char*>(st->d_table) + slot0 * (size_t)d.ixdimp * V * 2;
+    bl.row_scale = static_cast<const float*>(st->d_scale) + slot0 * V;
+    bl.geom = static_cast<const float4*>(st->d_geom);
+    bl.nviews = V;
+    bl.nslices = nb;
+    bl.ixdimp = d.ixdimp;
+    bl.table_stride = tstride;
+    bl.slice_table_stride = tstride * V;
+    bl.row_stride = d.ixdimp;
+    bl.slice_row_stride = (long long)d.ixdimp * V;
+    bl.out = mode == RV_MODE_REF ? (void*)(static_cast<int*>(d_out) + (size_t)s0 * npix)
+                                 : (void*)(static_cast<float*>(d_out) + (size_t)s0 * npix);
+    bl.out_slice_stride = (long long)npix;
+    bl.mode = mode;
+    bl.table_fmt = st->tfmt;
+    e = launch_backproject(bl, s);
+    if (!cuda_ok(e, RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
+    if (ev_c) cudaEventRecord(ev_c, s);
+    st->launches += 2;
+    return 0;
+}
+
 extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, void* stream) {
     if (!st || !d_raw || !d_out) {
         set_error(RV_ERR_BAD_ARGUMENT, "RvStackRunDevice: NULL argument");
         return RV_ERR_BAD_ARGUMENT;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    const Dims& d = st->d;
-    const int S = st->desc.nslices, V = st->nviews, mode = st->desc.mode;
-    const long long tstride = st->tstride;
-    const size_t npix = (size_t)d.ixdimp * d.ixdimp;
+    const int S = st->desc.nslices;
     st->launches = 0;
     float tf = 0, tb = 0;
     cudaEventRecord(st->ev[4], s);
     for (int s0 = 0; s0 < S; s0 += st->batch) {
         const int nb = (S - s0) < st->batch ? (S - s0) : st->batch;
-        FilterLaunch fl{};
-        fl.src = d_raw;
-        fl.raw = st->desc.input_is_sinogram ? 0 : 1;
-        fl.pixmin = (st->desc.iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit : RV_SINOGRAM_PIXEL_MIN16bit;
-        fl.jobs = static_cast<const RowJob*>(st->d_jobs) + (size_t)s0 * V;
-        fl.njobs = nb * V;
-        fl.filt = static_cast<const float*>(st->d_filt);
-        fl.tw = static_cast<const float2*>(st->d_tw);
-        fl.mode = mode;
-        fl.d = d;
-        fl.ic = (int)st->desc.center;
-        if (mode == RV_MODE_REF) {
-            fl.table = static_cast<int*>(st->d_table);
-            fl.table_stride = tstride;
-            fl.table_fmt = st->tfmt;
-        } else if (mode == RV_MODE_LIN) {
-            fl.rows = static_cast<float*>(st->d_table);
-            fl.row_stride = d.ixdimp;
-        } else {
-            fl.rows16 = st->d_table;
-            fl.row_scale = static_cast<float*>(st->d_scale);
-            fl.row_stride = d.ixdimp;
-        }
-        cudaEventRecord(st->ev[0], s);
-        cudaError_t e = launch_filter(fl, s);
-        if (!cuda_ok(e, RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
-        cudaEventRecord(st->ev[1], s);
-        BackprojLaunch bl{};
-        bl.table = static_cast<const int*>(st->d_table);
-        bl.rows = static_cast<const float*>(st->d_table);
-        bl.rows16 = st->d_table;
-        bl.row_scale = static_cast<const float*>(st->d_scale);
-        bl.geom = static_cast<const float4*>(st->d_geom);
-        bl.nviews = V;
-        bl.nslices = nb;
-        bl.ixdimp = d.ixdimp;
-        bl.table_stride = tstride;
-        bl.slice_table_stride = tstride * V;
-        bl.row_stride = d.ixdimp;
-        bl.slice_row_stride = (long long)d.ixdimp * V;
-        bl.out = mode == RV_MODE_REF ? (void*)(static_cast<int*>(d_out) + (size_t)s0 * npix)
-                                     : (void*)(static_cast<float*>(d_out) + (size_t)s0 * npix);
-        bl.out_slice_stride = (long long)npix;
-        bl.mode = mode;
-        bl.table_fmt = st->tfmt;
-        e = launch_backproject(bl, s);
-        if (!cuda_ok(e, RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
-        cudaEventRecord(st->ev[2], s);
-        st->launches += 2;
+        const int rc = run_slices(st, d_raw, d_out, s0, nb, s, st->ev[0], st->ev[1], st->ev[2]);
+        if (rc) return rc;
         if (cudaEventSynchronize(st->ev[2]) == cudaSuccess) {
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, st->ev[0], st->ev[1]);
@@ -298,14 +317,11 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
     return 0;
 }
 
-extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void* stream) {
-    if (!st || !h_raw || !h_out) {
-        set_error(RV_ERR_BAD_ARGUMENT, "RvStackRunHost: NULL argument");
-        return RV_ERR_BAD_ARGUMENT;
-    }
-    cudaStream_t s = (cudaStream_t)stream;
-    const size_t in_b = RvStackInputBytes(st);
-    const size_t out_b = RvStackSliceBytes(st) * st->desc.nslices;
+// Host-buffer run, pipelined: the slices are processed in pieces; piece k's frames (all frames,
+// the piece's detector rows: one strided 2-D copy) go up on an input copy stream, its filter and
+// back-projection run on the caller's stream, and its slices come back on an output copy stream,
+// so host<->device traffic overlaps the kernels of neighbouring pieces.
+static int ensure_host_buffers(RvStack* st, size_t in_b, size_t out_b) {
     if (st->in_bytes < in_b) {
         if (st->d_in) cudaFree(st->d_in);
         st->d_in = nullptr;
@@ -320,13 +336,94 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
         if (!cuda_ok(cudaMalloc(&st->d_out, out_b), RV_ERR_DEVICE_OOM, "output buffer")) return RV_ERR_DEVICE_OOM;
         st->out_bytes = out_b;
     }
-    if (!cuda_ok(cudaMemcpyAsync(st->d_in, h_raw, in_b, cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D, "raw frames"))
-        return RV_ERR_COPY_H2D;
-    int rc = RvStackRunDevice(st, st->d_in, st->d_out, stream);
+    if (!st->cs_in) {
+        if (!cuda_ok(cudaStreamCreateWithFlags(&st->cs_in, cudaStreamNonBlocking), RV_ERR_STREAM, "copy stream") ||
+            !cuda_ok(cudaStreamCreateWithFlags(&st->cs_out, cudaStreamNonBlocking), RV_ERR_STREAM, "copy stream"))
+            return RV_ERR_STREAM;
+    }
+    return 0;
+}
+
+static int piece_slices(const RvStack* st) {
+    int pieces = 8;
+    if (const char* e = getenv("RV_STACK_PIECES")) pieces = atoi(e);
+    const int S = st->desc.nslices;
+    if (pieces < 1) pieces = 1;
+    int p = (S + pieces - 1) / pieces;
+    if (p > st->batch) p = st->batch;
+    if (p < 1) p = 1;
+    while (st->batch % p) p--;   // a piece never straddles two table batches (slots s mod batch)
+    return p;
+}
+
+extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void* stream) {
+    if (!st || !h_raw || !h_out) {
+        set_error(RV_ERR_BAD_ARGUMENT, "RvStackRunHost: NULL argument");
+        return RV_ERR_BAD_ARGUMENT;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int S = st->desc.nslices, W = st->desc.ixdim, nfr = st->desc.nframes + 1;
+    const size_t in_b = RvStackInputBytes(st);
+    const size_t slice_b = RvStackSliceBytes(st);
+    int rc = ensure_host_buffers(st, in_b, slice_b * S);
     if (rc) return rc;
-    if (!cuda_ok(cudaMemcpyAsync(h_out, st->d_out, out_b, cudaMemcpyDeviceToHost, s), RV_ERR_COPY_D2H, "slices") ||
-        !cuda_ok(cudaStreamSynchronize(s), RV_ERR_COPY_D2H, "slices"))
-        return RV_ERR_COPY_D2H;
+    const int P = piece_slices(st);
+    const int npieces = (S + P - 1) / P;
+    // events: start, per piece {in copied, filter start, filter end, bp end, out copied}, end
+    const size_t need = 2 + 5 * (size_t)npieces;
+    while (st->pev.size() < need) {
+        cudaEvent_t e = nullptr;
+        if (!cuda_ok(cudaEventCreate(&e), RV_ERR_LAUNCH, "event")) return RV_ERR_LAUNCH;
+        st->pev.push_back(e);
+    }
+    cudaEvent_t* E = st->pev.data();
+    st->launches = 0;
+    // the copy streams start after earlier work of the caller's stream on these buffers
+    cudaEventRecord(E[0], s);
+    cudaStreamWaitEvent(st->cs_in, E[0], 0);
+    cudaStreamWaitEvent(st->cs_out, E[0], 0);
+    const size_t pitch = (size_t)S * W * 2;
+    for (int k = 0; k < npieces; k++) {
+        const int s0 = k * P, nb = (S - s0) < P ? (S - s0) : P;
+        cudaEvent_t* e = E + 1 + 5 * (size_t)k;
+        const char* src = static_cast<const char*>(h_raw) + (size_t)s0 * W * 2;
+        char* dst = static_cast<char*>(st->d_in) + (size_t)s0 * W * 2;
+        if (!cuda_ok(cudaMemcpy2DAsync(dst, pitch, src, pitch, (size_t)nb * W * 2, nfr, cudaMemcpyHostToDevice,
+                                       st->cs_in), RV_ERR_COPY_H2D, "raw frames"))
+            return RV_ERR_COPY_H2D;
+        cudaEventRecord(e[0], st->cs_in);
+        cudaStreamWaitEvent(s, e[0], 0);
+        rc = run_slices(st, st->d_in, st->d_out, s0, nb, s, e[1], e[2], e[3]);
+        if (rc) return rc;
+        cudaStreamWaitEvent(st->cs_out, e[3], 0);
+        if (!cuda_ok(cudaMemcpyAsync(static_cast<char*>(h_out) + (size_t)s0 * slice_b,
+                                     static_cast<const char*>(st->d_out) + (size_t)s0 * slice_b, (size_t)nb * slice_b,
+                                     cudaMemcpyDeviceToHost, st->cs_out), RV_ERR_COPY_D2H, "slices"))
+            return RV_ERR_COPY_D2H;
+        cudaEventRecord(e[4], st->cs_out);
+    }
+    // the caller's stream (and so a later call) waits for the last copy back
+    cudaEvent_t end = E[1 + 5 * (size_t)npieces];
+    cudaStreamWaitEvent(s, E[5 * (size_t)npieces], 0);
+    cudaEventRecord(end, s);
+    if (!cuda_ok(cudaEventSynchronize(end), RV_ERR_COPY_D2H, "stack run")) return RV_ERR_COPY_D2H;
+    if (take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+        return RV_ERR_KERNEL_STATUS;
+    }
+    float tf = 0, tb = 0, tt = 0;
+    for (int k = 0; k < npieces; k++) {
+        cudaEvent_t* e = E + 1 + 5 * (size_t)k;
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, e[1], e[2]);
+        cudaEventElapsedTime(&b, e[2], e[3]);
+        tf += a;
+        tb += b;
+    }
+    cudaEventElapsedTime(&tt, E[0], end);
+    st->t_filter = tf;
+    st->t_bp = tb;
+    st->t_total = tt;
     return 0;
 }
 

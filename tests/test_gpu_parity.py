@@ -249,6 +249,26 @@ def test_stack_ref_bit_exact(gpu, oracle, monkeypatch, W, V, S, cen, interp, bud
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("pieces,budget_mb", [(1, None), (3, 5), (4, 5), (5, 5), (64, None)])
+def test_stack_host_pipeline_pieces(gpu, oracle, monkeypatch, pieces, budget_mb):
+    """RvStackRunHost overlaps copies with kernels piece by piece; any piece size (and table
+    batches of 4 slices under a 5 MB budget) must give the same slices as the oracle."""
+    monkeypatch.setenv("RV_STACK_PIECES", str(pieces))
+    if budget_mb is not None:
+        monkeypatch.setenv("RV_TABLE_BUDGET_MB", str(budget_mb))
+    W, V, S, cen = 128, 150, 10, 63.3
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(71, W, V, S, cen, n_ellipsoids=10)
+    F = oracle.set_filter(abi.FILT_SHEPP, dims(W).ndim)
+    st = rv.Stack(ixdim=W, nframes=raw.shape[0] - 1, nslices=S, center=cen, bInc=bInc, fdeg=fdeg, fexp=fexp,
+                  fFilter=F)
+    want = _stack_oracle(oracle, raw, bInc, fdeg, fexp, cen, F, 2)
+    for _ in range(2):                       # a second call reuses buffers, streams and events
+        got = st.run_host(raw)
+        assert np.array_equal(got, want)
+    assert st.launches() >= 2 and st.launches() % 2 == 0     # a filter and a back-projection per piece
+    st.close()
+
+
 @pytest.mark.parametrize("mode,tol", [(abi.MODE_LIN, 2e-5), (abi.MODE_LIN_F16, 1e-3), (abi.MODE_LIN_BF16, 8e-3)])
 def test_stack_lin_modes_vs_fp64(gpu, oracle, mode, tol):
     """LIN modes: FP32 interpolation/accumulation with FP32/FP16/BF16 filtered rows; relative L2
