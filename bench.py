@@ -37,6 +37,10 @@ sys.path.insert(0, str(ROOT))
 W_DET, N_VIEWS, N_SLICES = 2048, 1800, 64
 PUBLISHED_TAU_NS = 0.029  # RTX A4000, 2048^2 x 1800 views (reference README, Build-220422)
 WORKLOAD = "fbp-2048det-1800views-64slices-raw-uint16"
+# DRAM bytes (read + write) per pixel-view update of k_bp_ref, from one ncu capture of the default
+# variant on 2 slices of this geometry (profiles/k_bp_ref_2048x1800x2.md); the traffic grows in
+# proportion to the slices processed, so a full launch moves this times its updates.
+BP_DRAM_BYTES_PER_UPDATE = 1.2609e-1
 
 
 def parse():
@@ -312,10 +316,12 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         del raw_h, out_h
 
     # ---- roofline of the dominant kernel (back-projection) ----------------------------------
-    probe = (C.c_double * 2)()
-    L.RvProbeThroughput(probe, 2)
-    fp32_tflops, f2i_gops = probe[0], probe[1]
-    achieved = 4.0 * updates_step / (bp_ms * 1e-3) / 1e12      # 4 FP32 FLOP per pixel-view update
+    probe = (C.c_double * 3)()
+    L.RvProbeThroughput(probe, 3)
+    fp32_tflops, f2i_gops, smem_gbs = probe[0], probe[1], probe[2]
+    upd_bp = updates_step / (bp_ms * 1e-3)                      # one k_bp_ref launch per step
+    # algorithmic shared-memory bytes: one 4-byte table entry gathered per pixel-view update
+    smem_achieved = 4.0 * upd_bp / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = peaks.get("hbm_gbs")
     nviews = st.nviews
@@ -325,7 +331,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     if hbm and filt_ms > 0:
         a = filt_bytes / (filt_ms * 1e-3) / 1e9
         roof_filter = {"bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
-                       "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+                       "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                       "note": "HBM is not this kernel's binding resource: its radix-2 passes are shared-memory bound"}
 
     if rank == 0:
         line = {
@@ -343,12 +350,16 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "stage_ms": {"filter": filt_ms, "backprojection": bp_ms},
             "e2e": e2e,
             "gpu_launches": launches,
-            "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": fp32_tflops, "unit": "TFLOP/s",
-                         "frac": achieved / fp32_tflops if fp32_tflops else None, "traffic": None,
-                         "kernel": "k_bp_ref", "flop_per_update": 4,
-                         "peak_source": "measured in this run (RvProbeThroughput FP32 FMA burst)",
+            "roofline": {"bound": "smem", "achieved": smem_achieved, "peak": smem_gbs, "unit": "GB/s",
+                         "frac": smem_achieved / smem_gbs if smem_gbs else None,
+                         "traffic": BP_DRAM_BYTES_PER_UPDATE * updates_step if mode == abi.MODE_REF else None,
+                         "kernel": "k_bp_ref", "bytes_per_update": 4,
+                         "peak_source": "measured in this run (RvProbeThroughput: conflict-free 32-bit shared loads)",
+                         "updates_per_s_bp": upd_bp,
+                         "fp32": {"achieved_tflops": 4.0 * upd_bp / 1e12, "peak_tflops": fp32_tflops,
+                                  "frac": 4.0 * upd_bp / 1e12 / fp32_tflops if fp32_tflops else None},
                          "f2i_gops_measured": f2i_gops,
-                         "updates_per_s_bp": updates_step / (bp_ms * 1e-3)},
+                         "hbm_frac": (BP_DRAM_BYTES_PER_UPDATE * upd_bp / 1e9 / hbm) if hbm else None},
             "roofline_filter": roof_filter,
             "clocks": clocks,
         }

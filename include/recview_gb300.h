@@ -367,15 +367,19 @@ int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInterpolation, 
  * afterwards).  format: 0 = the reference's 16-int table per detector pixel, 1 = the same padded
  * to 17 words (fewer shared-memory bank conflicts), 2 = the float pair (p0, slope) per
  * detector pixel, expanded by the kernel with the reference's operations (8x smaller tables,
- * conflict-free lookups).  variant 0..8 selects tile shape / threads / views per chunk, and
+ * conflict-free lookups).  variant 0..15 selects tile shape / threads / views per chunk, and
  * whether the per-view coordinate products are tabulated in shared memory (0-5) or formed in
- * registers (6-8) (default: format 0, variant 6).  All combinations give bit-identical slices. */
+ * registers (6-15), and whether warps synchronise per chunk (0-8) or only wait for their data
+ * (9-15) (default: format 0, variant 11).  All combinations give bit-identical slices. */
 int RvSetBackprojectionVariant(int variant, int format);
 int RvGetBackprojectionVariant(int* variant, int* format);
 
 /* Device throughput probes used as roofline denominators for the back-projection, which is
- * bound by instruction issue rather than HBM or tensor cores: out[0] = FP32 FMA TFLOP/s,
- * out[1] = float->int32 conversions in G/s, both measured on the current device. */
+ * bound by the shared-memory pipe (its table gathers) rather than HBM or tensor cores:
+ * out[0] = FP32 FMA TFLOP/s,
+ * out[1] = float->int32 conversions in G/s and, when n >= 3, out[2] = shared-memory load bandwidth
+ * in GB/s (conflict-free 32-bit loads, one 128-byte wavefront per warp instruction), all measured
+ * on the current device. */
 int RvProbeThroughput(double* out, int n);
 
 /* ---- Offset-CT (360-degree scan with the rotation axis near one edge of the frame) ----------

@@ -56,6 +56,9 @@ __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
 __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -381,6 +384,273 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_persistent(const 
     }
 }
 
+// ---- warp-decoupled pipeline ------------------------------------------------------------------
+// The same per-update arithmetic as bp_ref_tile (products in registers), but without a block-wide
+// barrier per chunk: NB window buffers, each with a "full" mbarrier (completed by the TMA bytes)
+// and an "empty" mbarrier (one arrival per warp when it has finished reading the buffer).  Warp 0
+// also produces: before consuming chunk c it refills the buffer of chunk c-1 with chunk c+NB-1,
+// after that buffer's empty barrier shows every warp is done with it.  Other warps never wait
+// for each other, only for data.  Every wait is bounded; a timeout sets g_kernel_status, gives
+// the copies this CTA issued a bounded chance to land, and ends the tile.
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD>
+struct PipeCfg {
+    using Base = BpCfg<WX, WY, RX, RY, VC, PAD, 1>;
+    static constexpr int NT = Base::NT, NW = NT / 32;
+    static constexpr int GX = Base::GX, GY = Base::GY, TX = Base::TX, TY = Base::TY;
+    static constexpr int ALIGN = Base::ALIGN, WIN = Base::WIN;
+    static constexpr int META_OFF = NB * VC * WIN;             // words
+    static constexpr int BAR_OFF = META_OFF + NB * VC * 8;     // full[NB], empty[NB] (8 B each)
+    static constexpr size_t SMEM = (size_t)BAR_OFF * 4 + (size_t)2 * NB * 8;
+};
+
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD>
+__device__ __forceinline__ void pipe_init_barriers(int* smi) {
+    using Cfg = PipeCfg<WX, WY, RX, RY, VC, NB, PAD>;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NB; b++) {
+            mbar_init(smem_u32(&bars[b]), 1);
+            mbar_init(smem_u32(&bars[NB + b]), Cfg::NW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+}
+
+// One tile.  gc = chunks this CTA has run through the buffers before this tile (the phase
+// bookkeeping of a persistent CTA); returns false after a bounded wait ran out.
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD, bool CHECKED>
+__device__ __forceinline__ bool bp_ref_tile_pipe(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter) {
+    using Cfg = PipeCfg<WX, WY, RX, RY, VC, NB, PAD>;
+    constexpr int TX = Cfg::TX, TY = Cfg::TY, WIN = Cfg::WIN;
+    int* win = smi;                                                     // [NB][VC][WIN]
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(smi + Cfg::META_OFF);  // [NB][VC]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);   // full[NB], empty[NB]
+    const int ixdimp = J.ixdimp;
+    const int X0 = J.X0, Y0 = J.Y0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = (warp % WX) * 8 + (lane & 7);
+    const int ty = (warp / WX) * 4 + (lane >> 3);
+    const int* tab = J.table;
+    const int nstore = PAD ? ((17 * ixdimp + 3) & ~3) : 16 * ixdimp;
+    const int nviews = J.nviews;
+    const int nchunks = (nviews + VC - 1) / VC;
+    unsigned viol = 0;
+    float colf[RX], rowf[RY];
+#pragma unroll
+    for (int c = 0; c < RX; c++) colf[c] = (float)(X0 + tx + Cfg::GX * c);
+#pragma unroll
+    for (int r = 0; r < RY; r++) rowf[r] = (float)(Y0 + ty + Cfg::GY * r);
+
+    // warp 0: fill the buffer of chunk c (global chunk number g); false on a timeout
+    auto produce = [&](int c, unsigned g) -> bool {
+        const int b = (int)(g % NB);
+        // warp-uniform verdict: every lane takes the same branch at the __syncwarp()s below
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
+            return false;
+        const int v0 = c * VC;
+        const int nv = min(VC, nviews - v0);
+        if (lane < nv) {
+            const float4 gg = __ldg(J.geom + v0 + lane);
+            float lo = 3.0e38f, hi = -3.0e38f;
+#pragma unroll
+            for (int cy = 0; cy < 2; cy++) {
+                const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), gg.y), gg.z);
+#pragma unroll
+                for (int cx = 0; cx < 2; cx++) {
+                    const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), gg.x), fy);
+                    lo = fminf(lo, fx);
+                    hi = fmaxf(hi, fx);
+                }
+            }
+            const int ilo = (int)floorf(lo) - 2;
+            const int lo_a = ilo >= 0 ? (ilo & ~(Cfg::ALIGN - 1)) : -((-ilo + Cfg::ALIGN - 1) & ~(Cfg::ALIGN - 1));
+            const int ihi = (int)floorf(hi) + 3;
+            ViewMeta m;
+            if (PAD) {
+                const int hi16 = (ihi + 15) & ~15;
+                m.w0 = lo_a + lo_a / 16;
+                const int w1 = hi16 + hi16 / 16;
+                m.nwin = min(((w1 - m.w0) + 3) & ~3, WIN);
+            } else {
+                m.w0 = lo_a;
+                m.nwin = min(((ihi - lo_a) + 3) & ~3, WIN);
+            }
+            m.a = max(m.w0, 0);
+            m.b = min(m.w0 + m.nwin, nstore);
+            const bool fast = lo >= 2.0f;
+            m.gc = gg.x;
+            m.gs = gg.y;
+            m.go = gg.z;
+            const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
+            m.off = (0u - 4u * (unsigned)m.w0 - (fast ? 4u * mag : 0u)) | (fast ? 1u : 0u);
+            meta[b * VC + lane] = m;
+        }
+        __syncwarp();
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[b * VC + vv];
+            if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
+            int4* w4 = reinterpret_cast<int4*>(win + (b * VC + vv) * WIN);
+            const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;
+            const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;
+            for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+            for (int e = zb + lane; e < (m.nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            unsigned bytes = 0;
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[b * VC + vv];
+                if (m.b > m.a) bytes += 4u * (unsigned)(m.b - m.a);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const unsigned bar = smem_u32(&bars[b]);
+            mbar_arrive_expect_tx(bar, bytes);
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[b * VC + vv];
+                if (m.b <= m.a) continue;
+                const int* src = tab + (size_t)(v0 + vv) * J.table_stride + m.a;
+                const unsigned dst = smem_u32(win + (b * VC + vv) * WIN + (m.a - m.w0));
+                tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
+            }
+        }
+        __syncwarp();
+        return true;
+    };
+
+    int acc[RY][RX];
+#pragma unroll
+    for (int r = 0; r < RY; r++)
+#pragma unroll
+        for (int c = 0; c < RX; c++) acc[r][c] = 0;
+
+    bool ok = true;
+    int produced = 0;   // warp 0: chunks of this tile whose fill has been issued
+    if (warp == 0) {
+        for (; produced < nchunks && produced < NB - 1; produced++)
+            if (!produce(produced, gc + (unsigned)produced)) { ok = false; break; }
+    }
+    for (int k = 0; ok && k < nchunks; k++) {
+        if (warp == 0 && produced < nchunks) {
+            if (!produce(produced, gc + (unsigned)produced)) { ok = false; break; }
+            produced++;
+        }
+        const unsigned g = gc + (unsigned)k;
+        const int b = (int)(g % NB);
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) { ok = false; break; }
+        const int nv = min(VC, nviews - k * VC);
+        for (int vv = 0; vv < nv; vv++) {
+            const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+            float xv[RX], yv[RY];
+#pragma unroll
+            for (int c = 0; c < RX; c++) xv[c] = fmulr(colf[c], gm.x);
+#pragma unroll
+            for (int r = 0; r < RY; r++) yv[r] = faddr(fmulr(rowf[r], gm.y), gm.z);
+            const unsigned offb = __float_as_uint(gm.w);
+            const unsigned base = smem_u32(win + (b * VC + vv) * WIN) + (offb & ~3u);
+            int cw0 = 0, cnw = 0;
+            if (CHECKED) {
+                cw0 = meta[b * VC + vv].w0;
+                cnw = meta[b * VC + vv].nwin;
+            }
+            if (offb & 1u) {
+#pragma unroll
+                for (int r = 0; r < RY; r++)
+#pragma unroll
+                    for (int c = 0; c < RX; c++) {
+                        const float fx = faddr(xv[c], yv[r]);
+                        const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
+                        const unsigned st = PAD ? bits + (bits >> 4) : bits;
+                        if (CHECKED) {
+                            const int v = (int)(bits - kMagicBits);
+                            const int sw = PAD ? v + (v >> 4) : v;
+                            if (fx < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+                        }
+                        acc[r][c] += lds_s32(base + 4u * st);
+                    }
+            } else {
+#pragma unroll
+                for (int r = 0; r < RY; r++)
+#pragma unroll
+                    for (int c = 0; c < RX; c++) {
+                        const float fx = faddr(xv[c], yv[r]);
+                        const int v = __float2int_rz(fx);
+                        const int sw = PAD ? v + (v >> 4) : v;
+                        if (CHECKED) {
+                            if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+                        }
+                        acc[r][c] += lds_s32(base + 4u * (unsigned)sw);
+                    }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
+    }
+    if (!ok) {
+        atomicOr(&g_kernel_status, 1u);
+        // warp 0 issued fills up to chunk `produced`: give them a bounded chance to land before
+        // the CTA can leave (later consumers of these buffers are gone)
+        if (warp == 0) {
+            for (int c = produced > NB ? produced - NB : 0; c < produced; c++) {   // last fill of each buffer
+                const unsigned g = gc + (unsigned)c;
+                mbar_wait_bounded(smem_u32(&bars[g % NB]), (g / NB) & 1u);
+            }
+        }
+        return false;
+    }
+    if (CHECKED && viol) atomicAdd(status_counter, viol);
+    int* out = J.out;
+#pragma unroll
+    for (int r = 0; r < RY; r++) {
+        const int y = Y0 + ty + Cfg::GY * r;
+        if (y >= ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < RX; c++) {
+            const int x = X0 + tx + Cfg::GX * c;
+            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+        }
+    }
+    return true;
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD, int MINB, bool CHECKED>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_pipe(BackprojLaunch p) {
+    using Cfg = PipeCfg<WX, WY, RX, RY, VC, NB, PAD>;
+    extern __shared__ __align__(128) int smi[];
+    pipe_init_barriers<WX, WY, RX, RY, VC, NB, PAD>(smi);
+    __syncthreads();
+    const int tiles_x = (p.ixdimp + Cfg::TX - 1) / Cfg::TX;
+    TileJob J;
+    J.table = p.table + (size_t)blockIdx.y * p.slice_table_stride;
+    J.geom = p.geom + (size_t)blockIdx.y * p.geom_slice_stride;
+    J.out = static_cast<int*>(p.out) + (size_t)blockIdx.y * p.out_slice_stride;
+    J.table_stride = p.table_stride;
+    J.nviews = p.nviews;
+    J.ixdimp = p.ixdimp;
+    J.X0 = (blockIdx.x % tiles_x) * Cfg::TX;
+    J.Y0 = (blockIdx.x / tiles_x) * Cfg::TY;
+    bp_ref_tile_pipe<WX, WY, RX, RY, VC, NB, PAD, CHECKED>(J, smi, 0u, p.status_counter);
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD, int MINB>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_pipe_persistent(const TileJob* jobs, int njobs,
+                                                                               unsigned* counter) {
+    extern __shared__ __align__(128) int smi[];
+    __shared__ int s_item;
+    pipe_init_barriers<WX, WY, RX, RY, VC, NB, PAD>(smi);
+    unsigned gc = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= njobs) break;
+        const TileJob J = jobs[it];
+        const bool tok = bp_ref_tile_pipe<WX, WY, RX, RY, VC, NB, PAD, false>(J, smi, gc, nullptr);
+        if (__syncthreads_or(!tok)) return;   // the CTA leaves together after a timeout
+        gc += (unsigned)((J.nviews + VC - 1) / VC);
+    }
+}
+
 // ---- pair-table variant ------------------------------------------------------------------------
 // The table holds, per detector pixel j, the float pair (p0, p1p0) from which the reference builds
 // its 16 ints (source/general.cpp:2130-2137).  Each update rebuilds its entry with the same float
@@ -610,6 +880,9 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //     4: 128x64, 512 threads, 16 px/thread, 4 views/chunk, 2 CTAs/SM
 //     5: 64x128, 256 threads, 32 px/thread, 4 views/chunk, 2 CTAs/SM
 //     6, 7, 8: variants 3, 0, 4 with the column/row products formed in registers (OTF)
+//     9, 10, 11: 64x64 OTF without block barriers (warp-decoupled pipeline) with 3x3, 4x2, 2x4
+//        buffers x views per chunk;  12: 128x128, 512 threads, 3 buffers x 4 views;
+//     13: 128x64, 512 threads, 2 x 4;  14, 15: 64x64, 2 buffers x 5 / 6 views, 3 CTAs/SM
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -619,7 +892,7 @@ static int env_int(const char* name, int dflt) {
 }
 static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
-    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 6);
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 11);
     if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
 int ref_table_fmt() {
@@ -654,6 +927,16 @@ static cudaError_t go_bp(const BackprojLaunch& p, cudaStream_t s, bool checked) 
     return launch_k(k_bp_ref<WX, WY, RX, RY, VC, PAD, MINB, OTF, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD, int MINB>
+static cudaError_t go_pipe(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    using Cfg = PipeCfg<WX, WY, RX, RY, VC, NB, PAD>;
+    const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
+    dim3 grid(tiles, p.nslices);
+    if (checked)
+        return launch_k(k_bp_ref_pipe<WX, WY, RX, RY, VC, NB, PAD, MINB, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    return launch_k(k_bp_ref_pipe<WX, WY, RX, RY, VC, NB, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
+}
+
 template <int WX, int WY, int RX, int RY, int VC, int MINB>
 static cudaError_t go_pair(const BackprojLaunch& p, cudaStream_t s, bool checked) {
     using Cfg = PairCfg<WX, WY, RX, RY, VC>;
@@ -674,6 +957,13 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 6: return go_bp<2, 4, 4, 4, 4, PAD, 4, 1>(p, s, checked);
     case 7: return go_bp<4, 4, 4, 8, 8, PAD, 1, 1>(p, s, checked);
     case 8: return go_bp<4, 4, 4, 4, 4, PAD, 2, 1>(p, s, checked);
+    case 9: return go_pipe<2, 4, 4, 4, 3, 3, PAD, 4>(p, s, checked);
+    case 10: return go_pipe<2, 4, 4, 4, 2, 4, PAD, 4>(p, s, checked);
+    case 11: return go_pipe<2, 4, 4, 4, 4, 2, PAD, 4>(p, s, checked);
+    case 12: return go_pipe<4, 4, 4, 8, 4, 3, PAD, 1>(p, s, checked);
+    case 13: return go_pipe<4, 4, 4, 4, 4, 2, PAD, 2>(p, s, checked);
+    case 14: return go_pipe<2, 4, 4, 4, 5, 2, PAD, 3>(p, s, checked);
+    case 15: return go_pipe<2, 4, 4, 4, 6, 2, PAD, 3>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -682,7 +972,8 @@ static cudaError_t dispatch_pair(const BackprojLaunch& p, cudaStream_t s, bool c
     switch (variant) {
     case 1: return go_pair<2, 4, 4, 8, 16, 2>(p, s, checked);
     case 2: case 4: case 5: case 8: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
-    case 3: case 6: return go_pair<2, 4, 4, 4, 8, 4>(p, s, checked);
+    case 3: case 6: case 9: case 10: case 11: case 14: case 15: return go_pair<2, 4, 4, 4, 8, 4>(p, s, checked);
+    case 13: return go_pair<4, 4, 4, 4, 16, 2>(p, s, checked);
     default: return go_pair<4, 4, 4, 8, 16, 1>(p, s, checked);
     }
 }
@@ -708,10 +999,29 @@ static cudaError_t go_persistent(const TileJob* jobs, int njobs, unsigned* count
     return cudaGetLastError();
 }
 
+template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD, int MINB>
+static cudaError_t go_pipe_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
+    using Cfg = PipeCfg<WX, WY, RX, RY, VC, NB, PAD>;
+    auto kern = k_bp_ref_pipe_persistent<WX, WY, RX, RY, VC, NB, PAD, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::NT, Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int grid = sms * per_sm;
+    if (grid > njobs) grid = njobs;
+    if (grid < 1) return cudaSuccess;
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(jobs, njobs, counter);
+    return cudaGetLastError();
+}
+
 static void persistent_shape(int variant, int* tx, int* ty) {
     switch (variant) {
-    case 0: case 2: case 7: *tx = 128; *ty = 128; break;
-    case 4: case 8: *tx = 128; *ty = 64; break;
+    case 0: case 2: case 7: case 12: *tx = 128; *ty = 128; break;
+    case 4: case 8: case 13: *tx = 128; *ty = 64; break;
     case 5: *tx = 64; *ty = 128; break;
     default: *tx = 64; *ty = 64; break;
     }
@@ -730,6 +1040,13 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 6: return go_persistent<2, 4, 4, 4, 4, PAD, 4, 1>(jobs, njobs, counter, s);
     case 7: return go_persistent<4, 4, 4, 8, 8, PAD, 1, 1>(jobs, njobs, counter, s);
     case 8: return go_persistent<4, 4, 4, 4, 4, PAD, 2, 1>(jobs, njobs, counter, s);
+    case 9: return go_pipe_persistent<2, 4, 4, 4, 3, 3, PAD, 4>(jobs, njobs, counter, s);
+    case 10: return go_pipe_persistent<2, 4, 4, 4, 2, 4, PAD, 4>(jobs, njobs, counter, s);
+    case 11: return go_pipe_persistent<2, 4, 4, 4, 4, 2, PAD, 4>(jobs, njobs, counter, s);
+    case 12: return go_pipe_persistent<4, 4, 4, 8, 4, 3, PAD, 1>(jobs, njobs, counter, s);
+    case 13: return go_pipe_persistent<4, 4, 4, 4, 4, 2, PAD, 2>(jobs, njobs, counter, s);
+    case 14: return go_pipe_persistent<2, 4, 4, 4, 5, 2, PAD, 3>(jobs, njobs, counter, s);
+    case 15: return go_pipe_persistent<2, 4, 4, 4, 6, 2, PAD, 3>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
 }
@@ -789,7 +1106,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 8 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 15 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;

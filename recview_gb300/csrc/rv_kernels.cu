@@ -507,6 +507,30 @@ __global__ void k_probe_f2i(int* sink, int iters) {
     for (int k = 0; k < 8; k++) s += acc[k];
     if (s == 123457) sink[0] = s;
 }
+// Conflict-free 32-bit shared-memory loads: each warp instruction reads 32 consecutive words
+// (one 128-byte wavefront); volatile asm keeps the loads in the loop.
+__global__ void k_probe_lds(int* sink, int iters) {
+    __shared__ int buf[8 * 1024];
+    for (int i = threadIdx.x; i < 8 * 1024; i += blockDim.x) buf[i] = i;
+    __syncthreads();
+    const unsigned base = static_cast<unsigned>(__cvta_generic_to_shared(buf)) + 4u * (threadIdx.x & 1023u);
+    int acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < iters; i++) {
+        int v[8];
+        asm volatile(
+            "ld.shared.s32 %0, [%8];\n ld.shared.s32 %1, [%8+4096];\n ld.shared.s32 %2, [%8+8192];\n"
+            " ld.shared.s32 %3, [%8+12288];\n ld.shared.s32 %4, [%8+16384];\n ld.shared.s32 %5, [%8+20480];\n"
+            " ld.shared.s32 %6, [%8+24576];\n ld.shared.s32 %7, [%8+28672];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+            : "r"(base));
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc[k] += v[k];
+    }
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += acc[k];
+    if (s == 123457) sink[0] = s;
+}
 }  // namespace rv
 
 extern "C" int RvProbeThroughput(double* out, int n) {
@@ -520,13 +544,14 @@ extern "C" int RvProbeThroughput(double* out, int n) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int blocks = sms * 4, threads = 512, iters = 4096;
-    double res[2] = {0, 0};
-    for (int which = 0; which < 2; which++) {
+    double res[3] = {0, 0, 0};
+    for (int which = 0; which < (n >= 3 ? 3 : 2); which++) {
         float best = 1e30f;
         for (int rep = 0; rep < 4; rep++) {
             cudaEventRecord(e0);
             if (which == 0) rv::k_probe_fma<<<blocks, threads>>>((float*)sink, iters);
-            else rv::k_probe_f2i<<<blocks, threads>>>((int*)sink, iters);
+            else if (which == 1) rv::k_probe_f2i<<<blocks, threads>>>((int*)sink, iters);
+            else rv::k_probe_lds<<<blocks, threads>>>((int*)sink, iters);
             cudaEventRecord(e1);
             cudaEventSynchronize(e1);
             float ms = 0;
@@ -534,12 +559,15 @@ extern "C" int RvProbeThroughput(double* out, int n) {
             if (rep > 0 && ms < best) best = ms;
         }
         const double ops = (double)blocks * threads * iters * 8;
-        res[which] = which == 0 ? 2.0 * ops / (best * 1e-3) / 1e12 : ops / (best * 1e-3) / 1e9;
+        if (which == 0) res[0] = 2.0 * ops / (best * 1e-3) / 1e12;   // FLOP/s
+        else if (which == 1) res[1] = ops / (best * 1e-3) / 1e9;       // conversions/s
+        else res[2] = 4.0 * ops / (best * 1e-3) / 1e9;                 // bytes/s of 32-bit loads
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(sink);
     out[0] = res[0];  // FP32 FMA TFLOP/s
     out[1] = res[1];  // float->int32 conversions, G/s
+    if (n >= 3) out[2] = res[2];  // shared-memory load bandwidth, GB/s (conflict-free 32-bit loads)
     return cudaGetLastError() == cudaSuccess ? 0 : RV_ERR_LAUNCH;
 }
