@@ -40,7 +40,7 @@ WORKLOAD = "fbp-2048det-1800views-64slices-raw-uint16"
 # DRAM bytes (read + write) per pixel-view update of k_bp_ref, from one ncu capture of the default
 # variant on 2 slices of this geometry (profiles/k_bp_ref_2048x1800x2.md); the traffic grows in
 # proportion to the slices processed, so a full launch moves this times its updates.
-BP_DRAM_BYTES_PER_UPDATE = 1.2609e-1
+BP_DRAM_BYTES_PER_UPDATE = 1.1223e-1
 
 
 def parse():

@@ -508,7 +508,8 @@ __global__ void k_probe_f2i(int* sink, int iters) {
     if (s == 123457) sink[0] = s;
 }
 // Conflict-free 32-bit shared-memory loads: each warp instruction reads 32 consecutive words
-// (one 128-byte wavefront); volatile asm keeps the loads in the loop.
+// (one 128-byte wavefront); ld.volatile keeps every load inside the loop (plain loads of an
+// unchanging address would be hoisted out of it).
 __global__ void k_probe_lds(int* sink, int iters) {
     __shared__ int buf[8 * 1024];
     for (int i = threadIdx.x; i < 8 * 1024; i += blockDim.x) buf[i] = i;
@@ -518,9 +519,10 @@ __global__ void k_probe_lds(int* sink, int iters) {
     for (int i = 0; i < iters; i++) {
         int v[8];
         asm volatile(
-            "ld.shared.s32 %0, [%8];\n ld.shared.s32 %1, [%8+4096];\n ld.shared.s32 %2, [%8+8192];\n"
-            " ld.shared.s32 %3, [%8+12288];\n ld.shared.s32 %4, [%8+16384];\n ld.shared.s32 %5, [%8+20480];\n"
-            " ld.shared.s32 %6, [%8+24576];\n ld.shared.s32 %7, [%8+28672];\n"
+            "ld.volatile.shared.s32 %0, [%8];\n ld.volatile.shared.s32 %1, [%8+4096];\n"
+            " ld.volatile.shared.s32 %2, [%8+8192];\n ld.volatile.shared.s32 %3, [%8+12288];\n"
+            " ld.volatile.shared.s32 %4, [%8+16384];\n ld.volatile.shared.s32 %5, [%8+20480];\n"
+            " ld.volatile.shared.s32 %6, [%8+24576];\n ld.volatile.shared.s32 %7, [%8+28672];\n"
             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
             : "r"(base));
 #pragma unroll
