@@ -83,15 +83,20 @@ void view_geometry(const Dims& d, double center, float fdeg, float tilt, float* 
 
 void fft_twiddles(int np, std::vector<float2>& out) {
     // CFft::Init1(np, -1) (source/cfft.cpp:374-410): angle a = -(float)2pi * (i/n) in float;
-    // cos/sin taken correctly rounded (the double result rounded to float).
-    const int n = 1 << np;
-    out.resize(n / 2);
+    // cos/sin taken correctly rounded (the double result rounded to float).  Stored per radix-2
+    // pass: pass l (2^l butterflies per group) reads w[q << (np-1-l)], q < 2^l, from
+    // out[2^l + q], so a warp's twiddle reads are consecutive addresses in every pass.
+    const int n = 1 << np, half = n / 2;
+    std::vector<float2> w(half);
     float p0 = (float)6.283185307178;
     p0 = p0 * -1.0f;
-    for (int i = 0; i < n / 2; i++) {
+    for (int i = 0; i < half; i++) {
         const float a = p0 * ((float)i / (float)n);
-        out[i] = make_float2((float)cos((double)a), (float)sin((double)a));
+        w[i] = make_float2((float)cos((double)a), (float)sin((double)a));
     }
+    out.assign(n, make_float2(1.0f, 0.0f));
+    for (int l = 1; l < np; l++)
+        for (int q = 0; q < (1 << l); q++) out[(1 << l) + q] = w[(size_t)q << (np - 1 - l)];
 }
 
 // ---------------------------------------------------------------------------- context -------

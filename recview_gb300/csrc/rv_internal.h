@@ -28,7 +28,8 @@ Dims make_dims(int ixdim, int iInterpolation);
 float fcenter_of(const Dims& d, double center);
 void view_geometry(const Dims& d, double center, float fdeg, float tilt, float* fcos, float* fsin,
                    float* foffset);
-// twiddles of CFft::Init1(np, -1), correctly rounded (float2 per entry, n/2 entries)
+// twiddles of CFft::Init1(np, -1), correctly rounded, laid out per radix-2 pass: entry 2^l + q
+// holds w[q << (np-1-l)] (n entries; 0 and 1 unused)
 void fft_twiddles(int np, std::vector<float2>& out);
 
 // limits of the on-chip FFT and of the back-projection tile windows
@@ -56,7 +57,7 @@ struct FilterLaunch {
     const RowJob* jobs;       // device array
     int njobs;
     const float* filt;        // device, ndim
-    const float2* tw;         // device, ndim/2
+    const float2* tw;         // device, ndim entries: pass l's twiddle q at [2^l + q]
     int* table;               // REF output: int table, 16*ixdimp ints per slot (may be null)
     float* rows;              // LIN output: filtered rows x BACKPROJ_SCALE (may be null)
     void* rows16;             // LIN_F16/BF16 output: half/bf16 rows (may be null)

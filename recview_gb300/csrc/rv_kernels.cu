@@ -81,22 +81,23 @@ cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
 
 // ---------------------------------------------------------------------------------------------
 // R5+R6+R7: filter one row per CTA.  Shared memory: buf[n] complex (in-place radix-2 passes with
-// a register hand-off between read and write phases), tw[n/2], strip[ixdim] shorts.
+// a register hand-off between read and write phases) and strip[ixdim] shorts; the twiddles come
+// from a per-pass table in global memory (pass l reads tw[2^l + q], consecutive per warp, so the
+// reads neither conflict nor leave L1).
 // The pass structure is the reference's Stockham FFT (source/cfft.cpp:193-369): pass l reads
 // x[j] and x[j + n/2] for butterfly j and writes y[2j - q], y[2j - q + al], q = j mod al.
 // ---------------------------------------------------------------------------------------------
 template <int BPT>
-__global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
+__global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_filter(FilterLaunch p) {
     extern __shared__ __align__(16) float2 sm[];
     const int n = p.d.ndim, half = n >> 1, np = p.d.ndimp;
     float2* buf = sm;
-    float2* tw = sm + n;
-    short* strip = reinterpret_cast<short*>(tw + half);
+    const float2* __restrict__ tw = p.tw;   // per-pass table: pass l reads tw[2^l + q]
+    short* strip = reinterpret_cast<short*>(sm + n);
     const int tid = threadIdx.x, NT = blockDim.x;
     const RowJob job = p.jobs[blockIdx.x];
     const int W = p.d.ixdim;
 
-    for (int i = tid; i < half; i += NT) tw[i] = p.tw[i];
     // ---- sinogram row (R1 on the fly for raw frames) -------------------------------------------
     if (p.raw) {
         const uint16_t* base = static_cast<const uint16_t*>(p.src);
@@ -148,12 +149,12 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
     }
     __syncthreads();
     for (int l = 1; l < np - 1; l++) {
-        const int al = 1 << l, mask = al - 1, sh = np - 1 - l;  // bt = half >> l = 1 << sh
+        const int al = 1 << l, mask = al - 1;
 #pragma unroll
         for (int i = 0; i < BPT; i++) {
             const int j = tid + i * NT;
             a[i] = buf[j];
-            b[i] = cmul(buf[j + half], tw[(j & mask) << sh]);
+            b[i] = cmul(buf[j + half], __ldg(tw + al + (j & mask)));
         }
         __syncthreads();
 #pragma unroll
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
         a[i] = buf[j];
-        b[i] = (j == 0) ? buf[j + half] : cmul(buf[j + half], tw[j]);
+        b[i] = (j == 0) ? buf[j + half] : cmul(buf[j + half], __ldg(tw + half + j));
     }
     __syncthreads();
 #pragma unroll
@@ -201,12 +202,12 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
     }
     __syncthreads();
     for (int l = 1; l < np - 1; l++) {
-        const int al = 1 << l, mask = al - 1, sh = np - 1 - l;
+        const int al = 1 << l, mask = al - 1;
 #pragma unroll
         for (int i = 0; i < BPT; i++) {
             const int j = tid + i * NT;
             a[i] = buf[j];
-            b[i] = cmul(buf[j + half], tw[(j & mask) << sh]);
+            b[i] = cmul(buf[j + half], __ldg(tw + al + (j & mask)));
         }
         __syncthreads();
 #pragma unroll
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(512) k_filter(FilterLaunch p) {
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
         a[i] = buf[j];
-        b[i] = cmul(buf[j + half], tw[j]);
+        b[i] = cmul(buf[j + half], __ldg(tw + half + j));
     }
     __syncthreads();
 #pragma unroll
@@ -312,7 +313,7 @@ cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {
     const int n = p.d.ndim, half = n / 2;
     const int nt = half < 512 ? half : 512;
     const int bpt = half / nt;
-    const size_t smem = (size_t)n * sizeof(float2) + (size_t)half * sizeof(float2) +
+    const size_t smem = (size_t)n * sizeof(float2) +
                         (((size_t)p.d.ixdim * sizeof(short) + 15) & ~(size_t)15);
     cudaError_t e = cudaSuccess;
     auto go = [&](auto kern) {

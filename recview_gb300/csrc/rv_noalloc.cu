@@ -73,7 +73,7 @@ extern "C" int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ix
     const long long tstride = ref_table_stride(d.ixdimp, pad);
     // scratch layout: twiddles | filter | row jobs | geometry | tables
     const size_t o_tw = 0;
-    const size_t o_filt = align256(o_tw + (size_t)(d.ndim / 2) * sizeof(float2));
+    const size_t o_filt = align256(o_tw + (size_t)d.ndim * sizeof(float2));   // per-pass twiddle table
     const size_t o_jobs = align256(o_filt + (size_t)d.ndim * sizeof(float));
     const size_t o_geom = align256(o_jobs + (size_t)nviews * sizeof(RowJob));
     const size_t o_tab = align256(o_geom + (size_t)nviews * sizeof(float4));
