@@ -356,8 +356,10 @@ int RvGetAxis(const unsigned short* sample0, const unsigned short* sample1, cons
 
 /* R11: the axis-scan sweep (source/gazoDoc.cpp:1994-2024) with a score: one slice (nviews
  * log-normalised int16 rows of ixdim, host) reconstructed at ncent trial centres (ri->center
- * convention), scores[i] = total variation of trial i inside the circle r < 0.45 ixdimp (this
- * library's criterion: lowest = sharpest; the reference leaves the choice to a person), and
+ * convention), scores[i] = total variation of trial i, averaged over b x b pixel boxes
+ * (b = max(1, ixdimp / 512)), inside the circle r < 0.45 of its width (this library's criterion:
+ * lowest = sharpest; the reference leaves the choice to a person; use a smoothing filter such as
+ * Hann with cutoff 0.25 for noisy data), and
  * best_centre = a parabola through the lowest score and its neighbours (equal steps). */
 int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInterpolation, const float* fdeg,
                   float fTiltAngle, const float* fFilter, const double* centres, int ncent,
@@ -422,6 +424,70 @@ int RvOffsetCtStitchDevice(const RvOffsetCtDesc* desc, const short* d_sino, shor
 /* The reference's host form: iSinogr[i*iMultiplex + j] rows in, ofSinogr[i*iMultiplex + j] rows
  * (width samples each, i < nof) out; synchronous.  Same return codes. */
 int RvOffsetCtStitchHost(const RvOffsetCtDesc* desc, short* const* iSinogr, short* const* ofSinogr);
+
+/* ---- learned centre proposal (no reference counterpart; RecView leaves the centre choice to a
+ * person looking at an axis-scan sweep, source/gazoDoc.cpp:1994-2024) ---------------------------
+ * A small BF16 CNN (6 x {conv 3x3 + ReLU + 2x2 average pool}, channels 4-32-32-64-64-128-128, then
+ * FC 128 + ReLU, FC 2) maps four detector rows of a sinogram, prepared by RvCentreNetInput, to
+ * (mu, s): the centre offset estimate and the log-variance of its error.  Trained on the device
+ * with its own forward/backward kernels and Adam.  Parameters are one FP32 vector in the order
+ * w0 b0 w1 b1 ... w5 b5 f0w f0b f1w f1b (conv weights [cout][cin][3][3], FC weights [out][in]).
+ * Inputs are device bf16 tensors [n][4][H][W]; H and W are multiples of 64. */
+typedef struct RvCentreNet RvCentreNet;
+int RvCentreNetCreate(int H, int W, int batch, unsigned long long seed, RvCentreNet** out);
+void RvCentreNetDestroy(RvCentreNet* net);
+long long RvCentreNetNumParams(const RvCentreNet* net);
+int RvCentreNetSetParams(RvCentreNet* net, const float* host_params);   /* also resets Adam */
+int RvCentreNetGetParams(const RvCentreNet* net, float* host_params);
+/* (mu, s) of count samples (host arrays of count; either may be NULL); synchronous. */
+int RvCentreNetForward(RvCentreNet* net, const void* d_x, int count, float* mu, float* s, void* stream);
+/* Mean Gaussian NLL 0.5 e^-s (y - mu)^2 + 0.5 s over the batch and its parameter gradients
+ * (host, RvCentreNetNumParams floats; may be NULL); no update.  y on the host. */
+int RvCentreNetGradients(RvCentreNet* net, const void* d_x, const float* y, int count, float* loss,
+                         float* grads_host, void* stream);
+/* One Adam step (0.9, 0.999, 1e-8) at learning rate lr; d_y on the device; *loss (may be NULL)
+ * receives the batch loss before the step (synchronising when requested). */
+int RvCentreNetTrainStep(RvCentreNet* net, const void* d_x, const float* d_y, int count, float lr, float* loss,
+                         void* stream);
+/* Synthetic raw frames for training and evaluating the centre search (no reference counterpart):
+ * a seeded ellipsoid phantom (n_ellipsoids, centres in a ball of radius 0.8, semi-axes
+ * U[0.05, 0.4], attenuation U[-0.2, 1.0]), flat 20000 (1 + 0.02 smooth), dark ~ N(100, 3),
+ * Poisson-like noise, rotation centre `center` (ri->center convention).  d_raw (device) receives
+ * [(nviews + 3)][S][W] uint16: frame 0 flat, frames 1..nviews samples at view_deg, frame
+ * nviews + 1 flat, the dark frame last; bInc/fdeg/fexp (host, nviews + 2 each, may be NULL) the
+ * frame table.  Synchronous. */
+int RvPhantomFrames(unsigned long long seed, int W, int S, const float* view_deg, int nviews, double center,
+                    int n_ellipsoids, void* d_raw, char* bInc, float* fdeg, float* fexp, void* stream);
+/* R1 on a device-resident raw stack (the normalisation of CudaSinogramHost, all SAMPLE frames):
+ * d_sino [(nframes + 1)][nslices][ixdim] int16, other rows zero.  Uses desc's ixdim, nframes,
+ * nslices, bInc, fexp, dReconFlags (Zernike) and iFlag.  Synchronous. */
+int RvNormaliseStack(const RvStackDesc* desc, const void* d_raw, short* d_sino, void* stream);
+/* The network input [4][256][512] bf16 (device) from normalised rows d_sino [frames][S][W]
+ * (W a multiple of 512): detector rows s0..s0+3, the 256 frames listed (in angle order over the
+ * half-turn), W/512 samples averaged per bin, values / 3000, rows 0..127 = frames[128..255] as
+ * measured, rows 128..255 = frames[0..127] mirrored about the detector centre (so the two ends of
+ * the half-turn meet in the middle row, where the centre offset shows as a horizontal shift).
+ * Synchronous. */
+int RvCentreNetInput(const short* d_sino, int S, int W, const int* frames256, int s0, void* d_x, void* stream);
+/* Centre search (row (f2)): the plain sweep on the grid grid_centre + step*k, k = -half_range..
+ * half_range (RvCentreSweep's criterion on detector row s_sweep of d_sino [nframes][S][W], the
+ * SAMPLE frames of bInc at fdeg), narrowed by the network when net is not NULL: the network reads
+ * rows s_net..s_net+3 (RvCentreNetInput, the proposal is (W-1)/2 + 16 mu with uncertainty
+ * 16 e^(s/2) pixels) and only the 2*window+1 grid trials around the proposal are reconstructed.
+ * The full sweep runs instead when the uncertainty exceeds sigma_max or the lowest score of the
+ * window lies on its edge.  centre = the sweep criterion's choice (parabola-refined). */
+typedef struct RvCentreSearchResult {
+    double centre;     /* chosen centre (ri->center convention) */
+    double proposal;   /* network proposal (NaN without a network) */
+    double sigma;      /* network's uncertainty in pixels (NaN without a network) */
+    int trials;        /* trial reconstructions run */
+    int fallback;      /* 1: the full sweep ran */
+    double ms;         /* wall time of the search */
+} RvCentreSearchResult;
+int RvCentreSearch(RvCentreNet* net, const short* d_sino, int S, int W, int nframes, const char* bInc,
+                   const float* fdeg, int s_net, int s_sweep, const float* fFilter, double grid_centre,
+                   int half_range, double step, int window, double sigma_max, RvCentreSearchResult* out,
+                   void* stream);
 
 #ifdef __cplusplus
 }

@@ -80,7 +80,8 @@ int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out);
  * overall SSD centre. */
 int rvo_get_axis(const unsigned short* s0, const unsigned short* s1, const unsigned short* flat,
                  int ixdim, int iydim, int iAxisOffset, double* pCenter, double* pGrad, double* pOverall);
-/* Project-defined centre-sweep score: total variation inside the circle r < 0.45 ixdimp. */
+/* Project-defined centre-sweep score: total variation inside the circle r < 0.45 n of the slice
+ * averaged over b x b boxes, b = max(1, ixdimp / 512), n = ixdimp / b. */
 double rvo_tv_score(const int* slice, int ixdimp);
 
 /* Offset-CT (360-degree scan, axis near a detector edge): GetSinogramYdim(TRUE)

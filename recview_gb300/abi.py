@@ -124,6 +124,17 @@ class RvOffsetCtDesc(C.Structure):
     ]
 
 
+class RvCentreSearchResult(C.Structure):
+    _fields_ = [
+        ("centre", C.c_double),
+        ("proposal", C.c_double),
+        ("sigma", C.c_double),
+        ("trials", C.c_int),
+        ("fallback", C.c_int),
+        ("ms", C.c_double),
+    ]
+
+
 # constants (include/recview_gb300.h)
 LOG_SCALE = 3000
 BACKPROJ_SCALE = 100
@@ -228,6 +239,23 @@ PROTOTYPES = {
     "RvOffsetCtReconCenter": (C.c_double, [C.POINTER(RvOffsetCtDesc), C.c_double]),
     "RvOffsetCtStitchDevice": (C.c_int, [C.POINTER(RvOffsetCtDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "RvOffsetCtStitchHost": (C.c_int, [C.POINTER(RvOffsetCtDesc), C.c_void_p, C.c_void_p]),
+    "RvCentreNetCreate": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "RvCentreNetDestroy": (None, [C.c_void_p]),
+    "RvCentreNetNumParams": (C.c_longlong, [C.c_void_p]),
+    "RvCentreNetSetParams": (C.c_int, [C.c_void_p, c_float_p]),
+    "RvCentreNetGetParams": (C.c_int, [C.c_void_p, c_float_p]),
+    "RvCentreNetForward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, c_float_p, c_float_p, C.c_void_p]),
+    "RvCentreNetGradients": (C.c_int, [C.c_void_p, C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p,
+                                       C.c_void_p]),
+    "RvCentreNetTrainStep": (C.c_int, [C.c_void_p, C.c_void_p, c_float_p, C.c_int, C.c_float, c_float_p,
+                                       C.c_void_p]),
+    "RvPhantomFrames": (C.c_int, [C.c_ulonglong, C.c_int, C.c_int, c_float_p, C.c_int, C.c_double, C.c_int,
+                                  C.c_void_p, C.c_void_p, c_float_p, c_float_p, C.c_void_p]),
+    "RvNormaliseStack": (C.c_int, [C.POINTER(RvStackDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "RvCentreNetInput": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_int_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "RvCentreSearch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, c_float_p, C.c_int,
+                                 C.c_int, c_float_p, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double,
+                                 C.POINTER(RvCentreSearchResult), C.c_void_p]),
 }
 
 

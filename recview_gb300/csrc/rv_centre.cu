@@ -10,9 +10,11 @@
 //                 double/float arithmetic.
 //  RvCentreSweep  the axis-scan batch (source/gazoDoc.cpp:1994-2024) -- one slice reconstructed at
 //                 many trial centres -- plus a score the reference does not have (it writes one TIFF
-//                 per centre and leaves the choice to a person): the total variation of each slice
-//                 inside the reconstruction circle, lowest = sharpest (project-defined), with a
-//                 parabola through the best three trials.
+//                 per centre and leaves the choice to a person): the total variation of each slice,
+//                 box-averaged to about 512 x 512 values, inside the reconstruction circle, lowest =
+//                 sharpest (project-defined), with a parabola through the best three trials.  Run
+//                 with a smoothing filter (e.g. Hann, cutoff 0.25) the criterion is unimodal over
+//                 tens of pixels on noisy full-size data.
 #include <cuda_runtime.h>
 #include <limits.h>
 #include <math.h>
@@ -75,20 +77,30 @@ __global__ void k_axis_ssd(const int* S0, const int* S1, int ixdim, int istep, i
     nd[(size_t)row * 2 * ixdimh + js + ixdimh] = n;
 }
 
-// Total variation per slice inside the circle r < 0.45 ixdimp, deterministic two-level sum.
+// Total variation per slice inside the circle r < 0.45 n of the slice averaged over b x b pixel
+// boxes, b = max(1, ixdimp / 512) and n = ixdimp / b (about 512 x 512 values whatever the slice
+// size, so reconstruction noise does not swamp the edges); deterministic two-level sum.
+__device__ __forceinline__ double tv_box(const int* f, int ixdimp, int b, int X, int Y) {
+    long long s = 0;
+    for (int j = 0; j < b; j++)
+        for (int i = 0; i < b; i++) s += f[(size_t)(Y * b + j) * ixdimp + X * b + i];
+    return (double)s / (double)(b * b);
+}
 __global__ void k_tv_partial(const int* slices, int ixdimp, double* partial) {
     const int slice = blockIdx.y;
     const int* f = slices + (size_t)slice * ixdimp * ixdimp;
-    const double h = ixdimp / 2.0, r2 = (0.45 * ixdimp) * (0.45 * ixdimp);
+    const int b = ixdimp / 512 > 1 ? ixdimp / 512 : 1;
+    const int nb = ixdimp / b;
+    const double h = nb / 2.0, r2 = (0.45 * nb) * (0.45 * nb);
     double acc = 0.0;
-    const long long n = (long long)(ixdimp - 1) * (ixdimp - 1);
+    const long long n = (long long)(nb - 1) * (nb - 1);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int y = (int)(i / (ixdimp - 1)), x = (int)(i % (ixdimp - 1));
+        const int y = (int)(i / (nb - 1)), x = (int)(i % (nb - 1));
         const double dx = x - h, dy = y - h;
         if (dx * dx + dy * dy >= r2) continue;
-        const double v = f[(size_t)y * ixdimp + x];
-        const double gx = f[(size_t)y * ixdimp + x + 1] - v;
-        const double gy = f[(size_t)(y + 1) * ixdimp + x] - v;
+        const double v = tv_box(f, ixdimp, b, x, y);
+        const double gx = tv_box(f, ixdimp, b, x + 1, y) - v;
+        const double gy = tv_box(f, ixdimp, b, x, y + 1) - v;
         acc += sqrt(gx * gx + gy * gy);
     }
     __shared__ double red[32];
