@@ -53,7 +53,17 @@ def parse():
     ap.add_argument("--mode", default="ref", choices=["ref", "lin", "f16", "bf16"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-centre", action="store_true", help="skip the centre-search summary of the default run")
     ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--workload", default="fbp", choices=["fbp", "centre"],
+                    help="fbp: the back-projection stack (default); centre: train the centre-proposal network "
+                         "and compare the learned search with the full sweep")
+    ap.add_argument("--datasets", type=int, default=200, help="centre: evaluation datasets")
+    ap.add_argument("--train", type=int, default=20000, help="centre: training scans")
+    ap.add_argument("--epochs", type=int, default=10, help="centre: training epochs")
+    ap.add_argument("--finetune", type=int, default=64, help="centre: scans labelled by the full sweep")
+    ap.add_argument("--net", default=None, help="centre: load network parameters instead of training")
+    ap.add_argument("--save-net", default=None, help="centre: write the trained parameters (float32)")
     return ap.parse_args()
 
 
@@ -371,12 +381,121 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             line["cpu_baseline"] = {"value": tau_cpu, "unit": "ns/(pixel*view)", "cores": threads, "kind": "port",
                                     "sample": "1 of 64 slices (2048^2 x 1800 views, normalisation + FBP), "
                                               "reference multi-worker scheme", "seconds": tcpu}
+        if not args.no_centre and world == 1 and NET_FILE.exists():
+            # the centre-search part of the metric: the shipped network on fresh scans (C5 shapes)
+            from recview_gb300 import centre as cs
+            net = cs.CentreNet(batch=1)
+            net.set_params(np.fromfile(NET_FILE, dtype=np.float32))
+            summ = centre_evaluate(net, 8, np.random.default_rng(args.seed + 1))
+            net.close()
+            summ.pop("disagreements", None)
+            line["centre_search"] = {"metric": "centre_search_s", "unit": "s/dataset", "value": summ.pop("learned_s"),
+                                     "network": str(NET_FILE.relative_to(ROOT)), **summ}
         print(json.dumps(line), flush=True)
     st.close()
 
 
+NET_FILE = ROOT / "recview_gb300" / "data" / "centre_net_256x512.f32"
+
+
+def centre_evaluate(net, n: int, rng) -> dict:
+    """Learned search vs the full sweep on n fresh synthetic scans (2048 x 1800, offset U[-40, 40])."""
+    from recview_gb300 import centre as cs
+    F = cs.sweep_filter(W_DET)
+    res = []
+    for j in range(n):
+        scan = cs.make_scan(9_000_000 + j, float(rng.uniform(-40, 40)), W_DET, N_VIEWS)
+        t0 = time.perf_counter()
+        grid = cs.getaxis_grid_centre(scan)
+        t_axis = time.perf_counter() - t0
+        rl = cs.search(net.h, scan, grid, F)
+        rf = cs.search(None, scan, grid, F)
+        res.append(dict(true=scan.centre, grid=grid, learned=rl.centre, full=rf.centre, trials=rl.trials,
+                        fallback=rl.fallback, ms_l=rl.ms, ms_f=rf.ms, axis_ms=t_axis * 1e3, sigma=rl.sigma,
+                        proposal=rl.proposal))
+        del scan
+    ms_l = float(np.mean([r["ms_l"] for r in res]))
+    ms_f = float(np.mean([r["ms_f"] for r in res]))
+    dis = [r for r in res if abs(r["learned"] - r["full"]) > 0.25]
+    return {
+        "learned_s": ms_l / 1e3, "full_sweep_s": ms_f / 1e3, "speedup": ms_f / ms_l,
+        "agreement_0p25px": 1.0 - len(dis) / len(res), "datasets": len(res),
+        "mean_trials": float(np.mean([r["trials"] for r in res])), "full_trials": 81,
+        "fallbacks": int(np.sum([r["fallback"] for r in res])),
+        "full_vs_true_px": {"p50": float(np.median([abs(r["full"] - r["true"]) for r in res])),
+                            "max": float(max(abs(r["full"] - r["true"]) for r in res))},
+        "proposal_err_px": {"p50": float(np.median([abs(r["proposal"] - r["true"]) for r in res])),
+                            "max": float(max(abs(r["proposal"] - r["true"]) for r in res))},
+        "getaxis_ms": float(np.mean([r["axis_ms"] for r in res])),
+        "disagreements": [{k: round(float(v), 3) for k, v in r.items()} for r in dis[:8]],
+        "criterion": "total variation of the 4x4-box-averaged trial slice (Hann 0.25 filter) inside r < 0.45",
+        "grid": "81 trials, 0.5 px apart, centred on GetAxis",
+    }
+
+
+def run_centre(args):
+    """Learned centre search vs the plain full sweep (configuration C5 shapes: 2048-pixel detector,
+    1800 views, uint16 Poisson raw frames, true offset U[-40, 40] px)."""
+    import torch
+    from recview_gb300 import abi
+    from recview_gb300 import centre as cs
+    from recview_gb300.build import build_lib
+    build_lib()
+    torch.cuda.set_device(0)
+    W = W_DET
+    rng = np.random.default_rng(args.seed)
+    net = cs.CentreNet(batch=32)
+    train = {}
+    if args.net:
+        net.set_params(np.fromfile(args.net, dtype=np.float32))
+        train["source"] = args.net
+    else:
+        nval = max(256, args.train // 16)
+        desc = abi.RvCentreTrainDesc(W=W, views=N_VIEWS, slices=4, n_ellipsoids=40, max_offset=40.0, seed=args.seed)
+        t0 = time.perf_counter()
+        X, Y = cs.make_samples(desc, 0, args.train + nval)
+        train["generate_s"] = time.perf_counter() - t0
+        st = cs.fit(net, X, Y, args.train, nval, args.epochs)
+        train.update(samples=args.train, held_out=nval, epochs=args.epochs, fit_s=float(st[3]),
+                     held_out_err_px={"p50": float(st[0]), "p90": float(st[1]), "p99": float(st[2])})
+        if args.finetune:
+            # the plain sweep's own optima as targets, mixed with as many generated samples
+            F = cs.sweep_filter(W)
+            t0 = time.perf_counter()
+            xs, ys = [], []
+            for j in range(args.finetune):
+                scan = cs.make_scan(5_000_000 + j, float(rng.uniform(-40, 40)), W, N_VIEWS)
+                r = cs.search(None, scan, cs.getaxis_grid_centre(scan), F)
+                xs.append(cs.scan_input(scan))
+                ys.append((r.centre - (W - 1) / 2.0) / 16.0)
+                del scan
+            m = len(xs)
+            Xf = torch.cat(xs + [X[:m]], 0).contiguous()
+            Yf = torch.cat([torch.tensor(ys, dtype=torch.float32, device="cuda"), Y[:m]], 0).contiguous()
+            cs.fit(net, Xf, Yf, 2 * m, 0, 4, lr_max=1e-4, lr_min=1e-5)
+            train["finetune_scans"] = m
+            train["finetune_s"] = time.perf_counter() - t0
+            del Xf, Yf
+        del X, Y
+        torch.cuda.empty_cache()
+        if args.save_net:
+            net.get_params().tofile(args.save_net)
+    line = {"metric": "centre_search_s", "unit": "s/dataset", "higher_is_better": False, "n_gpus": 1,
+            "workload": "centre-search-2048det-1800views-offset-40px",
+            "data": "synthetic (seeded ellipsoid phantom, Poisson uint16 frames, true centre offset U[-40, 40] px)"}
+    summ = centre_evaluate(net, args.datasets, rng)
+    line["value"] = summ.pop("learned_s")
+    line.update(summ)
+    line["train"] = train
+    print(json.dumps(line), flush=True)
+    net.close()
+
+
 def main():
     args = parse()
+    if args.workload == "centre":
+        run_centre(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -469,6 +469,28 @@ int RvNormaliseStack(const RvStackDesc* desc, const void* d_raw, short* d_sino, 
  * the half-turn meet in the middle row, where the centre offset shows as a horizontal shift).
  * Synchronous. */
 int RvCentreNetInput(const short* d_sino, int S, int W, const int* frames256, int s0, void* d_x, void* stream);
+/* Synthetic training data made by the plain method: scans of a seeded phantom with the centre
+ * (W-1)/2 + U[-max_offset, max_offset], the reference's normalisation, then RvCentreNetInput on
+ * the 256 views of a `views`-view half-turn the network reads.  Sample i of a description is
+ * always the same scan (seeded by seed and i). */
+typedef struct RvCentreTrainDesc {
+    int W;                   /* detector width, a multiple of 512 */
+    int views;               /* views over 180 degrees of the simulated scans (>= 256) */
+    int slices;              /* detector rows per scan (>= 4; rows 0..3 feed the network) */
+    int n_ellipsoids;
+    double max_offset;       /* pixels */
+    unsigned long long seed;
+} RvCentreTrainDesc;
+/* Samples first..first+count-1 into d_x ([count][4][256][512] bf16, device) and their targets
+ * offset/16 into d_y (device).  Synchronous. */
+int RvCentreNetMakeSamples(const RvCentreTrainDesc* desc, int first, int count, void* d_x, float* d_y,
+                           void* stream);
+/* Adam on samples [0, ntrain) of d_x/d_y for `epochs` shuffled passes in batches of `batch`
+ * (<= the network's batch), learning rate from lr_max to lr_min on a cosine; samples
+ * [ntrain, ntrain + nval) are held out.  stats (may be NULL) receives the held-out |error| of the
+ * proposal in pixels at the 50th / 90th / 99th percentile and the wall time in seconds. */
+int RvCentreNetFit(RvCentreNet* net, const void* d_x, const float* d_y, int ntrain, int nval, int epochs, int batch,
+                   float lr_max, float lr_min, unsigned long long seed, float* stats, void* stream);
 /* Centre search (row (f2)): the plain sweep on the grid grid_centre + step*k, k = -half_range..
  * half_range (RvCentreSweep's criterion on detector row s_sweep of d_sino [nframes][S][W], the
  * SAMPLE frames of bInc at fdeg), narrowed by the network when net is not NULL: the network reads

@@ -124,6 +124,17 @@ class RvOffsetCtDesc(C.Structure):
     ]
 
 
+class RvCentreTrainDesc(C.Structure):
+    _fields_ = [
+        ("W", C.c_int),
+        ("views", C.c_int),
+        ("slices", C.c_int),
+        ("n_ellipsoids", C.c_int),
+        ("max_offset", C.c_double),
+        ("seed", C.c_ulonglong),
+    ]
+
+
 class RvCentreSearchResult(C.Structure):
     _fields_ = [
         ("centre", C.c_double),
@@ -253,6 +264,10 @@ PROTOTYPES = {
                                   C.c_void_p, C.c_void_p, c_float_p, c_float_p, C.c_void_p]),
     "RvNormaliseStack": (C.c_int, [C.POINTER(RvStackDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "RvCentreNetInput": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_int_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "RvCentreNetMakeSamples": (C.c_int, [C.POINTER(RvCentreTrainDesc), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]),
+    "RvCentreNetFit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                 C.c_float, C.c_ulonglong, c_float_p, C.c_void_p]),
     "RvCentreSearch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, c_float_p, C.c_int,
                                  C.c_int, c_float_p, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double,
                                  C.POINTER(RvCentreSearchResult), C.c_void_p]),
