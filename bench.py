@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-centre", action="store_true", help="skip the centre-search summary of the default run")
+    ap.add_argument("--no-forms", action="store_true", help="skip the reduced-storage and queue summaries")
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--workload", default="fbp", choices=["fbp", "centre"],
                     help="fbp: the back-projection stack (default); centre: train the centre-proposal network "
@@ -381,6 +382,9 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             line["cpu_baseline"] = {"value": tau_cpu, "unit": "ns/(pixel*view)", "cores": threads, "kind": "port",
                                     "sample": "1 of 64 slices (2048^2 x 1800 views, normalisation + FBP), "
                                               "reference multi-worker scheme", "seconds": tcpu}
+        if not args.no_forms and world == 1 and mode == abi.MODE_REF:
+            line["forms"] = forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev)
+            line["queue"] = queue_summary(dev, args.seed)
         if not args.no_centre and world == 1 and NET_FILE.exists():
             # the centre-search part of the metric: the shipped network on fresh scans (C5 shapes)
             from recview_gb300 import centre as cs
@@ -393,6 +397,98 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                      "network": str(NET_FILE.relative_to(ROOT)), **summ}
         print(json.dumps(line), flush=True)
     st.close()
+
+
+def forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, steps: int = 3) -> dict:
+    """The reduced-storage forms on the same stack: filtered rows stored as FP32 / FP16 / BF16
+    (per-row scale), linear interpolation and FP32 accumulation (their FP64-oracle errors are
+    asserted in tests/test_gpu_parity.py::test_stack_lin_modes_vs_fp64)."""
+    import torch
+    import recview_gb300 as rv
+    from recview_gb300 import abi
+    out = {}
+    for name, mode in (("lin_fp32", abi.MODE_LIN), ("lin_fp16", abi.MODE_LIN_F16), ("lin_bf16", abi.MODE_LIN_BF16)):
+        st = rv.Stack(ixdim=W_DET, nframes=raw.shape[0] - 1, nslices=S, center=center, bInc=bInc, fdeg=fdeg,
+                      fexp=fexp, fFilter=F, mode=mode)
+        o = torch.empty((S, st.ixdimp, st.ixdimp), dtype=torch.float32, device=dev)
+        st.run_device(raw.data_ptr(), o.data_ptr())
+        tt, tb = [], []
+        for _ in range(steps):
+            st.run_device(raw.data_ptr(), o.data_ptr())
+            tf_, tb_, tt_ = st.timings()
+            tt.append(tt_)
+            tb.append(tb_)
+        ms = float(np.mean(tt))
+        out[name] = {"tau_ns": ms * 1e6 / (float(st.ixdimp) ** 2 * st.nviews * S), "ms_per_step": ms,
+                     "backprojection_ms": float(np.mean(tb))}
+        st.close()
+        del o
+    return out
+
+
+def queue_summary(dev, seed: int) -> dict:
+    """An uneven queue (configuration C3 shapes, scaled to seconds): widths 512-4096, 900/1800
+    views, 1-8 slices, zoom x1/x2/x4 ROIs, run as one persistent kernel per wave in a captured graph,
+    against the same datasets one stack at a time."""
+    import torch
+    import recview_gb300 as rv
+    from recview_gb300 import abi
+    L = rv.lib()
+    rng = np.random.default_rng(seed)
+    shapes = [(1024, 900, 8, 2), (1536, 1800, 4, 2), (2048, 1800, 4, 2), (4096, 900, 2, 2), (1024, 900, 4, 3),
+              (512, 1800, 4, 4)]
+    data = []
+    for i, (W, V, S, interp) in enumerate(shapes):
+        deg = (np.arange(V) * (180.0 / V)).astype(np.float32)
+        raw = torch.empty((V + 3, S, W), dtype=torch.int16, device=dev)
+        binc = np.zeros(V + 2, np.int8)
+        fdeg = np.zeros(V + 2, np.float32)
+        fexp = np.zeros(V + 2, np.float32)
+        cen = (W - 1) / 2.0 + float(rng.uniform(-20, 20)) / (2 ** (interp - 2))
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+        assert L.RvPhantomFrames(700 + i, W, S, fp(deg), V, cen, 40, C.c_void_p(raw.data_ptr()),
+                                 C.c_void_p(binc.ctypes.data), fp(fdeg), fp(fexp), None) == 0
+        F = rv.set_filter(abi.FILT_SHEPP, rv.dims(W, interp).ndim)
+        n = rv.dims(W, interp).ixdimp
+        out = torch.empty((S, n, n), dtype=torch.int32, device=dev)
+        data.append((W, V, S, interp, cen, raw, binc, fdeg, fexp, F, out))
+    q = C.c_void_p()
+    assert L.RvQueueCreate(C.byref(q)) == 0
+    keep = []
+    for (W, V, S, interp, cen, raw, binc, fdeg, fexp, F, out) in data:
+        d = abi.RvStackDesc()
+        d.ixdim, d.iInterpolation, d.center, d.nframes, d.nslices = W, interp, cen, V + 2, S
+        d.bInc = C.cast(C.c_void_p(binc.ctypes.data), C.POINTER(C.c_char))
+        d.fdeg = fdeg.ctypes.data_as(C.POINTER(C.c_float))
+        d.fexp = fexp.ctypes.data_as(C.POINTER(C.c_float))
+        d.fFilter = F.ctypes.data_as(C.POINTER(C.c_float))
+        d.mode = abi.MODE_REF
+        keep.append(d)
+        assert L.RvQueueAdd(q, C.byref(d), C.c_void_p(raw.data_ptr()), C.c_void_p(out.data_ptr())) == 0, rv.last_error()
+    chosen = C.c_int(-1)
+    assert L.RvQueueAutotune(q, None, C.byref(chosen)) == 0, rv.last_error()
+    assert L.RvQueueRun(q, None) == 0, rv.last_error()      # captures the graph
+    qms = []
+    for _ in range(3):
+        assert L.RvQueueRun(q, None) == 0, rv.last_error()
+        qms.append(L.RvQueueLastMs(q))
+    upd = L.RvQueueUpdates(q)
+    L.RvQueueDestroy(q)
+    sms = 0.0
+    for (W, V, S, interp, cen, raw, binc, fdeg, fexp, F, out) in data:
+        st = rv.Stack(ixdim=W, nframes=V + 2, nslices=S, center=cen, bInc=binc, fdeg=fdeg, fexp=fexp, fFilter=F,
+                      iInterpolation=interp)
+        st.run_device(raw.data_ptr(), out.data_ptr())
+        best = 1e30
+        for _ in range(2):
+            st.run_device(raw.data_ptr(), out.data_ptr())
+            best = min(best, st.timings()[2])
+        sms += best
+        st.close()
+    qm = float(np.median(qms))
+    return {"datasets": len(data), "shapes_W_V_S_zoom": [list(x[:3]) + [2 ** (x[3] - 2)] for x in data],
+            "updates": upd, "queue_ms": qm, "queue_tau_ns": qm * 1e6 / upd, "one_stack_at_a_time_ms": sms,
+            "speedup_vs_stacks": sms / qm, "autotuned_variant": chosen.value}
 
 
 NET_FILE = ROOT / "recview_gb300" / "data" / "centre_net_256x512.f32"
