@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-centre", action="store_true", help="skip the centre-search summary of the default run")
     ap.add_argument("--no-forms", action="store_true", help="skip the reduced-storage and queue summaries")
     ap.add_argument("--seed", type=int, default=2026)
-    ap.add_argument("--workload", default="fbp", choices=["fbp", "centre"],
+    ap.add_argument("--workload", default="fbp", choices=["fbp", "centre", "precision"],
                     help="fbp: the back-projection stack (default); centre: train the centre-proposal network "
                          "and compare the learned search with the full sweep")
     ap.add_argument("--datasets", type=int, default=200, help="centre: evaluation datasets")
@@ -529,6 +529,60 @@ def centre_evaluate(net, n: int, rng) -> dict:
     }
 
 
+def run_precision(args):
+    """Configuration C4 shapes: 4096-pixel detector x 3600 views, 32 slices of 4096^2; the REF
+    drop-in and the FP32 / FP16 / BF16 filtered-row forms on the same device-resident frames."""
+    import torch
+    import recview_gb300 as rv
+    from recview_gb300 import abi
+    from recview_gb300.build import build_lib
+    build_lib()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    L = rv.lib()
+    W, V, S = 4096, 3600, 32
+    deg = (np.arange(V) * (180.0 / V)).astype(np.float32)
+    raw = torch.empty((V + 3, S, W), dtype=torch.int16, device=dev)
+    bInc = np.zeros(V + 2, np.int8)
+    fdeg = np.zeros(V + 2, np.float32)
+    fexp = np.zeros(V + 2, np.float32)
+    rng = np.random.default_rng(args.seed)
+    cen = (W - 1) / 2.0 + float(rng.uniform(-10, 10))
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    assert L.RvPhantomFrames(args.seed, W, S, fp(deg), V, cen, 40, C.c_void_p(raw.data_ptr()),
+                             C.c_void_p(bInc.ctypes.data), fp(fdeg), fp(fexp), None) == 0, rv.last_error()
+    F = rv.set_filter(abi.FILT_SHEPP, rv.dims(W).ndim)
+    res = {}
+    for name, mode in (("ref", abi.MODE_REF), ("lin_fp32", abi.MODE_LIN), ("lin_fp16", abi.MODE_LIN_F16),
+                       ("lin_bf16", abi.MODE_LIN_BF16)):
+        st = rv.Stack(ixdim=W, nframes=V + 2, nslices=S, center=cen, bInc=bInc, fdeg=fdeg, fexp=fexp, fFilter=F,
+                      mode=mode)
+        out = torch.empty((S, st.ixdimp, st.ixdimp), dtype=torch.int32 if mode == abi.MODE_REF else torch.float32,
+                          device=dev)
+        for _ in range(max(1, args.warmup)):
+            st.run_device(raw.data_ptr(), out.data_ptr())
+        tt, tf, tb = [], [], []
+        for _ in range(args.steps):
+            st.run_device(raw.data_ptr(), out.data_ptr())
+            a, b, c = st.timings()
+            tf.append(a)
+            tb.append(b)
+            tt.append(c)
+        ms = float(np.mean(tt))
+        upd = float(st.ixdimp) ** 2 * st.nviews * S
+        res[name] = {"tau_ns": ms * 1e6 / upd, "ms_per_step": ms, "filter_ms": float(np.mean(tf)),
+                     "backprojection_ms": float(np.mean(tb)), "updates_per_s": upd / (ms * 1e-3)}
+        st.close()
+        del out
+        torch.cuda.empty_cache()
+    line = {"metric": "tau_ns_per_pixel_view", "value": res["ref"]["tau_ns"], "unit": "ns/(pixel*view)",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "workload": "precision-4096det-3600views-32slices-raw-uint16", "data": "synthetic (seeded ellipsoid "
+            "phantom, Poisson uint16 frames)", "forms": res,
+            "errors": "FP64-oracle relative L2 per form: tests/test_gpu_parity.py and the design notes"}
+    print(json.dumps(line), flush=True)
+
+
 def run_centre(args):
     """Learned centre search vs the plain full sweep (configuration C5 shapes: 2048-pixel detector,
     1800 views, uint16 Poisson raw frames, true offset U[-40, 40] px)."""
@@ -591,6 +645,9 @@ def main():
     args = parse()
     if args.workload == "centre":
         run_centre(args)
+        return
+    if args.workload == "precision":
+        run_precision(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -608,7 +608,7 @@ static void rvo_fft64(int np, int inverse, const double* wr, const double* wi, d
     }
 }
 
-int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
+static int rvo_lin64_band(RECONST_INFO* ri, double* out, int iy0, int iy1) {
     RvDims d;
     rvo_dims(ri->ixdim, ri->iInterpolation, &d);
     const int ixdimp = d.ixdimp, ndim = d.ndim;
@@ -623,7 +623,6 @@ int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
         wr[i] = cos(a);
         wi[i] = sin(a);
     }
-    memset(out, 0, sizeof(double) * (size_t)ixdimp * ixdimp);
     const double cen = (double)d.ixdimh + (center - (int)center) * d.iIntpDim;
     for (int i = 0; i < ri->iLenSinogr - 1; i++) {
         int sidx = 0;
@@ -639,7 +638,7 @@ int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
         const double th = (double)(ri->fdeg[i] + ri->fTiltAngle) * (M_PI / 180.0);
         const double c = cos(th), s = -sin(th);
         const double off = cen - d.ixdimh * (c + s);
-        for (int iy = 0; iy < ixdimp; iy++) {
+        for (int iy = iy0; iy < iy1; iy++) {
             for (int ix = 0; ix < ixdimp; ix++) {
                 const double x = ix * c + iy * s + off;
                 if (!(x >= 0.0) || !(x < ixdimp)) continue;
@@ -653,6 +652,46 @@ int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
     }
     free(buf); free(fre);
     return 0;
+}
+
+int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out) {
+    RvDims d;
+    rvo_dims(ri->ixdim, ri->iInterpolation, &d);
+    memset(out, 0, sizeof(double) * (size_t)d.ixdimp * d.ixdimp);
+    return rvo_lin64_band(ri, out, 0, d.ixdimp);
+}
+
+typedef struct { RECONST_INFO* ri; double* out; int y0, y1, rc; } RvoLinJob;
+
+static void* rvo_lin64_worker(void* arg) {
+    RvoLinJob* j = (RvoLinJob*)arg;
+    j->rc = rvo_lin64_band(j->ri, j->out, j->y0, j->y1);
+    return NULL;
+}
+
+int rvo_reconstruct_lin64_mt(RECONST_INFO* ri, double* out, int nthreads) {
+    /* the same sums, image rows split into bands (each band refilters every view) */
+    RvDims d;
+    rvo_dims(ri->ixdim, ri->iInterpolation, &d);
+    memset(out, 0, sizeof(double) * (size_t)d.ixdimp * d.ixdimp);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    RvoLinJob* jobs = (RvoLinJob*)calloc((size_t)nthreads, sizeof(RvoLinJob));
+    if (!th || !jobs) { free(th); free(jobs); return RV_ERR_HOST_ALLOC; }
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t].ri = ri;
+        jobs[t].out = out;
+        jobs[t].y0 = (int)((long long)d.ixdimp * t / nthreads);
+        jobs[t].y1 = (int)((long long)d.ixdimp * (t + 1) / nthreads);
+        pthread_create(&th[t], NULL, rvo_lin64_worker, &jobs[t]);
+    }
+    int rc = 0;
+    for (int t = 0; t < nthreads; t++) {
+        pthread_join(th[t], NULL);
+        if (jobs[t].rc) rc = jobs[t].rc;
+    }
+    free(th); free(jobs);
+    return rc;
 }
 
 /* ---------------------------------------------------------------- R11 ------------------- */

@@ -74,6 +74,8 @@ void rvo_rescale(int* slice, int ixdimp, double center_user, int ipintp, int ibi
  * interpolation of the filtered row and double accumulation; out[ixdimp^2] is scaled like the
  * int32 reference (x BACKPROJ_SCALE) so the two are directly comparable. */
 int rvo_reconstruct_lin64(RECONST_INFO* ri, double* out);
+/* The same with image rows split over nthreads threads (identical sums per pixel). */
+int rvo_reconstruct_lin64_mt(RECONST_INFO* ri, double* out, int nthreads);
 
 /* R11: CGazoDoc::GetAxis after the frame reads (source/gazoDoc.cpp:4379-4626): 0-degree frame,
  * ~180-degree frame and flat, ixdim x iydim each; returns the applied centre/gradient and the

@@ -45,6 +45,7 @@ class Oracle:
         L.rvo_reconstruct_mt.argtypes = [RIP, C.c_int]
         L.rvo_generate_sinogram.argtypes = [RIP]
         L.rvo_reconstruct_lin64.argtypes = [RIP, C.POINTER(C.c_double)]
+        L.rvo_reconstruct_lin64_mt.argtypes = [RIP, C.POINTER(C.c_double), C.c_int]
         L.rvo_rescale.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_double, C.c_int, C.c_int,
                                   C.POINTER(C.c_int), C.POINTER(C.c_int)]
         U16P = C.POINTER(C.c_ushort)
@@ -83,9 +84,12 @@ class Oracle:
     def generate_sinogram(self, ri: ReconInfo) -> int:
         return self.L.rvo_generate_sinogram(C.byref(ri.ri))
 
-    def lin64(self, ri: ReconInfo) -> np.ndarray:
+    def lin64(self, ri: ReconInfo, threads: int = 1) -> np.ndarray:
         out = np.zeros((ri.d.ixdimp, ri.d.ixdimp), np.float64)
-        self.L.rvo_reconstruct_lin64(C.byref(ri.ri), out.ctypes.data_as(C.POINTER(C.c_double)))
+        if threads > 1:
+            self.L.rvo_reconstruct_lin64_mt(C.byref(ri.ri), out.ctypes.data_as(C.POINTER(C.c_double)), threads)
+        else:
+            self.L.rvo_reconstruct_lin64(C.byref(ri.ri), out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
     def get_axis(self, s0, s1, flat, offset=0):

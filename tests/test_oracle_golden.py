@@ -77,3 +77,10 @@ def test_get_axis_bit_exact(golden, oracle, name):
     off, c, g = golden[f"{name}_params"]
     got = oracle.get_axis(s0, s1, fl, int(off))
     assert got[0] == c and got[1] == g
+
+
+def test_lin64_threads_equal_serial(oracle):
+    """The row-band parallel FP64 oracle sums every pixel exactly as the serial one."""
+    from tests.rvtest import fbp_case
+    ri = fbp_case(3, 96, 70, 47.3, oracle=oracle)
+    assert np.array_equal(oracle.lin64(ri), oracle.lin64(ri, threads=3))
