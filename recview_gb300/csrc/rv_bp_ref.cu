@@ -27,6 +27,7 @@
 //
 // Optional padded layout (table_fmt): 17 words per detector pixel, so lanes whose indices differ
 // by ~16 (views near 0 or 90 degrees) fall into different shared-memory banks.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -648,6 +649,232 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_pipe_persistent(c
         const bool tok = bp_ref_tile_pipe<WX, WY, RX, RY, VC, NB, PAD, false>(J, smi, gc, nullptr);
         if (__syncthreads_or(!tok)) return;   // the CTA leaves together after a timeout
         gc += (unsigned)((J.nviews + VC - 1) / VC);
+    }
+}
+
+// ---- LIN / FP16 / BF16: linear interpolation of filtered pair rows -------------------------------
+// Not the reference's arithmetic (that is REF): the filtered row of each view is stored as pairs
+// (r[j], r[j+1] - r[j]) in FP32 (8 B) or, with a per-row scale, FP16 / BF16 (4 B), and every update
+// interpolates at the FP32 detector coordinate u:  acc += scale * (r[j] + (u - j) * slope[j]).
+// Same warp-decoupled pipeline as bp_ref_tile_pipe: each view's window of pairs (the detector
+// pixels a tile can touch) is staged by one TMA bulk copy into NB buffers with full/empty
+// mbarriers, so 16-bit storage halves both the L2 traffic and the shared-memory gathers.
+// Per update: FADD (u), FADD.RZ (floor as bits), FADD (j as float), FADD (fraction), LEA, LDS,
+// [2 conversions], FFMA, FFMA.
+template <int MODE>
+struct LinElem;
+template <>
+struct LinElem<RV_MODE_LIN> { static constexpr int ES = 8; };
+template <>
+struct LinElem<RV_MODE_LIN_F16> { static constexpr int ES = 4; };
+template <>
+struct LinElem<RV_MODE_LIN_BF16> { static constexpr int ES = 4; };
+
+template <int MODE>
+__device__ __forceinline__ float2 lin_pair(unsigned addr) {
+    if (MODE == RV_MODE_LIN) {
+        float2 v;
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+        return v;
+    } else {
+        unsigned w;
+        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(addr));
+        if (MODE == RV_MODE_LIN_F16) {
+            __half2 h = *reinterpret_cast<__half2*>(&w);
+            return __half22float2(h);
+        }
+        return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+    }
+}
+
+template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE>
+struct LinCfg {
+    static constexpr int NT = 32 * WX * WY, NW = NT / 32;
+    static constexpr int GX = 8 * WX, GY = 4 * WY, TX = GX * RX, TY = GY * RY;
+    static constexpr int ES = LinElem<MODE>::ES;
+    // detector-pixel span of a tile + margins (2 below, 3 above) + 4-pair alignment, in pairs
+    static constexpr int WINP = ((isqrt_ceil((TX - 1) * (TX - 1) + (TY - 1) * (TY - 1)) + 2 + 3 + 4 + 4) + 15) / 16 * 16;
+    static constexpr int WIN_BYTES = WINP * ES;
+    static constexpr int META_OFF = NB * VC * WIN_BYTES;                  // bytes
+    static constexpr int BAR_OFF = META_OFF + NB * VC * (int)sizeof(ViewMeta);
+    static constexpr size_t SMEM = (size_t)BAR_OFF + (size_t)2 * NB * 8;
+};
+
+template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE, int MINB>
+__global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaunch p) {
+    using Cfg = LinCfg<WX, WY, RX, RY, VC, NB, MODE>;
+    constexpr int TX = Cfg::TX, TY = Cfg::TY, WINP = Cfg::WINP, ES = Cfg::ES;
+    extern __shared__ __align__(128) unsigned char smb[];
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(smb + Cfg::META_OFF);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smb + Cfg::BAR_OFF);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        for (int b = 0; b < NB; b++) {
+            mbar_init(smem_u32(&bars[b]), 1);
+            mbar_init(smem_u32(&bars[NB + b]), Cfg::NW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int ixdimp = p.ixdimp;
+    const int tiles_x = (ixdimp + TX - 1) / TX;
+    const int X0 = (blockIdx.x % tiles_x) * TX, Y0 = (blockIdx.x / tiles_x) * TY;
+    const int slice = blockIdx.y;
+    const int tx = (warp % WX) * 8 + (lane & 7), ty = (warp / WX) * 4 + (lane >> 3);
+    const unsigned char* rows = static_cast<const unsigned char*>(p.rows16) + (size_t)slice * p.slice_row_stride * ES;
+    const float* scales = p.row_scale ? p.row_scale + (size_t)slice * p.nviews : nullptr;
+    const LinGeom* geom = p.geom64 + (size_t)slice * p.geom_slice_stride;
+    const int nviews = p.nviews;
+    const int nchunks = (nviews + VC - 1) / VC;
+    // coordinates relative to the tile origin (small, so FP32 keeps ~1e-6 px); the tile-origin term
+    // of each view comes from the FP64 geometry
+    float colf[RX], rowf[RY];
+#pragma unroll
+    for (int c = 0; c < RX; c++) colf[c] = (float)(tx + Cfg::GX * c);
+#pragma unroll
+    for (int r = 0; r < RY; r++) rowf[r] = (float)(ty + Cfg::GY * r);
+
+    auto produce = [&](int c) -> bool {
+        const unsigned g = (unsigned)c;
+        const int b = (int)(g % NB);
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
+            return false;
+        const int v0 = c * VC;
+        const int nv = min(VC, nviews - v0);
+        if (lane < nv) {
+            const LinGeom gg = geom[v0 + lane];
+            // u at the tile origin in FP64 (two FMAs); the tile's lowest u adds the negative parts of
+            // the tile's extent, which FP32 gives well inside the window's 2-pixel margin
+            const double base = fma((double)X0, gg.c, fma((double)Y0, gg.s, gg.off));
+            const float lo = (float)base + fminf(0.0f, (float)(TX - 1) * (float)gg.c) + fminf(0.0f, (float)(TY - 1) * (float)gg.s);
+            const int ilo = (int)floorf(lo) - 2;
+            const int w0 = ilo >= 0 ? (ilo & ~3) : -((-ilo + 3) & ~3);
+            ViewMeta m;
+            m.w0 = w0;
+            m.nwin = WINP;
+            m.a = max(w0, 0);
+            m.b = min(w0 + WINP, (ixdimp + 3) & ~3);
+            m.gc = (float)gg.c;
+            m.gs = (float)gg.s;
+            m.go = (float)(base - (double)w0);   // window-relative u at the tile origin
+            m.off = __float_as_uint(scales ? scales[v0 + lane] : 1.0f);
+            meta[b * VC + lane] = m;
+        }
+        __syncwarp();
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[b * VC + vv];
+            if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
+            int4* w4 = reinterpret_cast<int4*>(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES);
+            const int bytes_a = (m.b > m.a ? m.a - m.w0 : m.nwin) * ES, bytes_b = (m.b > m.a ? m.b - m.w0 : m.nwin) * ES;
+            for (int e = lane; e < bytes_a / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+            for (int e = bytes_b / 16 + lane; e < Cfg::WIN_BYTES / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            unsigned bytes = 0;
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[b * VC + vv];
+                if (m.b > m.a) bytes += (unsigned)((m.b - m.a) * ES);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const unsigned bar = smem_u32(&bars[b]);
+            mbar_arrive_expect_tx(bar, bytes);
+            for (int vv = 0; vv < nv; vv++) {
+                const ViewMeta m = meta[b * VC + vv];
+                if (m.b <= m.a) continue;
+                const unsigned char* src = rows + ((size_t)(v0 + vv) * p.row_stride + m.a) * ES;
+                const unsigned dst = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
+                tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
+            }
+        }
+        __syncwarp();
+        return true;
+    };
+
+    float acc[RY][RX];
+#pragma unroll
+    for (int r = 0; r < RY; r++)
+#pragma unroll
+        for (int c = 0; c < RX; c++) acc[r][c] = 0.0f;
+    bool ok = true;
+    int produced = 0;
+    if (warp == 0)
+        for (; produced < nchunks && produced < NB - 1; produced++)
+            if (!produce(produced)) { ok = false; break; }
+    for (int k = 0; ok && k < nchunks; k++) {
+        if (warp == 0 && produced < nchunks) {
+            if (!produce(produced)) { ok = false; break; }
+            produced++;
+        }
+        const unsigned g = (unsigned)k;
+        const int b = (int)(g % NB);
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) { ok = false; break; }
+        const int nv = min(VC, nviews - k * VC);
+        for (int vv = 0; vv < nv; vv++) {
+            const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+            const float sc = __uint_as_float(__float_as_uint(gm.w));
+            float xv[RX], yv[RY];
+#pragma unroll
+            for (int c = 0; c < RX; c++) xv[c] = colf[c] * gm.x;
+#pragma unroll
+            for (int r = 0; r < RY; r++) yv[r] = fmaf(rowf[r], gm.y, gm.z);
+            // address of pair 0 minus the 2^23 bit pattern (unsigned wrap-around)
+            const unsigned base = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES) - (unsigned)ES * kMagicBits;
+#pragma unroll
+            for (int r = 0; r < RY; r++)
+#pragma unroll
+                for (int c = 0; c < RX; c++) {
+                    const float u = xv[c] + yv[r];                       // >= 1.9 inside the window
+                    const float t = __fadd_rz(u, 8388608.0f);
+                    const unsigned bits = __float_as_uint(t);
+                    const float f = u - (t - 8388608.0f);
+                    const float2 q = lin_pair<MODE>(base + (unsigned)ES * bits);
+                    const float v = fmaf(f, q.y, q.x);
+                    if (MODE == RV_MODE_LIN) acc[r][c] += v;
+                    else acc[r][c] = fmaf(v, sc, acc[r][c]);
+                }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
+    }
+    if (!ok) {
+        atomicOr(&g_kernel_status, 1u);
+        if (warp == 0)
+            for (int c = produced > NB ? produced - NB : 0; c < produced; c++)
+                mbar_wait_bounded(smem_u32(&bars[(unsigned)c % NB]), ((unsigned)c / NB) & 1u);
+        return;
+    }
+    float* out = static_cast<float*>(p.out) + (size_t)slice * p.out_slice_stride;
+#pragma unroll
+    for (int r = 0; r < RY; r++) {
+        const int y = Y0 + ty + Cfg::GY * r;
+        if (y >= ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < RX; c++) {
+            const int x = X0 + tx + Cfg::GX * c;
+            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+        }
+    }
+}
+
+template <int MODE>
+static cudaError_t go_lin(const BackprojLaunch& p, cudaStream_t s) {
+    constexpr int WX = 2, WY = 4, RX = 4, RY = 4, VC = 8, NB = 2, MINB = 4;
+    using Cfg = LinCfg<WX, WY, RX, RY, VC, NB, MODE>;
+    auto kern = k_bp_lin_pipe<WX, WY, RX, RY, VC, NB, MODE, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
+    kern<<<dim3(tiles, p.nslices), Cfg::NT, Cfg::SMEM, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bp_lin(const BackprojLaunch& p, cudaStream_t s) {
+    switch (p.mode) {
+    case RV_MODE_LIN: return go_lin<RV_MODE_LIN>(p, s);
+    case RV_MODE_LIN_F16: return go_lin<RV_MODE_LIN_F16>(p, s);
+    case RV_MODE_LIN_BF16: return go_lin<RV_MODE_LIN_BF16>(p, s);
+    default: return cudaErrorInvalidValue;
     }
 }
 

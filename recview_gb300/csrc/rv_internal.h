@@ -59,33 +59,36 @@ struct FilterLaunch {
     const float* filt;        // device, ndim
     const float2* tw;         // device, ndim entries: pass l's twiddle q at [2^l + q]
     int* table;               // REF output: int table, 16*ixdimp ints per slot (may be null)
-    float* rows;              // LIN output: filtered rows x BACKPROJ_SCALE (may be null)
-    void* rows16;             // LIN_F16/BF16 output: half/bf16 rows (may be null)
-    float* row_scale;         // per-row scale of the 16-bit rows
+    void* rows16;             // LIN output: pair rows (r, r[j+1]-r) x BACKPROJ_SCALE, FP32 / FP16 / BF16
+    float* row_scale;         // per-row scale of the 16-bit pair rows
     int mode;
     Dims d;
     int ic;                   // (int)center
     int ic_per_job;           // 1: take the integer centre from each RowJob (centre sweeps)
     long long table_stride;   // ints between table slots
-    long long row_stride;     // elements between filtered rows
+    long long row_stride;     // pairs between LIN rows (lin_pair_stride)
     int table_fmt;            // REF table format, see ref_table_fmt()
 };
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
 
 // ---- back-projection ---------------------------------------------------------------------
+// LIN geometry of one view in FP64: detector coordinate u = x c + y s + off (zoomed pixels)
+struct LinGeom {
+    double c, s, off, pad;
+};
 struct BackprojLaunch {
     const int* table;         // REF: int tables, slot-major
-    const float* rows;        // LIN: float rows
-    const void* rows16;       // LIN_F16/BF16 rows
+    const void* rows16;       // LIN: pair rows (8 B FP32 or 4 B FP16 / BF16 per detector pixel)
     const float* row_scale;
     const float4* geom;       // per view {fcos, fsin, foffset, 0} (REF units: x16)
+    const LinGeom* geom64;    // LIN: per view geometry in FP64 (slice stride geom_slice_stride)
     long long geom_slice_stride;  // float4s between the geometry of consecutive slices (0: shared)
     int nviews;               // views per slice
     int nslices;
     int ixdimp;
     long long table_stride;   // ints per view slot
     long long slice_table_stride;  // ints per slice (nviews * table_stride)
-    long long row_stride;     // LIN: elements per row
+    long long row_stride;     // LIN: pairs per row
     long long slice_row_stride;
     void* out;                // int32 (REF) or float (LIN) slices, ixdimp^2 each
     long long out_slice_stride;  // elements per output slice
@@ -110,6 +113,12 @@ int default_variant();
 cudaError_t launch_bp_ref_persistent(const TileJob* d_jobs, int njobs, unsigned* d_counter, int table_fmt,
                                      int variant, cudaStream_t s);
 cudaError_t launch_bp_ref(const BackprojLaunch& p, cudaStream_t s);
+// LIN / FP16 / BF16 back-projection of pair rows (rows16 = pairs (r[j], r[j+1]-r[j]) of 8 or 4 bytes,
+// row_stride / slice_row_stride in pairs, row_scale per row for the 16-bit forms)
+cudaError_t launch_bp_lin(const BackprojLaunch& p, cudaStream_t s);
+// pairs per stored LIN row (a multiple of 4 so every row starts on a 16-byte boundary)
+inline int lin_pair_stride(int ixdimp) { return (ixdimp + 3) & ~3; }
+inline int lin_pair_bytes(int mode) { return mode == RV_MODE_LIN ? 8 : 4; }
 // REF table format per detector pixel j, and the slot stride in 4-byte words:
 //   kTabInt16: the reference's 16 ints igp[16j+k]          (64 B per pixel)
 //   kTabInt17: the same with one unused word after each 16  (68 B, fewer bank conflicts)

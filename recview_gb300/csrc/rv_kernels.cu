@@ -3,9 +3,8 @@
 //  k_normalise  R1      flat/dark log normalisation -> int16 rows (CudaSinogramHost)
 //  k_filter     R1+R5+R6+R7  one CTA per sinogram row: [normalise] -> pad/zoom -> forward
 //                       radix-2 FFT -> filter -> inverse FFT -> 1/16 sub-sample int table
-//                       (REF) or FP32/FP16/BF16 filtered row (LIN modes)
-//  k_bp_ref     R8      pixel-tile back-projection with the reference's fixed-point table
-//  k_bp_lin     R8'     pixel-tile back-projection with linear interpolation (FP32 accumulate)
+//                       (REF) or FP32/FP16/BF16 (value, slope) pair row (LIN modes)
+//  (the back-projection kernels, REF and LIN, are in rv_bp_ref.cu)
 //
 // Floating-point discipline: every operation that the reference performs in float is done with
 // an explicitly rounded intrinsic (__fmul_rn/__fadd_rn/__fsub_rn) so nvcc never contracts it into
@@ -274,36 +273,40 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         if (p.table_fmt == kTabPair && (ixdimp & 1) && tid == 0)
             reinterpret_cast<float2*>(tab)[ixdimp] = make_float2(0.0f, 0.0f);
     }
-    if (p.rows) {
-        float* row = p.rows + (size_t)job.dst * p.row_stride;
-        for (int j = tid; j < ixdimp; j += NT) row[j] = fmul(fmul(buf[rbase - j].x, inv_n), 100.0f);
-    }
     if (p.rows16) {
-        // per-row scale: max |q*100| over the row / 16384 keeps FP16 far from overflow
-        __shared__ float red[32];
-        float m = 0.0f;
-        for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(buf[rbase - j].x));
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((tid & 31) == 0) red[tid >> 5] = m;
-        __syncthreads();
-        if (tid < 32) {
-            m = (tid < (NT >> 5)) ? red[tid] : 0.0f;
+        // LIN forms: pairs (r[j], r[j+1] - r[j]) of r = q * 100 (slope 0 at the last sample, zero
+        // pairs up to the padded stride), FP32 or -- with a per-row scale max |r| / 16384 that keeps
+        // FP16 far from overflow -- FP16 / BF16
+        float scale = 1.0f, rs = 1.0f;
+        if (p.mode != RV_MODE_LIN) {
+            __shared__ float red[32];
+            float m = 0.0f;
+            for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(buf[rbase - j].x));
             for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-            if (tid == 0) red[0] = m;
+            if ((tid & 31) == 0) red[tid >> 5] = m;
+            __syncthreads();
+            if (tid < 32) {
+                m = (tid < (NT >> 5)) ? red[tid] : 0.0f;
+                for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+                if (tid == 0) red[0] = m;
+            }
+            __syncthreads();
+            const float amax = red[0] * inv_n * 100.0f;
+            scale = amax > 0.0f ? amax / 16384.0f : 1.0f;
+            rs = 1.0f / scale;
+            if (tid == 0) p.row_scale[job.dst] = scale;
         }
-        __syncthreads();
-        const float amax = red[0] * inv_n * 100.0f;
-        const float scale = amax > 0.0f ? amax / 16384.0f : 1.0f;
-        const float rs = 1.0f / scale;
-        if (tid == 0) p.row_scale[job.dst] = scale;
-        if (p.mode == RV_MODE_LIN_F16) {
-            __half* row = static_cast<__half*>(p.rows16) + (size_t)job.dst * p.row_stride;
-            for (int j = tid; j < ixdimp; j += NT)
-                row[j] = __float2half_rn(buf[rbase - j].x * inv_n * 100.0f * rs);
-        } else {
-            __nv_bfloat16* row = static_cast<__nv_bfloat16*>(p.rows16) + (size_t)job.dst * p.row_stride;
-            for (int j = tid; j < ixdimp; j += NT)
-                row[j] = __float2bfloat16_rn(buf[rbase - j].x * inv_n * 100.0f * rs);
+        const int ps = (int)p.row_stride;
+        for (int j = tid; j < ps; j += NT) {
+            float v0 = 0.0f, dv = 0.0f;
+            if (j < ixdimp) {
+                v0 = fmul(fmul(buf[rbase - j].x, inv_n), 100.0f);
+                if (j + 1 < ixdimp) dv = fsub(fmul(fmul(buf[rbase - j - 1].x, inv_n), 100.0f), v0);
+            }
+            const size_t at = (size_t)job.dst * p.row_stride + j;
+            if (p.mode == RV_MODE_LIN) static_cast<float2*>(p.rows16)[at] = make_float2(v0, dv);
+            else if (p.mode == RV_MODE_LIN_F16) static_cast<__half2*>(p.rows16)[at] = __floats2half2_rn(v0 * rs, dv * rs);
+            else static_cast<__nv_bfloat162*>(p.rows16)[at] = __floats2bfloat162_rn(v0 * rs, dv * rs);
         }
     }
 }
@@ -333,140 +336,11 @@ cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {
     return e;
 }
 
-// Back-projection tiling shared by the LIN kernel (the REF kernel lives in rv_bp_ref.cu).
-constexpr int BP_T = 64;        // tile edge
-constexpr int BP_THREADS = 256;
-
-// ---------------------------------------------------------------------------------------------
-// R8' (LIN): the same tiling with true linear interpolation of the filtered row at the FP32
-// detector coordinate u = ix*cos + iy*(-sin) + off (detector-pixel units) and FP32
-// accumulation.  The window holds (r[j], r[j+1]-r[j]) pairs so one 64-bit shared load feeds
-// one FMA; FP16/BF16 rows are expanded to FP32 pairs while staging (per-row scale applied).
-// ---------------------------------------------------------------------------------------------
-constexpr int LIN_WIN = 128;    // detector pixels per view window (>= 63*sqrt(2) + margins)
-
-template <int VC, int MODE>
-__global__ void __launch_bounds__(BP_THREADS, 2) k_bp_lin(BackprojLaunch p) {
-    __shared__ __align__(16) float2 win[VC][LIN_WIN];
-    __shared__ __align__(16) float xs[VC][64];
-    __shared__ __align__(16) float ys[VC][64];
-    __shared__ int los[VC];
-
-    const int ixdimp = p.ixdimp;
-    const int tiles_x = (ixdimp + BP_T - 1) / BP_T;
-    const int X0 = (blockIdx.x % tiles_x) * BP_T;
-    const int Y0 = (blockIdx.x / tiles_x) * BP_T;
-    const int slice = blockIdx.y;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int tx = (warp & 1) * 8 + (lane & 7);
-    const int ty = (warp >> 1) * 4 + (lane >> 3);
-    const int nviews = p.nviews;
-    float acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[r][c] = 0.0f;
-
-    for (int v0 = 0; v0 < nviews; v0 += VC) {
-        const int nv = min(VC, nviews - v0);
-        if (tid < nv) {
-            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + tid);
-            float lo = 3.0e38f;
-#pragma unroll
-            for (int cy = 0; cy < 2; cy++)
-#pragma unroll
-                for (int cx = 0; cx < 2; cx++)
-                    lo = fminf(lo, fmaf((float)(X0 + cx * (BP_T - 1)), g.x, fmaf((float)(Y0 + cy * (BP_T - 1)), g.y, g.z)));
-            los[tid] = (int)floorf(lo) - 2;
-        }
-        for (int e = tid; e < VC * 128; e += BP_THREADS) {
-            const int vv = e >> 7, w = e & 127;
-            if (vv >= nv) continue;
-            const float4 g = __ldg(p.geom + (size_t)slice * p.geom_slice_stride + v0 + vv);
-            if (w < 64) xs[vv][w] = (float)(X0 + (w >> 2) + 16 * (w & 3)) * g.x;
-            else {
-                const int ww = w - 64;
-                ys[vv][ww] = fmaf((float)(Y0 + (ww >> 2) + 16 * (ww & 3)), g.y, g.z);
-            }
-        }
-        __syncthreads();
-        for (int e = tid; e < VC * LIN_WIN; e += BP_THREADS) {
-            const int vv = e / LIN_WIN, w = e - vv * LIN_WIN;
-            if (vv >= nv) continue;
-            // pair j: (r[j], r[j+1] - r[j]) for 0 <= j < ixdimp, slope 0 at the last sample
-            // (source/general.cpp:2132-2133); zero outside the detector.
-            const int j = los[vv] + w;
-            const size_t rb = (size_t)slice * p.slice_row_stride + (size_t)(v0 + vv) * p.row_stride;
-            float r0 = 0.0f, r1 = 0.0f;
-            if (j >= 0 && j < ixdimp) {
-                const int j1 = (j + 1 < ixdimp) ? j + 1 : j;
-                if (MODE == RV_MODE_LIN) {
-                    const float* row = p.rows + rb;
-                    r0 = __ldg(row + j);
-                    r1 = __ldg(row + j1);
-                } else {
-                    const float sc = __ldg(p.row_scale + (size_t)slice * p.nviews + v0 + vv);
-                    if (MODE == RV_MODE_LIN_F16) {
-                        const __half* row = static_cast<const __half*>(p.rows16) + rb;
-                        r0 = __half2float(row[j]) * sc;
-                        r1 = __half2float(row[j1]) * sc;
-                    } else {
-                        const __nv_bfloat16* row = static_cast<const __nv_bfloat16*>(p.rows16) + rb;
-                        r0 = __bfloat162float(row[j]) * sc;
-                        r1 = __bfloat162float(row[j1]) * sc;
-                    }
-                }
-            }
-            win[vv][w] = make_float2(r0, r1 - r0);
-        }
-        __syncthreads();
-        for (int vv = 0; vv < nv; vv++) {
-            const float4 xa = *reinterpret_cast<const float4*>(&xs[vv][tx * 4]);
-            const float4 ya = *reinterpret_cast<const float4*>(&ys[vv][ty * 4]);
-            const float xv[4] = {xa.x, xa.y, xa.z, xa.w};
-            const float yv[4] = {ya.x, ya.y, ya.z, ya.w};
-            const float flo = (float)los[vv];
-#pragma unroll
-            for (int r = 0; r < 4; r++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const float u = xv[c] + yv[r] - flo;   // >= 0 inside the window
-                    const float fl = floorf(u);
-                    const int j = (int)fl;
-                    const float f = u - fl;
-                    const float2 w2 = win[vv][min(j, LIN_WIN - 1)];
-                    acc[r][c] += fmaf(f, w2.y, w2.x);
-                }
-        }
-        __syncthreads();
-    }
-    float* out = static_cast<float*>(p.out) + (size_t)slice * p.out_slice_stride;
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int y = Y0 + ty + 16 * r;
-        if (y >= ixdimp) continue;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const int x = X0 + tx + 16 * c;
-            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
-        }
-    }
-}
-
 cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s) {
     if (p.nslices <= 0) return cudaSuccess;
     if (p.ixdimp > kMaxIxdimp) return cudaErrorInvalidValue;
     if (p.mode == RV_MODE_REF) return launch_bp_ref(p, s);
-    const int tiles = ((p.ixdimp + BP_T - 1) / BP_T) * ((p.ixdimp + BP_T - 1) / BP_T);
-    dim3 grid(tiles, p.nslices);
-    constexpr int VC = 8;
-    switch (p.mode) {
-    case RV_MODE_LIN: k_bp_lin<VC, RV_MODE_LIN><<<grid, BP_THREADS, 0, s>>>(p); break;
-    case RV_MODE_LIN_F16: k_bp_lin<VC, RV_MODE_LIN_F16><<<grid, BP_THREADS, 0, s>>>(p); break;
-    case RV_MODE_LIN_BF16: k_bp_lin<VC, RV_MODE_LIN_BF16><<<grid, BP_THREADS, 0, s>>>(p); break;
-    default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    return launch_bp_lin(p, s);
 }
 
 int kernel_launches_per_filter() { return 1; }

@@ -26,7 +26,8 @@ struct RvStack {
     int batch = 1;                  // slices per filter/back-projection batch
     std::vector<float> filt;
     std::vector<RowJob> jobs;       // slice-major: jobs[s * nviews + v]
-    std::vector<float4> geom_ref, geom_lin;
+    std::vector<float4> geom_ref;
+    std::vector<LinGeom> geom_lin;
     void* d_jobs = nullptr;
     void* d_geom = nullptr;
     void* d_filt = nullptr;
@@ -143,7 +144,7 @@ static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_table
         st->geom_ref[v] = make_float4(fc, fs, fo, 0.0f);
         const double th = (double)(desc->fdeg[views[v]] + desc->fTiltAngle) * (3.14159265358979323846 / 180.0);
         const double c = cos(th), sn = -sin(th);
-        st->geom_lin[v] = make_float4((float)c, (float)sn, (float)(cen_lin - d.ixdimh * (c + sn)), 0.0f);
+        st->geom_lin[v] = LinGeom{c, sn, cen_lin - d.ixdimh * (c + sn), 0.0};
     }
     st->filt.assign(desc->fFilter, desc->fFilter + d.ndim);
     // ---- batch size from the table budget ----------------------------------------------------
@@ -151,8 +152,9 @@ static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_table
     if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
     st->tfmt = ref_table_fmt();
     st->tstride = ref_table_stride(d.ixdimp, st->tfmt);
-    const size_t per_slice = desc->mode == RV_MODE_REF ? (size_t)V * st->tstride * sizeof(int)
-                                                       : (size_t)V * d.ixdimp * (desc->mode == RV_MODE_LIN ? 4 : 2);
+    const size_t per_slice = desc->mode == RV_MODE_REF
+                                 ? (size_t)V * st->tstride * sizeof(int)
+                                 : (size_t)V * lin_pair_stride(d.ixdimp) * lin_pair_bytes(desc->mode);
     size_t b = (budget_mb << 20) / (per_slice ? per_slice : 1);
     if (b < 1) b = 1;
     if (b > (size_t)S) b = S;
@@ -175,15 +177,16 @@ static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_table
     std::vector<float2> tw;
     fft_twiddles(d.ndimp, tw);
     bool ok = cuda_ok(cudaMalloc(&st->d_jobs, st->jobs.size() * sizeof(RowJob)), RV_ERR_DEVICE_OOM, "jobs") &&
-              cuda_ok(cudaMalloc(&st->d_geom, (size_t)V * sizeof(float4)), RV_ERR_DEVICE_OOM, "geometry") &&
+              cuda_ok(cudaMalloc(&st->d_geom, (size_t)V * sizeof(LinGeom)), RV_ERR_DEVICE_OOM, "geometry") &&
               cuda_ok(cudaMalloc(&st->d_filt, (size_t)d.ndim * sizeof(float)), RV_ERR_DEVICE_OOM, "filter") &&
               cuda_ok(cudaMalloc(&st->d_tw, tw.size() * sizeof(float2)), RV_ERR_DEVICE_OOM, "twiddles") &&
               (!alloc_tables || cuda_ok(cudaMalloc(&st->d_table, per_slice * st->batch), RV_ERR_DEVICE_OOM, "tables")) &&
               cuda_ok(cudaMalloc(&st->d_scale, (size_t)st->batch * V * sizeof(float)), RV_ERR_DEVICE_OOM, "scales");
     if (ok) {
-        const std::vector<float4>& g = desc->mode == RV_MODE_REF ? st->geom_ref : st->geom_lin;
+        const void* g = desc->mode == RV_MODE_REF ? (const void*)st->geom_ref.data() : (const void*)st->geom_lin.data();
+        const size_t gbytes = (size_t)V * (desc->mode == RV_MODE_REF ? sizeof(float4) : sizeof(LinGeom));
         ok = cuda_ok(cudaMemcpy(st->d_jobs, st->jobs.data(), st->jobs.size() * sizeof(RowJob), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "jobs") &&
-             cuda_ok(cudaMemcpy(st->d_geom, g.data(), (size_t)V * sizeof(float4), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "geometry") &&
+             cuda_ok(cudaMemcpy(st->d_geom, g, gbytes, cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "geometry") &&
              cuda_ok(cudaMemcpy(st->d_filt, st->filt.data(), (size_t)d.ndim * sizeof(float), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "filter") &&
              cuda_ok(cudaMemcpy(st->d_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice), RV_ERR_COPY_H2D, "twiddles");
     }
@@ -240,13 +243,10 @@ static int run_slices(RvStack* st, const void* d_raw, void* d_out, int s0, int n
         fl.table = static_cast<int*>(st->d_table);
         fl.table_stride = tstride;
         fl.table_fmt = st->tfmt;
-    } else if (mode == RV_MODE_LIN) {
-        fl.rows = static_cast<float*>(st->d_table);
-        fl.row_stride = d.ixdimp;
-    } else {
+    } else {   // LIN forms: pair rows
         fl.rows16 = st->d_table;
         fl.row_scale = static_cast<float*>(st->d_scale);
-        fl.row_stride = d.ixdimp;
+        fl.row_stride = lin_pair_stride(d.ixdimp);
     }
     // jobs of slice s write table slot (s mod batch): rebase so the first slice of this call
     // lands where its jobs point
@@ -257,17 +257,19 @@ static int run_slices(RvStack* st, const void* d_raw, void* d_out, int s0, int n
     BackprojLaunch bl{};
     const size_t slot0 = (size_t)(s0 % st->batch);
     bl.table = static_cast<const int*>(st->d_table) + slot0 * (size_t)(tstride * V);
-    bl.rows = static_cast<const float*>(st->d_table) + slot0 * (size_t)d.ixdimp * V;
-    bl.rows16 = static_cast<const char*>(st->d_table) + slot0 * (size_t)d.ixdimp * V * 2;
-    bl.row_scale = static_cast<const float*>(st->d_scale) + slot0 * V;
+    const int lps = lin_pair_stride(d.ixdimp);
+    bl.rows16 = static_cast<const char*>(st->d_table) + slot0 * (size_t)lps * V * lin_pair_bytes(mode);
+    bl.row_scale = mode == RV_MODE_LIN_F16 || mode == RV_MODE_LIN_BF16 ? static_cast<const float*>(st->d_scale) + slot0 * V
+                                                                       : nullptr;
     bl.geom = static_cast<const float4*>(st->d_geom);
+    bl.geom64 = static_cast<const LinGeom*>(st->d_geom);
     bl.nviews = V;
     bl.nslices = nb;
     bl.ixdimp = d.ixdimp;
     bl.table_stride = tstride;
     bl.slice_table_stride = tstride * V;
-    bl.row_stride = d.ixdimp;
-    bl.slice_row_stride = (long long)d.ixdimp * V;
+    bl.row_stride = lps;
+    bl.slice_row_stride = (long long)lps * V;
     bl.out = mode == RV_MODE_REF ? (void*)(static_cast<int*>(d_out) + (size_t)s0 * npix)
                                  : (void*)(static_cast<float*>(d_out) + (size_t)s0 * npix);
     bl.out_slice_stride = (long long)npix;
