@@ -42,6 +42,7 @@ struct RvStack {
     float t_filter = 0, t_bp = 0, t_total = 0;
     int launches = 0;
     cudaStream_t cs_in = nullptr, cs_out = nullptr;   // RunHost copy streams
+    cudaStream_t cs_alt = nullptr;                    // RunHost second compute stream
     std::vector<cudaEvent_t> pev;   // RunHost pipeline events
     int tfmt = 0;                   // REF table layout (ref_table_fmt at creation)
     long long tstride = 0;          // ints per table slot
@@ -57,6 +58,7 @@ static void stack_free(RvStack* st) {
         if (e) cudaEventDestroy(e);
     if (st->cs_in) cudaStreamDestroy(st->cs_in);
     if (st->cs_out) cudaStreamDestroy(st->cs_out);
+    if (st->cs_alt) cudaStreamDestroy(st->cs_alt);
 }
 
 static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_tables) {
@@ -321,8 +323,9 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
 
 // Host-buffer run, pipelined: the slices are processed in pieces; piece k's frames (all frames,
 // the piece's detector rows: one strided 2-D copy) go up on an input copy stream, its filter and
-// back-projection run on the caller's stream, and its slices come back on an output copy stream,
-// so host<->device traffic overlaps the kernels of neighbouring pieces.
+// back-projection run on the caller's stream or (odd pieces) a second compute stream, and its
+// slices come back on an output copy stream, so host<->device traffic and the tail of one
+// piece's back-projection overlap the work of neighbouring pieces.
 static int ensure_host_buffers(RvStack* st, size_t in_b, size_t out_b) {
     if (st->in_bytes < in_b) {
         if (st->d_in) cudaFree(st->d_in);
@@ -340,7 +343,8 @@ static int ensure_host_buffers(RvStack* st, size_t in_b, size_t out_b) {
     }
     if (!st->cs_in) {
         if (!cuda_ok(cudaStreamCreateWithFlags(&st->cs_in, cudaStreamNonBlocking), RV_ERR_STREAM, "copy stream") ||
-            !cuda_ok(cudaStreamCreateWithFlags(&st->cs_out, cudaStreamNonBlocking), RV_ERR_STREAM, "copy stream"))
+            !cuda_ok(cudaStreamCreateWithFlags(&st->cs_out, cudaStreamNonBlocking), RV_ERR_STREAM, "copy stream") ||
+            !cuda_ok(cudaStreamCreateWithFlags(&st->cs_alt, cudaStreamNonBlocking), RV_ERR_STREAM, "compute stream"))
             return RV_ERR_STREAM;
     }
     return 0;
@@ -384,7 +388,9 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
     cudaEventRecord(E[0], s);
     cudaStreamWaitEvent(st->cs_in, E[0], 0);
     cudaStreamWaitEvent(st->cs_out, E[0], 0);
+    cudaStreamWaitEvent(st->cs_alt, E[0], 0);
     const size_t pitch = (size_t)S * W * 2;
+    const int reuse = st->batch / P;   // pieces later a piece's table slots come round again
     for (int k = 0; k < npieces; k++) {
         const int s0 = k * P, nb = (S - s0) < P ? (S - s0) : P;
         cudaEvent_t* e = E + 1 + 5 * (size_t)k;
@@ -394,8 +400,12 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
                                        st->cs_in), RV_ERR_COPY_H2D, "raw frames"))
             return RV_ERR_COPY_H2D;
         cudaEventRecord(e[0], st->cs_in);
-        cudaStreamWaitEvent(s, e[0], 0);
-        rc = run_slices(st, st->d_in, st->d_out, s0, nb, s, e[1], e[2], e[3]);
+        // consecutive pieces alternate between two compute streams, so one piece's filter (and the
+        // start of its back-projection) fills the SMs the previous back-projection's last wave leaves
+        cudaStream_t ks = (k & 1) ? st->cs_alt : s;
+        cudaStreamWaitEvent(ks, e[0], 0);
+        if (k >= reuse) cudaStreamWaitEvent(ks, E[1 + 5 * (size_t)(k - reuse) + 3], 0);   // its table slots are free
+        rc = run_slices(st, st->d_in, st->d_out, s0, nb, ks, e[1], e[2], e[3]);
         if (rc) return rc;
         cudaStreamWaitEvent(st->cs_out, e[3], 0);
         if (!cuda_ok(cudaMemcpyAsync(static_cast<char*>(h_out) + (size_t)s0 * slice_b,
