@@ -417,6 +417,91 @@ __device__ __forceinline__ void pipe_init_barriers(int* smi) {
     }
 }
 
+// Warp 0 of a pipelined CTA: fill buffer g % NB with the table windows of chunk c (views
+// c*VC ..) once that buffer's empty barrier shows every warp is done with it.  Records each view's
+// geometry and window in meta, zero-fills the parts of a window outside the table, and issues one
+// TMA bulk copy per view on the buffer's full barrier.  Returns false (warp-uniform) when the wait
+// for the empty barrier ran out.
+template <int TX, int TY, int WIN, int ALIGN, int VC, int NB, int PAD>
+__device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* meta, uint64_t* bars, int c,
+                                          unsigned g, int lane) {
+    const int X0 = J.X0, Y0 = J.Y0;
+    const int nviews = J.nviews;
+    const int nstore = PAD ? ((17 * J.ixdimp + 3) & ~3) : 16 * J.ixdimp;
+    const int b = (int)(g % NB);
+    // warp-uniform verdict: every lane takes the same branch at the __syncwarp()s below
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
+        return false;
+    const int v0 = c * VC;
+    const int nv = min(VC, nviews - v0);
+    if (lane < nv) {
+        const float4 gg = __ldg(J.geom + v0 + lane);
+        float lo = 3.0e38f, hi = -3.0e38f;
+#pragma unroll
+        for (int cy = 0; cy < 2; cy++) {
+            const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), gg.y), gg.z);
+#pragma unroll
+            for (int cx = 0; cx < 2; cx++) {
+                const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), gg.x), fy);
+                lo = fminf(lo, fx);
+                hi = fmaxf(hi, fx);
+            }
+        }
+        const int ilo = (int)floorf(lo) - 2;
+        const int lo_a = ilo >= 0 ? (ilo & ~(ALIGN - 1)) : -((-ilo + ALIGN - 1) & ~(ALIGN - 1));
+        const int ihi = (int)floorf(hi) + 3;
+        ViewMeta m;
+        if (PAD) {
+            const int hi16 = (ihi + 15) & ~15;
+            m.w0 = lo_a + lo_a / 16;
+            const int w1 = hi16 + hi16 / 16;
+            m.nwin = min(((w1 - m.w0) + 3) & ~3, WIN);
+        } else {
+            m.w0 = lo_a;
+            m.nwin = min(((ihi - lo_a) + 3) & ~3, WIN);
+        }
+        m.a = max(m.w0, 0);
+        m.b = min(m.w0 + m.nwin, nstore);
+        const bool fast = lo >= 2.0f;
+        m.gc = gg.x;
+        m.gs = gg.y;
+        m.go = gg.z;
+        const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
+        m.off = (0u - 4u * (unsigned)m.w0 - (fast ? 4u * mag : 0u)) | (fast ? 1u : 0u);
+        meta[b * VC + lane] = m;
+    }
+    __syncwarp();
+    for (int vv = 0; vv < nv; vv++) {
+        const ViewMeta m = meta[b * VC + vv];
+        if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
+        int4* w4 = reinterpret_cast<int4*>(win + (b * VC + vv) * WIN);
+        const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;
+        const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;
+        for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        for (int e = zb + lane; e < (m.nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        unsigned bytes = 0;
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[b * VC + vv];
+            if (m.b > m.a) bytes += 4u * (unsigned)(m.b - m.a);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const unsigned bar = smem_u32(&bars[b]);
+        mbar_arrive_expect_tx(bar, bytes);
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[b * VC + vv];
+            if (m.b <= m.a) continue;
+            const int* src = J.table + (size_t)(v0 + vv) * J.table_stride + m.a;
+            const unsigned dst = smem_u32(win + (b * VC + vv) * WIN + (m.a - m.w0));
+            tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
+        }
+    }
+    __syncwarp();
+    return true;
+}
+
 // One tile.  gc = chunks this CTA has run through the buffers before this tile (the phase
 // bookkeeping of a persistent CTA); returns false after a bounded wait ran out.
 template <int WX, int WY, int RX, int RY, int VC, int NB, int PAD, bool CHECKED>
@@ -431,8 +516,6 @@ __device__ __forceinline__ bool bp_ref_tile_pipe(const TileJob& J, int* smi, uns
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % WX) * 8 + (lane & 7);
     const int ty = (warp / WX) * 4 + (lane >> 3);
-    const int* tab = J.table;
-    const int nstore = PAD ? ((17 * ixdimp + 3) & ~3) : 16 * ixdimp;
     const int nviews = J.nviews;
     const int nchunks = (nviews + VC - 1) / VC;
     unsigned viol = 0;
@@ -444,78 +527,7 @@ __device__ __forceinline__ bool bp_ref_tile_pipe(const TileJob& J, int* smi, uns
 
     // warp 0: fill the buffer of chunk c (global chunk number g); false on a timeout
     auto produce = [&](int c, unsigned g) -> bool {
-        const int b = (int)(g % NB);
-        // warp-uniform verdict: every lane takes the same branch at the __syncwarp()s below
-        if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
-            return false;
-        const int v0 = c * VC;
-        const int nv = min(VC, nviews - v0);
-        if (lane < nv) {
-            const float4 gg = __ldg(J.geom + v0 + lane);
-            float lo = 3.0e38f, hi = -3.0e38f;
-#pragma unroll
-            for (int cy = 0; cy < 2; cy++) {
-                const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), gg.y), gg.z);
-#pragma unroll
-                for (int cx = 0; cx < 2; cx++) {
-                    const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), gg.x), fy);
-                    lo = fminf(lo, fx);
-                    hi = fmaxf(hi, fx);
-                }
-            }
-            const int ilo = (int)floorf(lo) - 2;
-            const int lo_a = ilo >= 0 ? (ilo & ~(Cfg::ALIGN - 1)) : -((-ilo + Cfg::ALIGN - 1) & ~(Cfg::ALIGN - 1));
-            const int ihi = (int)floorf(hi) + 3;
-            ViewMeta m;
-            if (PAD) {
-                const int hi16 = (ihi + 15) & ~15;
-                m.w0 = lo_a + lo_a / 16;
-                const int w1 = hi16 + hi16 / 16;
-                m.nwin = min(((w1 - m.w0) + 3) & ~3, WIN);
-            } else {
-                m.w0 = lo_a;
-                m.nwin = min(((ihi - lo_a) + 3) & ~3, WIN);
-            }
-            m.a = max(m.w0, 0);
-            m.b = min(m.w0 + m.nwin, nstore);
-            const bool fast = lo >= 2.0f;
-            m.gc = gg.x;
-            m.gs = gg.y;
-            m.go = gg.z;
-            const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
-            m.off = (0u - 4u * (unsigned)m.w0 - (fast ? 4u * mag : 0u)) | (fast ? 1u : 0u);
-            meta[b * VC + lane] = m;
-        }
-        __syncwarp();
-        for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[b * VC + vv];
-            if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
-            int4* w4 = reinterpret_cast<int4*>(win + (b * VC + vv) * WIN);
-            const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;
-            const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;
-            for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
-            for (int e = zb + lane; e < (m.nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
-        }
-        __syncwarp();
-        if (lane == 0) {
-            unsigned bytes = 0;
-            for (int vv = 0; vv < nv; vv++) {
-                const ViewMeta m = meta[b * VC + vv];
-                if (m.b > m.a) bytes += 4u * (unsigned)(m.b - m.a);
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const unsigned bar = smem_u32(&bars[b]);
-            mbar_arrive_expect_tx(bar, bytes);
-            for (int vv = 0; vv < nv; vv++) {
-                const ViewMeta m = meta[b * VC + vv];
-                if (m.b <= m.a) continue;
-                const int* src = tab + (size_t)(v0 + vv) * J.table_stride + m.a;
-                const unsigned dst = smem_u32(win + (b * VC + vv) * WIN + (m.a - m.w0));
-                tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
-            }
-        }
-        __syncwarp();
-        return true;
+        return pipe_fill<TX, TY, WIN, Cfg::ALIGN, VC, NB, PAD>(J, win, meta, bars, c, g, lane);
     };
 
     int acc[RY][RX];
@@ -648,6 +660,362 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_pipe_persistent(c
         const TileJob J = jobs[it];
         const bool tok = bp_ref_tile_pipe<WX, WY, RX, RY, VC, NB, PAD, false>(J, smi, gc, nullptr);
         if (__syncthreads_or(!tok)) return;   // the CTA leaves together after a timeout
+        gc += (unsigned)((J.nviews + VC - 1) / VC);
+    }
+}
+
+// ---- warp-specialised producer, ray-aligned lane footprints ------------------------------------
+// Two changes to the warp-decoupled pipeline above, each bit-identical.
+//
+// Producer warp.  A ninth warp only fills window buffers: it waits for a buffer's empty barrier,
+// records the views' windows and issues their TMA copies, so the eight consumer warps never wait
+// for a fill that a busy consumer has not issued yet, and all of them do the same work.
+//
+// Ray-aligned footprints (NQ > 0).  A warp's 32 lookups of one view cost one shared-memory
+// wavefront per distinct word in its busiest bank.  A compact 8x4 pixel block spreads the lanes'
+// indices over ~100 words (2.3 wavefronts per gather).  Here every register of a warp holds 32
+// pixels along one line of the view's iso-index direction (x*fcos + y*fsin = const), so its
+// indices fall within a few dozen consecutive words (~1.3 wavefronts).
+// Layouts: a 64x64 tile, 8 consumer warps, 16 accumulators per thread in slots s = 2q + p
+// (q 0..7, p 0..1); w = warp, j = lane.  A regime is an orientation and a shear k in [-NQ, NQ]:
+//     V (|fcos| >= |fsin|):  x = (w + sh(j) + 8q) mod 64,  y = j + 32p,   sh(j) = round(j k / NQ)
+//     H (|fsin| >  |fcos|):  x = j + 32p,  y = (w + sh(j) + 8q) mod 64
+// Each maps (w, j, q, p) one-to-one onto the tile, and a thread's 16 pixels are 8 sheared x 2
+// fixed coordinates, so the per-view products cost 8 + 2*2 (V) or 2 + 8*2 (H) FP32 operations.
+// The regime of a chunk follows from the geometry of its first view (every consumer computes
+// the same value).  When it changes, the accumulators move through the buffer just consumed,
+// between barriers of the consumer warps: written at (slot, thread), read back from the old owner
+// of each new pixel.  Two layouts of the same orientation give each pixel the same lane in both,
+// so that exchange is free of bank conflicts.  Every pixel still sums the same int32 entries over
+// the same views.
+//
+// Failure protocol.  The consumer barriers of an exchange need all eight consumer warps, so a
+// warp whose bounded wait ran out does not leave the loop: it raises the CTA's abort word (the
+// others then skip their waits), skips the rest of its work, and the consumers leave together at
+// the next exchange or after the last chunk; the producer stops at the abort word or at its own
+// bounded wait.  All 288 threads then meet at one block barrier.
+__device__ __forceinline__ bool consumers_bar_or(bool pred) {   // named barrier 1: the 256 consumers
+    unsigned r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 256, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((unsigned)pred)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void consumers_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+template <int VC, int NB, int PAD>
+struct WsCfg {
+    using Pipe = PipeCfg<2, 4, 4, 4, VC, NB, PAD>;   // 64x64 tile: the same windows and records
+    static constexpr int NT = 288;                   // 8 consumer warps + 1 producer warp
+    static constexpr int TX = Pipe::TX, TY = Pipe::TY, ALIGN = Pipe::ALIGN, WIN = Pipe::WIN;
+    static constexpr int META_OFF = Pipe::META_OFF, BAR_OFF = Pipe::BAR_OFF;
+    static constexpr int ABORT_OFF = BAR_OFF + 4 * NB;   // words: after full[NB], empty[NB]
+    static constexpr size_t SMEM = (size_t)ABORT_OFF * 4 + 16;
+    static constexpr bool EXCHANGE_FITS = VC * WIN >= 16 * 256;   // one buffer holds the exchange
+    static_assert(TX == 64 && TY == 64 && Pipe::NT == 256, "8 consumer warps tile 64x64 pixels");
+};
+
+// regime = orientation (bit 0: H) | (k + NQ) << 1, from a view's fcos, fsin; any value gives the
+// same slice, it only has to be the same in every consumer thread (a pure function of the inputs)
+template <int NQ>
+__device__ __forceinline__ int ray_regime(float gc, float gs) {
+    const bool h = fabsf(gs) > fabsf(gc);
+    const float t = h ? __fdividef(-gc, gs) : __fdividef(-gs, gc);   // |t| <= 1
+    int k = __float2int_rn(t * (float)NQ);                             // NaN (fcos = fsin = 0) gives 0
+    k = max(-NQ, min(NQ, k));
+    return (h ? 1 : 0) | ((k + NQ) << 1);
+}
+// sh(j) = round(j k / NQ), halves up (the numerator is kept positive for the division)
+template <int NQ>
+__device__ __forceinline__ int ray_shift(int j, int regime) {
+    constexpr int D = NQ > 0 ? 2 * NQ : 1;   // (NQ = 0, the compact layout, never shears)
+    const int k = (regime >> 1) - NQ;
+    return NQ > 0 ? (2 * j * k + NQ + 128 * NQ) / D - 64 : 0;
+}
+// the thread's sheared (lin) and fixed (fix) absolute pixel coordinates under a regime
+template <int NQ>
+__device__ __forceinline__ void ray_coords(int regime, int X0, int Y0, int warp, int lane, float (&lin)[8],
+                                           float (&fix)[2]) {
+    const int sh = ray_shift<NQ>(lane, regime);
+    const int lb = (regime & 1) ? Y0 : X0, fb = (regime & 1) ? X0 : Y0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) lin[q] = (float)(lb + ((warp + sh + 8 * q) & 63));
+#pragma unroll
+    for (int p = 0; p < 2; p++) fix[p] = (float)(fb + lane + 32 * p);
+}
+
+// acc[s] += the table entry of slot s's pixel, for the views of one staged chunk.  fx[s] is
+// fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of that pixel (formed by the caller's functor).
+template <int VC, int WIN, int PAD, bool CHECKED, typename FX>
+__device__ __forceinline__ void ws_gather(int (&acc)[16], const int* win, const ViewMeta* meta, int b, int vv,
+                                          unsigned& viol, FX fx_of) {
+    const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+    const unsigned offb = __float_as_uint(gm.w);
+    const unsigned base = smem_u32(win + (b * VC + vv) * WIN) + (offb & ~3u);
+    int cw0 = 0, cnw = 0;
+    if (CHECKED) {
+        cw0 = meta[b * VC + vv].w0;
+        cnw = meta[b * VC + vv].nwin;
+    }
+    if (offb & 1u) {
+#pragma unroll
+        for (int s = 0; s < 16; s++) {
+            const float fx = fx_of(s, gm);
+            const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
+            const unsigned st = PAD ? bits + (bits >> 4) : bits;
+            if (CHECKED) {
+                const int v = (int)(bits - kMagicBits);
+                const int sw = PAD ? v + (v >> 4) : v;
+                if (fx < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+            }
+            acc[s] += lds_s32(base + 4u * st);
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < 16; s++) {
+            const float fx = fx_of(s, gm);
+            const int v = __float2int_rz(fx);
+            const int sw = PAD ? v + (v >> 4) : v;
+            if (CHECKED) {
+                if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+            }
+            acc[s] += lds_s32(base + 4u * (unsigned)sw);
+        }
+    }
+}
+
+// one chunk of views: NQ == 0 compact blocks (colf/rowf in lin[0..3] / lin[4..7]), else the
+// ray layout of orientation O
+template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED>
+__device__ __forceinline__ void ws_consume(int (&acc)[16], const float (&lin)[8], const float (&fix)[2],
+                                           const int* win, const ViewMeta* meta, int b, int nv, unsigned& viol) {
+    for (int vv = 0; vv < nv; vv++) {
+        const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+        if (NQ == 0) {   // slot s = 4 r + c: x = lin[c], y = lin[4 + r]
+            float xv[4], yv[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) xv[c] = fmulr(lin[c], g.x);
+#pragma unroll
+            for (int r = 0; r < 4; r++) yv[r] = faddr(fmulr(lin[4 + r], g.y), g.z);
+            ws_gather<VC, WIN, PAD, CHECKED>(acc, win, meta, b, vv, viol,
+                                             [&](int s, float4) { return faddr(xv[s & 3], yv[s >> 2]); });
+        } else if (O == 0) {   // V: x = lin[q], y = fix[p]
+            float xs[8], ys[2];
+#pragma unroll
+            for (int q = 0; q < 8; q++) xs[q] = fmulr(lin[q], g.x);
+#pragma unroll
+            for (int p = 0; p < 2; p++) ys[p] = faddr(fmulr(fix[p], g.y), g.z);
+            ws_gather<VC, WIN, PAD, CHECKED>(acc, win, meta, b, vv, viol,
+                                             [&](int s, float4) { return faddr(xs[s >> 1], ys[s & 1]); });
+        } else {   // H: x = fix[p], y = lin[q]
+            float xs[2], ys[8];
+#pragma unroll
+            for (int p = 0; p < 2; p++) xs[p] = fmulr(fix[p], g.x);
+#pragma unroll
+            for (int q = 0; q < 8; q++) ys[q] = faddr(fmulr(lin[q], g.y), g.z);
+            ws_gather<VC, WIN, PAD, CHECKED>(acc, win, meta, b, vv, viol,
+                                             [&](int s, float4) { return faddr(xs[s & 1], ys[s >> 1]); });
+        }
+    }
+}
+
+template <int VC, int NB, int PAD>
+__device__ __forceinline__ void ws_init(int* smi) {
+    using Cfg = WsCfg<VC, NB, PAD>;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < NB; b++) {
+            mbar_init(smem_u32(&bars[b]), 1);
+            mbar_init(smem_u32(&bars[NB + b]), 8);   // one arrival per consumer warp
+        }
+        smi[Cfg::ABORT_OFF] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+}
+
+// One 64x64 tile; gc as in bp_ref_tile_pipe.  Returns false (for the whole CTA) after a bounded
+// wait ran out.  Warps 0-7 consume, warp 8 produces.
+template <int VC, int NB, int PAD, int NQ, bool CHECKED>
+__device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter) {
+    using Cfg = WsCfg<VC, NB, PAD>;
+    static_assert(NQ == 0 || Cfg::EXCHANGE_FITS, "the accumulator exchange needs 4096 words in one buffer");
+    constexpr int WIN = Cfg::WIN;
+    int* win = smi;                                                     // [NB][VC][WIN]
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(smi + Cfg::META_OFF);  // [NB][VC]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);   // full[NB], empty[NB]
+    volatile int* abortw = smi + Cfg::ABORT_OFF;
+    const int ixdimp = J.ixdimp;
+    const int X0 = J.X0, Y0 = J.Y0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nviews = J.nviews;
+    const int nchunks = (nviews + VC - 1) / VC;
+    bool failed = false;   // warp-uniform
+    int produced = 0;      // producer: chunks of this tile whose fill has been issued
+    if (warp == 8) {
+        for (; produced < nchunks; produced++) {
+            if (__any_sync(0xffffffffu, *abortw != 0)) {
+                failed = true;
+                break;
+            }
+            if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD>(J, win, meta, bars, produced, gc + (unsigned)produced,
+                                                                 lane)) {
+                failed = true;
+                if (lane == 0) *abortw = 1;
+                break;
+            }
+        }
+    } else {
+        unsigned viol = 0;
+        int acc[16];
+#pragma unroll
+        for (int s = 0; s < 16; s++) acc[s] = 0;
+        float lin[8], fix[2];
+        int regime = 0;
+        float2 gnext = make_float2(0.0f, 0.0f);   // fcos, fsin of the first view of chunk k + 1
+        if (NQ > 0) {
+            if (nchunks > 0) {
+                const float4 g0 = __ldg(J.geom);
+                regime = ray_regime<NQ>(g0.x, g0.y);
+            }
+            if (nchunks > 1) {
+                const float4 g1 = __ldg(J.geom + VC);
+                gnext = make_float2(g1.x, g1.y);
+            }
+            ray_coords<NQ>(regime, X0, Y0, warp, lane, lin, fix);
+        } else {
+            const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
+#pragma unroll
+            for (int c = 0; c < 4; c++) lin[c] = (float)(X0 + tx + 16 * c);
+#pragma unroll
+            for (int r = 0; r < 4; r++) lin[4 + r] = (float)(Y0 + ty + 16 * r);
+            fix[0] = fix[1] = 0.0f;
+        }
+        for (int k = 0; k < nchunks; k++) {
+            const unsigned g = gc + (unsigned)k;
+            const int b = (int)(g % NB);
+            if (!failed && __any_sync(0xffffffffu, *abortw != 0)) failed = true;
+            if (!failed && !__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) failed = true;
+            if (!failed) {
+                const int nv = min(VC, nviews - k * VC);
+                if (NQ == 0 || !(regime & 1)) ws_consume<NQ, 0, VC, WIN, PAD, CHECKED>(acc, lin, fix, win, meta, b, nv, viol);
+                else ws_consume<NQ, 1, VC, WIN, PAD, CHECKED>(acc, lin, fix, win, meta, b, nv, viol);
+            } else if (lane == 0) {
+                *abortw = 1;
+            }
+            if (NQ > 0) {
+                // the next chunk's regime (the same value in every consumer thread)
+                int next = regime;
+                if (k + 1 < nchunks) {
+                    next = ray_regime<NQ>(gnext.x, gnext.y);
+                    if (k + 2 < nchunks) {
+                        const float4 gn = __ldg(J.geom + (size_t)(k + 2) * VC);
+                        gnext = make_float2(gn.x, gn.y);
+                    }
+                }
+                if (next != regime) {
+                    // every consumer is done reading buffer b and none has released it: exchange
+                    if (consumers_bar_or(failed)) {
+                        failed = true;
+                        break;
+                    }
+                    int* xs = win + b * VC * WIN;   // [16 slots][256 threads]
+#pragma unroll
+                    for (int s = 0; s < 16; s++) xs[s * 256 + tid] = acc[s];
+                    consumers_bar();
+                    const int on = next & 1, oo = regime & 1;
+                    const int shn = ray_shift<NQ>(lane, next);
+#pragma unroll
+                    for (int q = 0; q < 8; q++)
+#pragma unroll
+                        for (int p = 0; p < 2; p++) {
+                            const int u = (warp + shn + 8 * q) & 63, f = lane + 32 * p;   // new layout
+                            const int xr = on ? f : u, yr = on ? u : f;
+                            const int a = oo ? xr : yr, c = oo ? yr : xr;                  // old fixed / sheared
+                            const int jj = a & 31, pp = a >> 5;
+                            const int m = (c - ray_shift<NQ>(jj, regime)) & 63;             // old w + 8 q
+                            acc[2 * q + p] = xs[((m >> 3) * 2 + pp) * 256 + (m & 7) * 32 + jj];
+                        }
+                    regime = next;
+                    ray_coords<NQ>(regime, X0, Y0, warp, lane, lin, fix);
+                    // these generic accesses come before the next TMA fill of buffer b
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+            }
+            if (!failed) {
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
+            }
+        }
+        if (!failed) {
+            if (CHECKED && viol) atomicAdd(status_counter, viol);
+            int* out = J.out;
+            const int sh = NQ > 0 ? ray_shift<NQ>(lane, regime) : 0;
+            const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
+#pragma unroll
+            for (int s = 0; s < 16; s++) {
+                int x, y;
+                if (NQ == 0) {
+                    x = X0 + tx + 16 * (s & 3);
+                    y = Y0 + ty + 16 * (s >> 2);
+                } else {
+                    const int u = (warp + sh + 8 * (s >> 1)) & 63, f = lane + 32 * (s & 1);
+                    x = X0 + ((regime & 1) ? f : u);
+                    y = Y0 + ((regime & 1) ? u : f);
+                }
+                if (x < ixdimp && y < ixdimp) out[(size_t)y * ixdimp + x] = acc[s];
+            }
+        }
+    }
+    if (__syncthreads_or(failed)) {
+        if (tid == 0) atomicOr(&g_kernel_status, 1u);
+        // the producer's fills up to chunk `produced`: give them a bounded chance to land before
+        // the CTA can leave
+        if (warp == 8) {
+            for (int c = produced > NB ? produced - NB : 0; c < produced; c++) {
+                const unsigned g = gc + (unsigned)c;
+                mbar_wait_bounded(smem_u32(&bars[g % NB]), (g / NB) & 1u);
+            }
+        }
+        return false;
+    }
+    return true;
+}
+
+template <int VC, int NB, int PAD, int NQ, int MINB, bool CHECKED>
+__global__ void __launch_bounds__(288, MINB) k_bp_ref_ws(BackprojLaunch p) {
+    extern __shared__ __align__(128) int smi[];
+    ws_init<VC, NB, PAD>(smi);
+    __syncthreads();
+    const int tiles_x = (p.ixdimp + 63) / 64;
+    TileJob J;
+    J.table = p.table + (size_t)blockIdx.y * p.slice_table_stride;
+    J.geom = p.geom + (size_t)blockIdx.y * p.geom_slice_stride;
+    J.out = static_cast<int*>(p.out) + (size_t)blockIdx.y * p.out_slice_stride;
+    J.table_stride = p.table_stride;
+    J.nviews = p.nviews;
+    J.ixdimp = p.ixdimp;
+    J.X0 = (blockIdx.x % tiles_x) * 64;
+    J.Y0 = (blockIdx.x / tiles_x) * 64;
+    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED>(J, smi, 0u, p.status_counter);
+}
+
+template <int VC, int NB, int PAD, int NQ, int MINB>
+__global__ void __launch_bounds__(288, MINB) k_bp_ref_ws_persistent(const TileJob* jobs, int njobs,
+                                                                    unsigned* counter) {
+    extern __shared__ __align__(128) int smi[];
+    __shared__ int s_item;
+    ws_init<VC, NB, PAD>(smi);
+    unsigned gc = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= njobs) break;
+        const TileJob J = jobs[it];
+        if (!bp_ref_tile_ws<VC, NB, PAD, NQ, false>(J, smi, gc, nullptr)) return;   // CTA-uniform
         gc += (unsigned)((J.nviews + VC - 1) / VC);
     }
 }
@@ -1110,6 +1478,9 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //     9, 10, 11: 64x64 OTF without block barriers (warp-decoupled pipeline) with 3x3, 4x2, 2x4
 //        buffers x views per chunk;  12: 128x128, 512 threads, 3 buffers x 4 views;
 //     13: 128x64, 512 threads, 2 x 4;  14, 15: 64x64, 2 buffers x 5 / 6 views, 3 CTAs/SM
+//     16: 64x64, 8 consumer warps + 1 producer warp, ray-aligned lane footprints (shear steps
+//         of 1/8), 2 buffers x 6 views, 3 CTAs/SM;  17: the same with compact 8x4 lane blocks,
+//         2 buffers x 4 views, 4 CTAs/SM
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -1119,7 +1490,7 @@ static int env_int(const char* name, int dflt) {
 }
 static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
-    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 11);
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 16);
     if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
 int ref_table_fmt() {
@@ -1164,6 +1535,15 @@ static cudaError_t go_pipe(const BackprojLaunch& p, cudaStream_t s, bool checked
     return launch_k(k_bp_ref_pipe<WX, WY, RX, RY, VC, NB, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
+template <int VC, int NB, int PAD, int NQ, int MINB>
+static cudaError_t go_ws(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    using Cfg = WsCfg<VC, NB, PAD>;
+    const int tiles = ((p.ixdimp + 63) / 64) * ((p.ixdimp + 63) / 64);
+    dim3 grid(tiles, p.nslices);
+    if (checked) return launch_k(k_bp_ref_ws<VC, NB, PAD, NQ, MINB, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    return launch_k(k_bp_ref_ws<VC, NB, PAD, NQ, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
+}
+
 template <int WX, int WY, int RX, int RY, int VC, int MINB>
 static cudaError_t go_pair(const BackprojLaunch& p, cudaStream_t s, bool checked) {
     using Cfg = PairCfg<WX, WY, RX, RY, VC>;
@@ -1191,6 +1571,8 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 13: return go_pipe<4, 4, 4, 4, 4, 2, PAD, 2>(p, s, checked);
     case 14: return go_pipe<2, 4, 4, 4, 5, 2, PAD, 3>(p, s, checked);
     case 15: return go_pipe<2, 4, 4, 4, 6, 2, PAD, 3>(p, s, checked);
+    case 16: return go_ws<6, 2, PAD, 8, 3>(p, s, checked);
+    case 17: return go_ws<4, 2, PAD, 0, 4>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -1245,6 +1627,25 @@ static cudaError_t go_pipe_persistent(const TileJob* jobs, int njobs, unsigned* 
     return cudaGetLastError();
 }
 
+template <int VC, int NB, int PAD, int NQ, int MINB>
+static cudaError_t go_ws_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
+    using Cfg = WsCfg<VC, NB, PAD>;
+    auto kern = k_bp_ref_ws_persistent<VC, NB, PAD, NQ, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::NT, Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int grid = sms * per_sm;
+    if (grid > njobs) grid = njobs;
+    if (grid < 1) return cudaSuccess;
+    kern<<<grid, Cfg::NT, Cfg::SMEM, s>>>(jobs, njobs, counter);
+    return cudaGetLastError();
+}
+
 static void persistent_shape(int variant, int* tx, int* ty) {
     switch (variant) {
     case 0: case 2: case 7: case 12: *tx = 128; *ty = 128; break;
@@ -1274,6 +1675,8 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 13: return go_pipe_persistent<4, 4, 4, 4, 4, 2, PAD, 2>(jobs, njobs, counter, s);
     case 14: return go_pipe_persistent<2, 4, 4, 4, 5, 2, PAD, 3>(jobs, njobs, counter, s);
     case 15: return go_pipe_persistent<2, 4, 4, 4, 6, 2, PAD, 3>(jobs, njobs, counter, s);
+    case 16: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
+    case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
 }
@@ -1333,7 +1736,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 15 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 17 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;

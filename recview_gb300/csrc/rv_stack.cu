@@ -701,7 +701,7 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
     // keeps the fastest for the captured graph
     if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
-    const int cands[] = {11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
+    const int cands[] = {16, 17, 11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
     float best = 3.0e38f;
     int bestv = q->variant;
     for (int v : cands) {
