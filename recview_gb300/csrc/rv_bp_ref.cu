@@ -37,6 +37,7 @@
 namespace rv {
 
 __device__ unsigned int g_kernel_status = 0;   // bit 0: an mbarrier wait ran out
+static int env_int(const char* name, int dflt);  // tuning overrides from the environment
 
 constexpr unsigned kMagicBits = 0x4B000000u;   // bit pattern of 2^23
 
@@ -1057,6 +1058,7 @@ __device__ __forceinline__ float2 lin_pair(unsigned addr) {
 
 template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE>
 struct LinCfg {
+    static constexpr int VC_ = VC, NB_ = NB, RX_ = RX, RY_ = RY;
     static constexpr int NT = 32 * WX * WY, NW = NT / 32;
     static constexpr int GX = 8 * WX, GY = 4 * WY, TX = GX * RX, TY = GY * RY;
     static constexpr int ES = LinElem<MODE>::ES;
@@ -1066,12 +1068,147 @@ struct LinCfg {
     static constexpr int META_OFF = NB * VC * WIN_BYTES;                  // bytes
     static constexpr int BAR_OFF = META_OFF + NB * VC * (int)sizeof(ViewMeta);
     static constexpr size_t SMEM = (size_t)BAR_OFF + (size_t)2 * NB * 8;
+    static constexpr size_t SMEM_WS = SMEM + 16;   // + the abort word of the producer-warp form
 };
 
+// Per-CTA state of a LIN tile: the slice's pair rows, scales and FP64 geometry, and the tile.
+struct LinTile {
+    const unsigned char* rows;
+    const float* scales;
+    const LinGeom* geom;
+    int X0, Y0, nviews, ixdimp;
+    long long row_stride;
+};
+__device__ __forceinline__ LinTile lin_tile(const BackprojLaunch& p, int TX, int TY, int ES) {
+    LinTile t;
+    const int tiles_x = (p.ixdimp + TX - 1) / TX;
+    t.X0 = (blockIdx.x % tiles_x) * TX;
+    t.Y0 = (blockIdx.x / tiles_x) * TY;
+    t.rows = static_cast<const unsigned char*>(p.rows16) + (size_t)blockIdx.y * p.slice_row_stride * ES;
+    t.scales = p.row_scale ? p.row_scale + (size_t)blockIdx.y * p.nviews : nullptr;
+    t.geom = p.geom64 + (size_t)blockIdx.y * p.geom_slice_stride;
+    t.nviews = p.nviews;
+    t.ixdimp = p.ixdimp;
+    t.row_stride = p.row_stride;
+    return t;
+}
+
+// One warp fills buffer c % NB with the pair windows of chunk c (views c*VC ..) once that
+// buffer's empty barrier shows every consumer is done with it; false (warp-uniform) when that
+// bounded wait ran out.
+template <typename Cfg>
+__device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, ViewMeta* meta, uint64_t* bars, int c,
+                                         int lane) {
+    constexpr int NB = Cfg::NB_, VC = Cfg::VC_, TX = Cfg::TX, TY = Cfg::TY, WINP = Cfg::WINP, ES = Cfg::ES;
+    const unsigned g = (unsigned)c;
+    const int b = (int)(g % NB);
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
+        return false;
+    const int v0 = c * VC;
+    const int nv = min(VC, T.nviews - v0);
+    if (lane < nv) {
+        const LinGeom gg = T.geom[v0 + lane];
+        // u at the tile origin in FP64 (two FMAs); the tile's lowest u adds the negative parts of
+        // the tile's extent, which FP32 gives well inside the window's 2-pixel margin
+        const double base = fma((double)T.X0, gg.c, fma((double)T.Y0, gg.s, gg.off));
+        const float lo = (float)base + fminf(0.0f, (float)(TX - 1) * (float)gg.c) + fminf(0.0f, (float)(TY - 1) * (float)gg.s);
+        const int ilo = (int)floorf(lo) - 2;
+        const int w0 = ilo >= 0 ? (ilo & ~3) : -((-ilo + 3) & ~3);
+        ViewMeta m;
+        m.w0 = w0;
+        m.nwin = WINP;
+        m.a = max(w0, 0);
+        m.b = min(w0 + WINP, (T.ixdimp + 3) & ~3);
+        m.gc = (float)gg.c;
+        m.gs = (float)gg.s;
+        m.go = (float)(base - (double)w0);   // window-relative u at the tile origin
+        m.off = __float_as_uint(T.scales ? T.scales[v0 + lane] : 1.0f);
+        meta[b * VC + lane] = m;
+    }
+    __syncwarp();
+    for (int vv = 0; vv < nv; vv++) {
+        const ViewMeta m = meta[b * VC + vv];
+        if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
+        int4* w4 = reinterpret_cast<int4*>(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES);
+        const int bytes_a = (m.b > m.a ? m.a - m.w0 : m.nwin) * ES, bytes_b = (m.b > m.a ? m.b - m.w0 : m.nwin) * ES;
+        for (int e = lane; e < bytes_a / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        for (int e = bytes_b / 16 + lane; e < Cfg::WIN_BYTES / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        unsigned bytes = 0;
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[b * VC + vv];
+            if (m.b > m.a) bytes += (unsigned)((m.b - m.a) * ES);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const unsigned bar = smem_u32(&bars[b]);
+        mbar_arrive_expect_tx(bar, bytes);
+        for (int vv = 0; vv < nv; vv++) {
+            const ViewMeta m = meta[b * VC + vv];
+            if (m.b <= m.a) continue;
+            const unsigned char* src = T.rows + ((size_t)(v0 + vv) * T.row_stride + m.a) * ES;
+            const unsigned dst = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
+            tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
+        }
+    }
+    __syncwarp();
+    return true;
+}
+
+// acc += the interpolated, scaled row value of every pixel of the thread, for the nv views of
+// buffer b
+template <typename Cfg, int MODE>
+__device__ __forceinline__ void lin_consume(float (&acc)[Cfg::RY_][Cfg::RX_], const float (&colf)[Cfg::RX_],
+                                            const float (&rowf)[Cfg::RY_], const unsigned char* smb,
+                                            const ViewMeta* meta, int b, int nv) {
+    constexpr int RX = Cfg::RX_, RY = Cfg::RY_, VC = Cfg::VC_, ES = Cfg::ES;
+    for (int vv = 0; vv < nv; vv++) {
+        const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+        const float sc = __uint_as_float(__float_as_uint(gm.w));
+        float xv[RX], yv[RY];
+#pragma unroll
+        for (int c = 0; c < RX; c++) xv[c] = colf[c] * gm.x;
+#pragma unroll
+        for (int r = 0; r < RY; r++) yv[r] = fmaf(rowf[r], gm.y, gm.z);
+        // address of pair 0 minus the 2^23 bit pattern (unsigned wrap-around)
+        const unsigned base = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES) - (unsigned)ES * kMagicBits;
+#pragma unroll
+        for (int r = 0; r < RY; r++)
+#pragma unroll
+            for (int c = 0; c < RX; c++) {
+                const float u = xv[c] + yv[r];                       // >= 1.9 inside the window
+                const float t = __fadd_rz(u, 8388608.0f);
+                const unsigned bits = __float_as_uint(t);
+                const float f = u - (t - 8388608.0f);
+                const float2 q = lin_pair<MODE>(base + (unsigned)ES * bits);
+                const float v = fmaf(f, q.y, q.x);
+                if (MODE == RV_MODE_LIN) acc[r][c] += v;
+                else acc[r][c] = fmaf(v, sc, acc[r][c]);
+            }
+    }
+}
+
+template <typename Cfg>
+__device__ __forceinline__ void lin_store(const BackprojLaunch& p, const LinTile& T, const float (&acc)[Cfg::RY_][Cfg::RX_],
+                                          int tx, int ty) {
+    float* out = static_cast<float*>(p.out) + (size_t)blockIdx.y * p.out_slice_stride;
+#pragma unroll
+    for (int r = 0; r < Cfg::RY_; r++) {
+        const int y = T.Y0 + ty + Cfg::GY * r;
+        if (y >= T.ixdimp) continue;
+#pragma unroll
+        for (int c = 0; c < Cfg::RX_; c++) {
+            const int x = T.X0 + tx + Cfg::GX * c;
+            if (x < T.ixdimp) out[(size_t)y * T.ixdimp + x] = acc[r][c];
+        }
+    }
+}
+
+// Warp 0 produces as well as consumes (the layout of the REF pipeline's variant 11).
 template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE, int MINB>
 __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaunch p) {
     using Cfg = LinCfg<WX, WY, RX, RY, VC, NB, MODE>;
-    constexpr int TX = Cfg::TX, TY = Cfg::TY, WINP = Cfg::WINP, ES = Cfg::ES;
     extern __shared__ __align__(128) unsigned char smb[];
     ViewMeta* meta = reinterpret_cast<ViewMeta*>(smb + Cfg::META_OFF);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smb + Cfg::BAR_OFF);
@@ -1084,16 +1221,9 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const int ixdimp = p.ixdimp;
-    const int tiles_x = (ixdimp + TX - 1) / TX;
-    const int X0 = (blockIdx.x % tiles_x) * TX, Y0 = (blockIdx.x / tiles_x) * TY;
-    const int slice = blockIdx.y;
+    const LinTile T = lin_tile(p, Cfg::TX, Cfg::TY, Cfg::ES);
     const int tx = (warp % WX) * 8 + (lane & 7), ty = (warp / WX) * 4 + (lane >> 3);
-    const unsigned char* rows = static_cast<const unsigned char*>(p.rows16) + (size_t)slice * p.slice_row_stride * ES;
-    const float* scales = p.row_scale ? p.row_scale + (size_t)slice * p.nviews : nullptr;
-    const LinGeom* geom = p.geom64 + (size_t)slice * p.geom_slice_stride;
-    const int nviews = p.nviews;
-    const int nchunks = (nviews + VC - 1) / VC;
+    const int nchunks = (T.nviews + VC - 1) / VC;
     // coordinates relative to the tile origin (small, so FP32 keeps ~1e-6 px); the tile-origin term
     // of each view comes from the FP64 geometry
     float colf[RX], rowf[RY];
@@ -1101,64 +1231,6 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
     for (int c = 0; c < RX; c++) colf[c] = (float)(tx + Cfg::GX * c);
 #pragma unroll
     for (int r = 0; r < RY; r++) rowf[r] = (float)(ty + Cfg::GY * r);
-
-    auto produce = [&](int c) -> bool {
-        const unsigned g = (unsigned)c;
-        const int b = (int)(g % NB);
-        if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
-            return false;
-        const int v0 = c * VC;
-        const int nv = min(VC, nviews - v0);
-        if (lane < nv) {
-            const LinGeom gg = geom[v0 + lane];
-            // u at the tile origin in FP64 (two FMAs); the tile's lowest u adds the negative parts of
-            // the tile's extent, which FP32 gives well inside the window's 2-pixel margin
-            const double base = fma((double)X0, gg.c, fma((double)Y0, gg.s, gg.off));
-            const float lo = (float)base + fminf(0.0f, (float)(TX - 1) * (float)gg.c) + fminf(0.0f, (float)(TY - 1) * (float)gg.s);
-            const int ilo = (int)floorf(lo) - 2;
-            const int w0 = ilo >= 0 ? (ilo & ~3) : -((-ilo + 3) & ~3);
-            ViewMeta m;
-            m.w0 = w0;
-            m.nwin = WINP;
-            m.a = max(w0, 0);
-            m.b = min(w0 + WINP, (ixdimp + 3) & ~3);
-            m.gc = (float)gg.c;
-            m.gs = (float)gg.s;
-            m.go = (float)(base - (double)w0);   // window-relative u at the tile origin
-            m.off = __float_as_uint(scales ? scales[v0 + lane] : 1.0f);
-            meta[b * VC + lane] = m;
-        }
-        __syncwarp();
-        for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[b * VC + vv];
-            if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
-            int4* w4 = reinterpret_cast<int4*>(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES);
-            const int bytes_a = (m.b > m.a ? m.a - m.w0 : m.nwin) * ES, bytes_b = (m.b > m.a ? m.b - m.w0 : m.nwin) * ES;
-            for (int e = lane; e < bytes_a / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
-            for (int e = bytes_b / 16 + lane; e < Cfg::WIN_BYTES / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
-        }
-        __syncwarp();
-        if (lane == 0) {
-            unsigned bytes = 0;
-            for (int vv = 0; vv < nv; vv++) {
-                const ViewMeta m = meta[b * VC + vv];
-                if (m.b > m.a) bytes += (unsigned)((m.b - m.a) * ES);
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const unsigned bar = smem_u32(&bars[b]);
-            mbar_arrive_expect_tx(bar, bytes);
-            for (int vv = 0; vv < nv; vv++) {
-                const ViewMeta m = meta[b * VC + vv];
-                if (m.b <= m.a) continue;
-                const unsigned char* src = rows + ((size_t)(v0 + vv) * p.row_stride + m.a) * ES;
-                const unsigned dst = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
-                tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
-            }
-        }
-        __syncwarp();
-        return true;
-    };
-
     float acc[RY][RX];
 #pragma unroll
     for (int r = 0; r < RY; r++)
@@ -1168,40 +1240,16 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
     int produced = 0;
     if (warp == 0)
         for (; produced < nchunks && produced < NB - 1; produced++)
-            if (!produce(produced)) { ok = false; break; }
+            if (!lin_fill<Cfg>(T, smb, meta, bars, produced, lane)) { ok = false; break; }
     for (int k = 0; ok && k < nchunks; k++) {
         if (warp == 0 && produced < nchunks) {
-            if (!produce(produced)) { ok = false; break; }
+            if (!lin_fill<Cfg>(T, smb, meta, bars, produced, lane)) { ok = false; break; }
             produced++;
         }
         const unsigned g = (unsigned)k;
         const int b = (int)(g % NB);
         if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) { ok = false; break; }
-        const int nv = min(VC, nviews - k * VC);
-        for (int vv = 0; vv < nv; vv++) {
-            const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
-            const float sc = __uint_as_float(__float_as_uint(gm.w));
-            float xv[RX], yv[RY];
-#pragma unroll
-            for (int c = 0; c < RX; c++) xv[c] = colf[c] * gm.x;
-#pragma unroll
-            for (int r = 0; r < RY; r++) yv[r] = fmaf(rowf[r], gm.y, gm.z);
-            // address of pair 0 minus the 2^23 bit pattern (unsigned wrap-around)
-            const unsigned base = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES) - (unsigned)ES * kMagicBits;
-#pragma unroll
-            for (int r = 0; r < RY; r++)
-#pragma unroll
-                for (int c = 0; c < RX; c++) {
-                    const float u = xv[c] + yv[r];                       // >= 1.9 inside the window
-                    const float t = __fadd_rz(u, 8388608.0f);
-                    const unsigned bits = __float_as_uint(t);
-                    const float f = u - (t - 8388608.0f);
-                    const float2 q = lin_pair<MODE>(base + (unsigned)ES * bits);
-                    const float v = fmaf(f, q.y, q.x);
-                    if (MODE == RV_MODE_LIN) acc[r][c] += v;
-                    else acc[r][c] = fmaf(v, sc, acc[r][c]);
-                }
-        }
+        lin_consume<Cfg, MODE>(acc, colf, rowf, smb, meta, b, min(VC, T.nviews - k * VC));
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
     }
@@ -1212,16 +1260,77 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
                 mbar_wait_bounded(smem_u32(&bars[(unsigned)c % NB]), ((unsigned)c / NB) & 1u);
         return;
     }
-    float* out = static_cast<float*>(p.out) + (size_t)slice * p.out_slice_stride;
-#pragma unroll
-    for (int r = 0; r < RY; r++) {
-        const int y = Y0 + ty + Cfg::GY * r;
-        if (y >= ixdimp) continue;
-#pragma unroll
-        for (int c = 0; c < RX; c++) {
-            const int x = X0 + tx + Cfg::GX * c;
-            if (x < ixdimp) out[(size_t)y * ixdimp + x] = acc[r][c];
+    lin_store<Cfg>(p, T, acc, tx, ty);
+}
+
+// A ninth warp only produces (as the REF kernel's variant 16); the eight consumer warps do the
+// same work and never wait for a fill a busy consumer has not issued.  A consumer whose bounded
+// wait ran out raises the abort word and leaves its loop (the consumers share no barrier here);
+// all 288 threads meet at one block barrier at the end.
+template <int VC, int NB, int MODE, int MINB>
+__global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p) {
+    using Cfg = LinCfg<2, 4, 4, 4, VC, NB, MODE>;
+    static_assert(Cfg::NT == 256, "8 consumer warps");
+    constexpr int ABORT_OFF = Cfg::BAR_OFF + 2 * NB * 8;   // bytes
+    extern __shared__ __align__(128) unsigned char smb[];
+    ViewMeta* meta = reinterpret_cast<ViewMeta*>(smb + Cfg::META_OFF);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smb + Cfg::BAR_OFF);
+    volatile int* abortw = reinterpret_cast<volatile int*>(smb + ABORT_OFF);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        for (int b = 0; b < NB; b++) {
+            mbar_init(smem_u32(&bars[b]), 1);
+            mbar_init(smem_u32(&bars[NB + b]), 8);
         }
+        *abortw = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const LinTile T = lin_tile(p, Cfg::TX, Cfg::TY, Cfg::ES);
+    const int nchunks = (T.nviews + VC - 1) / VC;
+    bool failed = false;
+    int produced = 0;
+    if (warp == 8) {
+        for (; produced < nchunks; produced++) {
+            if (__any_sync(0xffffffffu, *abortw != 0)) { failed = true; break; }
+            if (!lin_fill<Cfg>(T, smb, meta, bars, produced, lane)) {
+                failed = true;
+                if (lane == 0) *abortw = 1;
+                break;
+            }
+        }
+    } else {
+        const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
+        float colf[4], rowf[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) colf[c] = (float)(tx + Cfg::GX * c);
+#pragma unroll
+        for (int r = 0; r < 4; r++) rowf[r] = (float)(ty + Cfg::GY * r);
+        float acc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[r][c] = 0.0f;
+        for (int k = 0; k < nchunks; k++) {
+            const unsigned g = (unsigned)k;
+            const int b = (int)(g % NB);
+            if (__any_sync(0xffffffffu, *abortw != 0) ||
+                !__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) {
+                failed = true;
+                if (lane == 0) *abortw = 1;
+                break;
+            }
+            lin_consume<Cfg, MODE>(acc, colf, rowf, smb, meta, b, min(VC, T.nviews - k * VC));
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
+        }
+        if (!failed) lin_store<Cfg>(p, T, acc, tx, ty);
+    }
+    if (__syncthreads_or(failed)) {
+        if (tid == 0) atomicOr(&g_kernel_status, 1u);
+        if (warp == 8)
+            for (int c = produced > NB ? produced - NB : 0; c < produced; c++)
+                mbar_wait_bounded(smem_u32(&bars[(unsigned)c % NB]), ((unsigned)c / NB) & 1u);
     }
 }
 
@@ -1237,11 +1346,35 @@ static cudaError_t go_lin(const BackprojLaunch& p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int MODE, int VC, int NB, int MINB>
+static cudaError_t go_lin_ws(const BackprojLaunch& p, cudaStream_t s) {
+    using Cfg = LinCfg<2, 4, 4, 4, VC, NB, MODE>;
+    auto kern = k_bp_lin_ws<VC, NB, MODE, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM_WS);
+    if (e != cudaSuccess) return e;
+    const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
+    kern<<<dim3(tiles, p.nslices), 288, Cfg::SMEM_WS, s>>>(p);
+    return cudaGetLastError();
+}
+
+// LIN kernel form (RV_LIN_VARIANT): 0 = warp 0 also produces, 2 buffers x 8 views; 1 = a
+// dedicated producer warp, 2 x 8; 2 = producer warp, 3 x 8, 3 CTAs/SM; 3 = producer warp, 2 x 16
+template <int MODE>
+static cudaError_t dispatch_lin(const BackprojLaunch& p, cudaStream_t s) {
+    static const int v = env_int("RV_LIN_VARIANT", 1);
+    switch (v) {
+    case 0: return go_lin<MODE>(p, s);
+    case 2: return go_lin_ws<MODE, 8, 3, 3>(p, s);
+    case 3: return go_lin_ws<MODE, 16, 2, 3>(p, s);
+    default: return go_lin_ws<MODE, 8, 2, 4>(p, s);
+    }
+}
+
 cudaError_t launch_bp_lin(const BackprojLaunch& p, cudaStream_t s) {
     switch (p.mode) {
-    case RV_MODE_LIN: return go_lin<RV_MODE_LIN>(p, s);
-    case RV_MODE_LIN_F16: return go_lin<RV_MODE_LIN_F16>(p, s);
-    case RV_MODE_LIN_BF16: return go_lin<RV_MODE_LIN_BF16>(p, s);
+    case RV_MODE_LIN: return dispatch_lin<RV_MODE_LIN>(p, s);
+    case RV_MODE_LIN_F16: return dispatch_lin<RV_MODE_LIN_F16>(p, s);
+    case RV_MODE_LIN_BF16: return dispatch_lin<RV_MODE_LIN_BF16>(p, s);
     default: return cudaErrorInvalidValue;
     }
 }
