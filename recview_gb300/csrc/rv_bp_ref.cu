@@ -52,6 +52,12 @@ __device__ __forceinline__ int lds_s32(unsigned addr) {
     asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(addr));
     return v;
 }
+template <int OFF>
+__device__ __forceinline__ int lds_s32_off(unsigned addr) {   // [addr + OFF], OFF in the instruction
+    int v;
+    asm volatile("ld.shared.s32 %0, [%1+%2];" : "=r"(v) : "r"(addr), "n"(OFF));
+    return v;
+}
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
 }
@@ -423,9 +429,12 @@ __device__ __forceinline__ void pipe_init_barriers(int* smi) {
 // geometry and window in meta, zero-fills the parts of a window outside the table, and issues one
 // TMA bulk copy per view on the buffer's full barrier.  Returns false (warp-uniform) when the wait
 // for the empty barrier ran out.
-template <int TX, int TY, int WIN, int ALIGN, int VC, int NB, int PAD>
+// NS = 2 stages, for every view, the windows of two slices that share the geometry (the same
+// window bounds, tables J.table and table2) one after the other: window (b, vv, s) at
+// ((b * VC + vv) * NS + s) * WIN.
+template <int TX, int TY, int WIN, int ALIGN, int VC, int NB, int PAD, int NS = 1>
 __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* meta, uint64_t* bars, int c,
-                                          unsigned g, int lane) {
+                                          unsigned g, int lane, const int* table2 = nullptr) {
     const int X0 = J.X0, Y0 = J.Y0;
     const int nviews = J.nviews;
     const int nstore = PAD ? ((17 * J.ixdimp + 3) & ~3) : 16 * J.ixdimp;
@@ -475,18 +484,21 @@ __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* 
     for (int vv = 0; vv < nv; vv++) {
         const ViewMeta m = meta[b * VC + vv];
         if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
-        int4* w4 = reinterpret_cast<int4*>(win + (b * VC + vv) * WIN);
         const int za = (m.b > m.a) ? (m.a - m.w0) >> 2 : m.nwin >> 2;
         const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;
-        for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
-        for (int e = zb + lane; e < (m.nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) {
+            int4* w4 = reinterpret_cast<int4*>(win + ((b * VC + vv) * NS + sl) * WIN);
+            for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+            for (int e = zb + lane; e < (m.nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        }
     }
     __syncwarp();
     if (lane == 0) {
         unsigned bytes = 0;
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[b * VC + vv];
-            if (m.b > m.a) bytes += 4u * (unsigned)(m.b - m.a);
+            if (m.b > m.a) bytes += 4u * NS * (unsigned)(m.b - m.a);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const unsigned bar = smem_u32(&bars[b]);
@@ -494,9 +506,12 @@ __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* 
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[b * VC + vv];
             if (m.b <= m.a) continue;
-            const int* src = J.table + (size_t)(v0 + vv) * J.table_stride + m.a;
-            const unsigned dst = smem_u32(win + (b * VC + vv) * WIN + (m.a - m.w0));
-            tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
+#pragma unroll
+            for (int sl = 0; sl < NS; sl++) {
+                const int* src = (sl ? table2 : J.table) + (size_t)(v0 + vv) * J.table_stride + m.a;
+                const unsigned dst = smem_u32(win + ((b * VC + vv) * NS + sl) * WIN + (m.a - m.w0));
+                tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
+            }
         }
     }
     __syncwarp();
@@ -706,13 +721,14 @@ __device__ __forceinline__ bool consumers_bar_or(bool pred) {   // named barrier
 }
 __device__ __forceinline__ void consumers_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-template <int VC, int NB, int PAD>
+template <int VC, int NB, int PAD, int NS = 1>
 struct WsCfg {
-    using Pipe = PipeCfg<2, 4, 4, 4, VC, NB, PAD>;   // 64x64 tile: the same windows and records
+    using Pipe = PipeCfg<2, 4, 4, 4, VC, NB, PAD>;   // 64x64 tile: the same window size
     static constexpr int NT = 288;                   // 8 consumer warps + 1 producer warp
     static constexpr int TX = Pipe::TX, TY = Pipe::TY, ALIGN = Pipe::ALIGN, WIN = Pipe::WIN;
-    static constexpr int META_OFF = Pipe::META_OFF, BAR_OFF = Pipe::BAR_OFF;
-    static constexpr int ABORT_OFF = BAR_OFF + 4 * NB;   // words: after full[NB], empty[NB]
+    static constexpr int META_OFF = NB * VC * NS * WIN;      // words: windows [NB][VC][NS][WIN]
+    static constexpr int BAR_OFF = META_OFF + NB * VC * 8;   // view records [NB][VC]
+    static constexpr int ABORT_OFF = BAR_OFF + 4 * NB;       // after full[NB], empty[NB]
     static constexpr size_t SMEM = (size_t)ABORT_OFF * 4 + 16;
     static constexpr bool EXCHANGE_FITS = VC * WIN >= 16 * 256;   // one buffer holds the exchange
     static_assert(TX == 64 && TY == 64 && Pipe::NT == 256, "8 consumer warps tile 64x64 pixels");
@@ -747,14 +763,15 @@ __device__ __forceinline__ void ray_coords(int regime, int X0, int Y0, int warp,
     for (int p = 0; p < 2; p++) fix[p] = (float)(fb + lane + 32 * p);
 }
 
-// acc[s] += the table entry of slot s's pixel, for the views of one staged chunk.  fx[s] is
-// fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of that pixel (formed by the caller's functor).
-template <int VC, int WIN, int PAD, bool CHECKED, typename FX>
-__device__ __forceinline__ void ws_gather(int (&acc)[16], const int* win, const ViewMeta* meta, int b, int vv,
+// acc[sl][s] += the table entry of slot s's pixel in slice sl, for one view of a staged chunk.
+// fx_of(s) is fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of that pixel; the NS slices share it, so
+// a second slice costs one more shared load (its window sits WIN words further) and one add.
+template <int VC, int WIN, int PAD, bool CHECKED, int NS, typename FX>
+__device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, const ViewMeta* meta, int b, int vv,
                                           unsigned& viol, FX fx_of) {
     const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
     const unsigned offb = __float_as_uint(gm.w);
-    const unsigned base = smem_u32(win + (b * VC + vv) * WIN) + (offb & ~3u);
+    const unsigned base = smem_u32(win + (b * VC + vv) * NS * WIN) + (offb & ~3u);
     int cw0 = 0, cnw = 0;
     if (CHECKED) {
         cw0 = meta[b * VC + vv].w0;
@@ -763,7 +780,7 @@ __device__ __forceinline__ void ws_gather(int (&acc)[16], const int* win, const 
     if (offb & 1u) {
 #pragma unroll
         for (int s = 0; s < 16; s++) {
-            const float fx = fx_of(s, gm);
+            const float fx = fx_of(s);
             const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
             const unsigned st = PAD ? bits + (bits >> 4) : bits;
             if (CHECKED) {
@@ -771,26 +788,30 @@ __device__ __forceinline__ void ws_gather(int (&acc)[16], const int* win, const 
                 const int sw = PAD ? v + (v >> 4) : v;
                 if (fx < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
             }
-            acc[s] += lds_s32(base + 4u * st);
+            const unsigned a = base + 4u * st;
+            acc[0][s] += lds_s32(a);
+            if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
         }
     } else {
 #pragma unroll
         for (int s = 0; s < 16; s++) {
-            const float fx = fx_of(s, gm);
+            const float fx = fx_of(s);
             const int v = __float2int_rz(fx);
             const int sw = PAD ? v + (v >> 4) : v;
             if (CHECKED) {
                 if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
             }
-            acc[s] += lds_s32(base + 4u * (unsigned)sw);
+            const unsigned a = base + 4u * (unsigned)sw;
+            acc[0][s] += lds_s32(a);
+            if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
         }
     }
 }
 
 // one chunk of views: NQ == 0 compact blocks (colf/rowf in lin[0..3] / lin[4..7]), else the
 // ray layout of orientation O
-template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED>
-__device__ __forceinline__ void ws_consume(int (&acc)[16], const float (&lin)[8], const float (&fix)[2],
+template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS>
+__device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin)[8], const float (&fix)[2],
                                            const int* win, const ViewMeta* meta, int b, int nv, unsigned& viol) {
     for (int vv = 0; vv < nv; vv++) {
         const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
@@ -800,31 +821,31 @@ __device__ __forceinline__ void ws_consume(int (&acc)[16], const float (&lin)[8]
             for (int c = 0; c < 4; c++) xv[c] = fmulr(lin[c], g.x);
 #pragma unroll
             for (int r = 0; r < 4; r++) yv[r] = faddr(fmulr(lin[4 + r], g.y), g.z);
-            ws_gather<VC, WIN, PAD, CHECKED>(acc, win, meta, b, vv, viol,
-                                             [&](int s, float4) { return faddr(xv[s & 3], yv[s >> 2]); });
+            ws_gather<VC, WIN, PAD, CHECKED, NS>(acc, win, meta, b, vv, viol,
+                                                 [&](int s) { return faddr(xv[s & 3], yv[s >> 2]); });
         } else if (O == 0) {   // V: x = lin[q], y = fix[p]
             float xs[8], ys[2];
 #pragma unroll
             for (int q = 0; q < 8; q++) xs[q] = fmulr(lin[q], g.x);
 #pragma unroll
             for (int p = 0; p < 2; p++) ys[p] = faddr(fmulr(fix[p], g.y), g.z);
-            ws_gather<VC, WIN, PAD, CHECKED>(acc, win, meta, b, vv, viol,
-                                             [&](int s, float4) { return faddr(xs[s >> 1], ys[s & 1]); });
+            ws_gather<VC, WIN, PAD, CHECKED, NS>(acc, win, meta, b, vv, viol,
+                                                 [&](int s) { return faddr(xs[s >> 1], ys[s & 1]); });
         } else {   // H: x = fix[p], y = lin[q]
             float xs[2], ys[8];
 #pragma unroll
             for (int p = 0; p < 2; p++) xs[p] = fmulr(fix[p], g.x);
 #pragma unroll
             for (int q = 0; q < 8; q++) ys[q] = faddr(fmulr(lin[q], g.y), g.z);
-            ws_gather<VC, WIN, PAD, CHECKED>(acc, win, meta, b, vv, viol,
-                                             [&](int s, float4) { return faddr(xs[s & 1], ys[s >> 1]); });
+            ws_gather<VC, WIN, PAD, CHECKED, NS>(acc, win, meta, b, vv, viol,
+                                                 [&](int s) { return faddr(xs[s & 1], ys[s >> 1]); });
         }
     }
 }
 
-template <int VC, int NB, int PAD>
+template <int VC, int NB, int PAD, int NS>
 __device__ __forceinline__ void ws_init(int* smi) {
-    using Cfg = WsCfg<VC, NB, PAD>;
+    using Cfg = WsCfg<VC, NB, PAD, NS>;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);
     if (threadIdx.x == 0) {
         for (int b = 0; b < NB; b++) {
@@ -836,14 +857,16 @@ __device__ __forceinline__ void ws_init(int* smi) {
     }
 }
 
-// One 64x64 tile; gc as in bp_ref_tile_pipe.  Returns false (for the whole CTA) after a bounded
-// wait ran out.  Warps 0-7 consume, warp 8 produces.
-template <int VC, int NB, int PAD, int NQ, bool CHECKED>
-__device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter) {
-    using Cfg = WsCfg<VC, NB, PAD>;
-    static_assert(NQ == 0 || Cfg::EXCHANGE_FITS, "the accumulator exchange needs 4096 words in one buffer");
+// One 64x64 tile of NS slices (NS = 2: J and a second slice with the same geometry, tables
+// table2, output out2); gc as in bp_ref_tile_pipe.  Returns false (for the whole CTA) after a
+// bounded wait ran out.  Warps 0-7 consume, warp 8 produces.
+template <int VC, int NB, int PAD, int NQ, bool CHECKED, int NS = 1>
+__device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter,
+                                               const int* table2 = nullptr, int* out2 = nullptr) {
+    using Cfg = WsCfg<VC, NB, PAD, NS>;
+    static_assert(NQ == 0 || Cfg::EXCHANGE_FITS, "the accumulator exchange needs 4096 words per slice in one buffer");
     constexpr int WIN = Cfg::WIN;
-    int* win = smi;                                                     // [NB][VC][WIN]
+    int* win = smi;                                                     // [NB][VC][NS][WIN]
     ViewMeta* meta = reinterpret_cast<ViewMeta*>(smi + Cfg::META_OFF);  // [NB][VC]
     uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);   // full[NB], empty[NB]
     volatile int* abortw = smi + Cfg::ABORT_OFF;
@@ -860,8 +883,8 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 failed = true;
                 break;
             }
-            if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD>(J, win, meta, bars, produced, gc + (unsigned)produced,
-                                                                 lane)) {
+            if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD, NS>(J, win, meta, bars, produced,
+                                                                     gc + (unsigned)produced, lane, table2)) {
                 failed = true;
                 if (lane == 0) *abortw = 1;
                 break;
@@ -869,9 +892,11 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
         }
     } else {
         unsigned viol = 0;
-        int acc[16];
+        int acc[NS][16];
 #pragma unroll
-        for (int s = 0; s < 16; s++) acc[s] = 0;
+        for (int sl = 0; sl < NS; sl++)
+#pragma unroll
+            for (int s = 0; s < 16; s++) acc[sl][s] = 0;
         float lin[8], fix[2];
         int regime = 0;
         float2 gnext = make_float2(0.0f, 0.0f);   // fcos, fsin of the first view of chunk k + 1
@@ -900,8 +925,8 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
             if (!failed && !__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) failed = true;
             if (!failed) {
                 const int nv = min(VC, nviews - k * VC);
-                if (NQ == 0 || !(regime & 1)) ws_consume<NQ, 0, VC, WIN, PAD, CHECKED>(acc, lin, fix, win, meta, b, nv, viol);
-                else ws_consume<NQ, 1, VC, WIN, PAD, CHECKED>(acc, lin, fix, win, meta, b, nv, viol);
+                if (NQ == 0 || !(regime & 1)) ws_consume<NQ, 0, VC, WIN, PAD, CHECKED, NS>(acc, lin, fix, win, meta, b, nv, viol);
+                else ws_consume<NQ, 1, VC, WIN, PAD, CHECKED, NS>(acc, lin, fix, win, meta, b, nv, viol);
             } else if (lane == 0) {
                 *abortw = 1;
             }
@@ -921,9 +946,11 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                         failed = true;
                         break;
                     }
-                    int* xs = win + b * VC * WIN;   // [16 slots][256 threads]
+                    int* xs = win + b * VC * NS * WIN;   // [NS][16 slots][256 threads]
 #pragma unroll
-                    for (int s = 0; s < 16; s++) xs[s * 256 + tid] = acc[s];
+                    for (int sl = 0; sl < NS; sl++)
+#pragma unroll
+                        for (int s = 0; s < 16; s++) xs[(sl * 16 + s) * 256 + tid] = acc[sl][s];
                     consumers_bar();
                     const int on = next & 1, oo = regime & 1;
                     const int shn = ray_shift<NQ>(lane, next);
@@ -936,7 +963,9 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                             const int a = oo ? xr : yr, c = oo ? yr : xr;                  // old fixed / sheared
                             const int jj = a & 31, pp = a >> 5;
                             const int m = (c - ray_shift<NQ>(jj, regime)) & 63;             // old w + 8 q
-                            acc[2 * q + p] = xs[((m >> 3) * 2 + pp) * 256 + (m & 7) * 32 + jj];
+                            const int src = ((m >> 3) * 2 + pp) * 256 + (m & 7) * 32 + jj;
+#pragma unroll
+                            for (int sl = 0; sl < NS; sl++) acc[sl][2 * q + p] = xs[sl * 4096 + src];
                         }
                     regime = next;
                     ray_coords<NQ>(regime, X0, Y0, warp, lane, lin, fix);
@@ -951,7 +980,6 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
         }
         if (!failed) {
             if (CHECKED && viol) atomicAdd(status_counter, viol);
-            int* out = J.out;
             const int sh = NQ > 0 ? ray_shift<NQ>(lane, regime) : 0;
             const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
 #pragma unroll
@@ -965,7 +993,10 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                     x = X0 + ((regime & 1) ? f : u);
                     y = Y0 + ((regime & 1) ? u : f);
                 }
-                if (x < ixdimp && y < ixdimp) out[(size_t)y * ixdimp + x] = acc[s];
+                if (x < ixdimp && y < ixdimp) {
+                    J.out[(size_t)y * ixdimp + x] = acc[0][s];
+                    if (NS > 1) out2[(size_t)y * ixdimp + x] = acc[NS - 1][s];
+                }
             }
         }
     }
@@ -984,22 +1015,26 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
     return true;
 }
 
-template <int VC, int NB, int PAD, int NQ, int MINB, bool CHECKED>
-__global__ void __launch_bounds__(288, MINB) k_bp_ref_ws(BackprojLaunch p) {
+// grid (tiles, slices / NS): CTA row y covers slices slice0 + NS y (.. + NS - 1); NS = 2 needs
+// slices that share the geometry (geom_slice_stride 0)
+template <int VC, int NB, int PAD, int NQ, int MINB, bool CHECKED, int NS = 1>
+__global__ void __launch_bounds__(288, MINB) k_bp_ref_ws(BackprojLaunch p, int slice0) {
     extern __shared__ __align__(128) int smi[];
-    ws_init<VC, NB, PAD>(smi);
+    ws_init<VC, NB, PAD, NS>(smi);
     __syncthreads();
     const int tiles_x = (p.ixdimp + 63) / 64;
+    const int sl = slice0 + NS * (int)blockIdx.y;
     TileJob J;
-    J.table = p.table + (size_t)blockIdx.y * p.slice_table_stride;
-    J.geom = p.geom + (size_t)blockIdx.y * p.geom_slice_stride;
-    J.out = static_cast<int*>(p.out) + (size_t)blockIdx.y * p.out_slice_stride;
+    J.table = p.table + (size_t)sl * p.slice_table_stride;
+    J.geom = p.geom + (size_t)sl * p.geom_slice_stride;
+    J.out = static_cast<int*>(p.out) + (size_t)sl * p.out_slice_stride;
     J.table_stride = p.table_stride;
     J.nviews = p.nviews;
     J.ixdimp = p.ixdimp;
     J.X0 = (blockIdx.x % tiles_x) * 64;
     J.Y0 = (blockIdx.x / tiles_x) * 64;
-    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED>(J, smi, 0u, p.status_counter);
+    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED, NS>(J, smi, 0u, p.status_counter, J.table + p.slice_table_stride,
+                                                 J.out + p.out_slice_stride);
 }
 
 template <int VC, int NB, int PAD, int NQ, int MINB>
@@ -1007,7 +1042,7 @@ __global__ void __launch_bounds__(288, MINB) k_bp_ref_ws_persistent(const TileJo
                                                                     unsigned* counter) {
     extern __shared__ __align__(128) int smi[];
     __shared__ int s_item;
-    ws_init<VC, NB, PAD>(smi);
+    ws_init<VC, NB, PAD, 1>(smi);
     unsigned gc = 0;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
@@ -1613,7 +1648,9 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //     13: 128x64, 512 threads, 2 x 4;  14, 15: 64x64, 2 buffers x 5 / 6 views, 3 CTAs/SM
 //     16: 64x64, 8 consumer warps + 1 producer warp, ray-aligned lane footprints (shear steps
 //         of 1/8), 2 buffers x 6 views, 3 CTAs/SM;  17: the same with compact 8x4 lane blocks,
-//         2 buffers x 4 views, 4 CTAs/SM
+//         2 buffers x 4 views, 4 CTAs/SM;  18: variant 16's layout over slice pairs (two
+//         slices sharing the geometry per CTA: one index per pixel and view, two gathers),
+//         2 buffers x 4 views x 2 slices, 2 CTAs/SM
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -1623,7 +1660,7 @@ static int env_int(const char* name, int dflt) {
 }
 static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
-    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 16);
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 18);
     if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
 int ref_table_fmt() {
@@ -1668,13 +1705,30 @@ static cudaError_t go_pipe(const BackprojLaunch& p, cudaStream_t s, bool checked
     return launch_k(k_bp_ref_pipe<WX, WY, RX, RY, VC, NB, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
+template <int VC, int NB, int PAD, int NQ, int MINB, int NS = 1>
+static cudaError_t go_ws_rows(const BackprojLaunch& p, cudaStream_t s, bool checked, int slice0, int rows) {
+    using Cfg = WsCfg<VC, NB, PAD, NS>;
+    const int tiles = ((p.ixdimp + 63) / 64) * ((p.ixdimp + 63) / 64);
+    auto kern = checked ? k_bp_ref_ws<VC, NB, PAD, NQ, MINB, true, NS> : k_bp_ref_ws<VC, NB, PAD, NQ, MINB, false, NS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
+    if (e != cudaSuccess) return e;
+    kern<<<dim3(tiles, rows), Cfg::NT, Cfg::SMEM, s>>>(p, slice0);
+    return cudaGetLastError();
+}
+
 template <int VC, int NB, int PAD, int NQ, int MINB>
 static cudaError_t go_ws(const BackprojLaunch& p, cudaStream_t s, bool checked) {
-    using Cfg = WsCfg<VC, NB, PAD>;
-    const int tiles = ((p.ixdimp + 63) / 64) * ((p.ixdimp + 63) / 64);
-    dim3 grid(tiles, p.nslices);
-    if (checked) return launch_k(k_bp_ref_ws<VC, NB, PAD, NQ, MINB, true>, grid, Cfg::NT, Cfg::SMEM, p, s);
-    return launch_k(k_bp_ref_ws<VC, NB, PAD, NQ, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
+    return go_ws_rows<VC, NB, PAD, NQ, MINB>(p, s, checked, 0, p.nslices);
+}
+
+// slice pairs (two slices per CTA sharing the index arithmetic) when the slices share the
+// geometry; an odd last slice, or per-slice geometry, runs one slice per CTA (variant 16's form)
+template <int VC, int NB, int PAD, int NQ, int MINB>
+static cudaError_t go_ws_pairs(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    if (p.geom_slice_stride != 0 || p.nslices < 2) return go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, 0, p.nslices);
+    cudaError_t e = go_ws_rows<VC, NB, PAD, NQ, MINB, 2>(p, s, checked, 0, p.nslices / 2);
+    if (e == cudaSuccess && (p.nslices & 1)) e = go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, p.nslices - 1, 1);
+    return e;
 }
 
 template <int WX, int WY, int RX, int RY, int VC, int MINB>
@@ -1706,6 +1760,7 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 15: return go_pipe<2, 4, 4, 4, 6, 2, PAD, 3>(p, s, checked);
     case 16: return go_ws<6, 2, PAD, 8, 3>(p, s, checked);
     case 17: return go_ws<4, 2, PAD, 0, 4>(p, s, checked);
+    case 18: return go_ws_pairs<4, 2, PAD, 8, 2>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -1762,7 +1817,7 @@ static cudaError_t go_pipe_persistent(const TileJob* jobs, int njobs, unsigned* 
 
 template <int VC, int NB, int PAD, int NQ, int MINB>
 static cudaError_t go_ws_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
-    using Cfg = WsCfg<VC, NB, PAD>;
+    using Cfg = WsCfg<VC, NB, PAD, 1>;
     auto kern = k_bp_ref_ws_persistent<VC, NB, PAD, NQ, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
     if (e != cudaSuccess) return e;
@@ -1808,7 +1863,7 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 13: return go_pipe_persistent<4, 4, 4, 4, 4, 2, PAD, 2>(jobs, njobs, counter, s);
     case 14: return go_pipe_persistent<2, 4, 4, 4, 5, 2, PAD, 3>(jobs, njobs, counter, s);
     case 15: return go_pipe_persistent<2, 4, 4, 4, 6, 2, PAD, 3>(jobs, njobs, counter, s);
-    case 16: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
+    case 16: case 18: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
@@ -1869,7 +1924,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 17 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 18 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;
