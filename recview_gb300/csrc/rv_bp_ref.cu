@@ -764,13 +764,44 @@ __device__ __forceinline__ void ray_coords(int regime, int X0, int Y0, int warp,
 }
 
 // acc[sl][s] += the table entry of slot s's pixel in slice sl, for one view of a staged chunk.
-// fx_of(s) is fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of that pixel; the NS slices share it, so
-// a second slice costs one more shared load (its window sits WIN words further) and one add.
-template <int VC, int WIN, int PAD, bool CHECKED, int NS, typename FX>
+// fx2(i) gives fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of the two pixels of slot pair i
+// (slots ws_slot<COMPACT>(i, 0) and (i, 1)), formed with the paired FP32 instructions (each lane
+// rounds like the scalar operation).  The NS slices share the index, so a second slice costs one
+// more shared load (its window sits WIN words further) and one add.
+__device__ __forceinline__ float2 bcast2(float v) { return make_float2(v, v); }
+// Paired FP32 additions (two lanes per instruction), each lane rounded like the scalar addition.
+// Only additions are paired: the compiler fuses a paired multiply into a following paired add
+// (one rounding instead of two) even with explicit rounding, so every product is a scalar
+// __fmul_rn, which it never fuses.
+__device__ __forceinline__ unsigned long long pk2(float2 v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+__device__ __forceinline__ float2 add2_rz(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+
+template <bool COMPACT>
+__device__ __forceinline__ constexpr int ws_slot(int i, int h) {
+    // ray layouts: slot 2q + p, pairs (q, q+1) at even q;  compact: slot 4r + c, pairs (c, c+1)
+    return COMPACT ? 4 * (i >> 1) + 2 * (i & 1) + h : 4 * (i >> 1) + (i & 1) + 2 * h;
+}
+template <int VC, int WIN, int PAD, bool CHECKED, int NS, bool COMPACT, typename FX2>
 __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, const ViewMeta* meta, int b, int vv,
-                                          unsigned& viol, FX fx_of) {
-    const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
-    const unsigned offb = __float_as_uint(gm.w);
+                                          unsigned offb, unsigned& viol, FX2 fx2) {
     const unsigned base = smem_u32(win + (b * VC + vv) * NS * WIN) + (offb & ~3u);
     int cw0 = 0, cnw = 0;
     if (CHECKED) {
@@ -778,67 +809,79 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, co
         cnw = meta[b * VC + vv].nwin;
     }
     if (offb & 1u) {
+        const float2 mag = make_float2(8388608.0f, 8388608.0f);
 #pragma unroll
-        for (int s = 0; s < 16; s++) {
-            const float fx = fx_of(s);
-            const unsigned bits = __float_as_uint(__fadd_rz(fx, 8388608.0f));
-            const unsigned st = PAD ? bits + (bits >> 4) : bits;
-            if (CHECKED) {
-                const int v = (int)(bits - kMagicBits);
-                const int sw = PAD ? v + (v >> 4) : v;
-                if (fx < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+        for (int i = 0; i < 8; i++) {
+            const float2 fx = fx2(i);
+            const float2 t = add2_rz(fx, mag);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int s = ws_slot<COMPACT>(i, h);
+                const unsigned bits = __float_as_uint(h ? t.y : t.x);
+                const unsigned st = PAD ? bits + (bits >> 4) : bits;
+                if (CHECKED) {
+                    const int v = (int)(bits - kMagicBits);
+                    const int sw = PAD ? v + (v >> 4) : v;
+                    if ((h ? fx.y : fx.x) < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+                }
+                const unsigned a = base + 4u * st;
+                acc[0][s] += lds_s32(a);
+                if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
             }
-            const unsigned a = base + 4u * st;
-            acc[0][s] += lds_s32(a);
-            if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
         }
     } else {
 #pragma unroll
-        for (int s = 0; s < 16; s++) {
-            const float fx = fx_of(s);
-            const int v = __float2int_rz(fx);
-            const int sw = PAD ? v + (v >> 4) : v;
-            if (CHECKED) {
-                if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+        for (int i = 0; i < 8; i++) {
+            const float2 fx = fx2(i);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int s = ws_slot<COMPACT>(i, h);
+                const int v = __float2int_rz(h ? fx.y : fx.x);
+                const int sw = PAD ? v + (v >> 4) : v;
+                if (CHECKED) {
+                    if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
+                }
+                const unsigned a = base + 4u * (unsigned)sw;
+                acc[0][s] += lds_s32(a);
+                if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
             }
-            const unsigned a = base + 4u * (unsigned)sw;
-            acc[0][s] += lds_s32(a);
-            if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
         }
     }
 }
 
+
 // one chunk of views: NQ == 0 compact blocks (colf/rowf in lin[0..3] / lin[4..7]), else the
-// ray layout of orientation O
+// ray layout of orientation O.  Products and y terms are scalar (fl(x fcos), fl(fl(y fsin) +
+// foffset)); the per-pixel sums are paired.
 template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS>
 __device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin)[8], const float (&fix)[2],
                                            const int* win, const ViewMeta* meta, int b, int nv, unsigned& viol) {
     for (int vv = 0; vv < nv; vv++) {
         const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+        const unsigned offb = __float_as_uint(g.w);
         if (NQ == 0) {   // slot s = 4 r + c: x = lin[c], y = lin[4 + r]
-            float xv[4], yv[4];
+            float2 X[2], Yb[4];
 #pragma unroll
-            for (int c = 0; c < 4; c++) xv[c] = fmulr(lin[c], g.x);
+            for (int k = 0; k < 2; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
 #pragma unroll
-            for (int r = 0; r < 4; r++) yv[r] = faddr(fmulr(lin[4 + r], g.y), g.z);
-            ws_gather<VC, WIN, PAD, CHECKED, NS>(acc, win, meta, b, vv, viol,
-                                                 [&](int s) { return faddr(xv[s & 3], yv[s >> 2]); });
+            for (int r = 0; r < 4; r++) Yb[r] = bcast2(faddr(fmulr(lin[4 + r], g.y), g.z));
+            ws_gather<VC, WIN, PAD, CHECKED, NS, true>(acc, win, meta, b, vv, offb, viol,
+                                                       [&](int i) { return add2_rn(X[i & 1], Yb[i >> 1]); });
         } else if (O == 0) {   // V: x = lin[q], y = fix[p]
-            float xs[8], ys[2];
+            float2 X[4];
 #pragma unroll
-            for (int q = 0; q < 8; q++) xs[q] = fmulr(lin[q], g.x);
-#pragma unroll
-            for (int p = 0; p < 2; p++) ys[p] = faddr(fmulr(fix[p], g.y), g.z);
-            ws_gather<VC, WIN, PAD, CHECKED, NS>(acc, win, meta, b, vv, viol,
-                                                 [&](int s) { return faddr(xs[s >> 1], ys[s & 1]); });
+            for (int k = 0; k < 4; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
+            const float2 Y0 = bcast2(faddr(fmulr(fix[0], g.y), g.z)), Y1 = bcast2(faddr(fmulr(fix[1], g.y), g.z));
+            ws_gather<VC, WIN, PAD, CHECKED, NS, false>(acc, win, meta, b, vv, offb, viol,
+                                                        [&](int i) { return add2_rn(X[i >> 1], (i & 1) ? Y1 : Y0); });
         } else {   // H: x = fix[p], y = lin[q]
-            float xs[2], ys[8];
+            float2 Y[4];
 #pragma unroll
-            for (int p = 0; p < 2; p++) xs[p] = fmulr(fix[p], g.x);
-#pragma unroll
-            for (int q = 0; q < 8; q++) ys[q] = faddr(fmulr(lin[q], g.y), g.z);
-            ws_gather<VC, WIN, PAD, CHECKED, NS>(acc, win, meta, b, vv, viol,
-                                                 [&](int s) { return faddr(xs[s & 1], ys[s >> 1]); });
+            for (int k = 0; k < 4; k++)
+                Y[k] = make_float2(faddr(fmulr(lin[2 * k], g.y), g.z), faddr(fmulr(lin[2 * k + 1], g.y), g.z));
+            const float2 X0 = bcast2(fmulr(fix[0], g.x)), X1 = bcast2(fmulr(fix[1], g.x));
+            ws_gather<VC, WIN, PAD, CHECKED, NS, false>(acc, win, meta, b, vv, offb, viol,
+                                                        [&](int i) { return add2_rn((i & 1) ? X1 : X0, Y[i >> 1]); });
         }
     }
 }
