@@ -432,7 +432,8 @@ __device__ __forceinline__ void pipe_init_barriers(int* smi) {
 // NS = 2 stages, for every view, the windows of two slices that share the geometry (the same
 // window bounds, tables J.table and table2) one after the other: window (b, vv, s) at
 // ((b * VC + vv) * NS + s) * WIN.
-template <int TX, int TY, int WIN, int ALIGN, int VC, int NB, int PAD, int NS = 1>
+// NSL (>= NS) is the number of window slots per view in the buffer layout.
+template <int TX, int TY, int WIN, int ALIGN, int VC, int NB, int PAD, int NS = 1, int NSL = NS>
 __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* meta, uint64_t* bars, int c,
                                           unsigned g, int lane, const int* table2 = nullptr) {
     const int X0 = J.X0, Y0 = J.Y0;
@@ -488,7 +489,7 @@ __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* 
         const int zb = (m.b > m.a) ? (m.b - m.w0) >> 2 : m.nwin >> 2;
 #pragma unroll
         for (int sl = 0; sl < NS; sl++) {
-            int4* w4 = reinterpret_cast<int4*>(win + ((b * VC + vv) * NS + sl) * WIN);
+            int4* w4 = reinterpret_cast<int4*>(win + ((b * VC + vv) * NSL + sl) * WIN);
             for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
             for (int e = zb + lane; e < (m.nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
         }
@@ -509,7 +510,7 @@ __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* 
 #pragma unroll
             for (int sl = 0; sl < NS; sl++) {
                 const int* src = (sl ? table2 : J.table) + (size_t)(v0 + vv) * J.table_stride + m.a;
-                const unsigned dst = smem_u32(win + ((b * VC + vv) * NS + sl) * WIN + (m.a - m.w0));
+                const unsigned dst = smem_u32(win + ((b * VC + vv) * NSL + sl) * WIN + (m.a - m.w0));
                 tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
             }
         }
@@ -799,10 +800,10 @@ __device__ __forceinline__ constexpr int ws_slot(int i, int h) {
     // ray layouts: slot 2q + p, pairs (q, q+1) at even q;  compact: slot 4r + c, pairs (c, c+1)
     return COMPACT ? 4 * (i >> 1) + 2 * (i & 1) + h : 4 * (i >> 1) + (i & 1) + 2 * h;
 }
-template <int VC, int WIN, int PAD, bool CHECKED, int NS, bool COMPACT, typename FX2>
+template <int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, bool COMPACT, typename FX2>
 __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, const ViewMeta* meta, int b, int vv,
                                           unsigned offb, unsigned& viol, FX2 fx2) {
-    const unsigned base = smem_u32(win + (b * VC + vv) * NS * WIN) + (offb & ~3u);
+    const unsigned base = smem_u32(win + (b * VC + vv) * NSL * WIN) + (offb & ~3u);
     int cw0 = 0, cnw = 0;
     if (CHECKED) {
         cw0 = meta[b * VC + vv].w0;
@@ -853,7 +854,7 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, co
 // one chunk of views: NQ == 0 compact blocks (colf/rowf in lin[0..3] / lin[4..7]), else the
 // ray layout of orientation O.  Products and y terms are scalar (fl(x fcos), fl(fl(y fsin) +
 // foffset)); the per-pixel sums are paired.
-template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS>
+template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL>
 __device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin)[8], const float (&fix)[2],
                                            const int* win, const ViewMeta* meta, int b, int nv, unsigned& viol) {
     for (int vv = 0; vv < nv; vv++) {
@@ -865,14 +866,14 @@ __device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin
             for (int k = 0; k < 2; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
 #pragma unroll
             for (int r = 0; r < 4; r++) Yb[r] = bcast2(faddr(fmulr(lin[4 + r], g.y), g.z));
-            ws_gather<VC, WIN, PAD, CHECKED, NS, true>(acc, win, meta, b, vv, offb, viol,
+            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, true>(acc, win, meta, b, vv, offb, viol,
                                                        [&](int i) { return add2_rn(X[i & 1], Yb[i >> 1]); });
         } else if (O == 0) {   // V: x = lin[q], y = fix[p]
             float2 X[4];
 #pragma unroll
             for (int k = 0; k < 4; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
             const float2 Y0 = bcast2(faddr(fmulr(fix[0], g.y), g.z)), Y1 = bcast2(faddr(fmulr(fix[1], g.y), g.z));
-            ws_gather<VC, WIN, PAD, CHECKED, NS, false>(acc, win, meta, b, vv, offb, viol,
+            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, false>(acc, win, meta, b, vv, offb, viol,
                                                         [&](int i) { return add2_rn(X[i >> 1], (i & 1) ? Y1 : Y0); });
         } else {   // H: x = fix[p], y = lin[q]
             float2 Y[4];
@@ -880,7 +881,7 @@ __device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin
             for (int k = 0; k < 4; k++)
                 Y[k] = make_float2(faddr(fmulr(lin[2 * k], g.y), g.z), faddr(fmulr(lin[2 * k + 1], g.y), g.z));
             const float2 X0 = bcast2(fmulr(fix[0], g.x)), X1 = bcast2(fmulr(fix[1], g.x));
-            ws_gather<VC, WIN, PAD, CHECKED, NS, false>(acc, win, meta, b, vv, offb, viol,
+            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, false>(acc, win, meta, b, vv, offb, viol,
                                                         [&](int i) { return add2_rn((i & 1) ? X1 : X0, Y[i >> 1]); });
         }
     }
@@ -903,13 +904,14 @@ __device__ __forceinline__ void ws_init(int* smi) {
 // One 64x64 tile of NS slices (NS = 2: J and a second slice with the same geometry, tables
 // table2, output out2); gc as in bp_ref_tile_pipe.  Returns false (for the whole CTA) after a
 // bounded wait ran out.  Warps 0-7 consume, warp 8 produces.
-template <int VC, int NB, int PAD, int NQ, bool CHECKED, int NS = 1>
+template <int VC, int NB, int PAD, int NQ, bool CHECKED, int NS = 1, int NSL = NS>
 __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter,
                                                const int* table2 = nullptr, int* out2 = nullptr) {
-    using Cfg = WsCfg<VC, NB, PAD, NS>;
+    using Cfg = WsCfg<VC, NB, PAD, NSL>;
+    static_assert(NS <= NSL, "the buffer layout holds NSL windows per view");
     static_assert(NQ == 0 || Cfg::EXCHANGE_FITS, "the accumulator exchange needs 4096 words per slice in one buffer");
     constexpr int WIN = Cfg::WIN;
-    int* win = smi;                                                     // [NB][VC][NS][WIN]
+    int* win = smi;                                                     // [NB][VC][NSL][WIN]
     ViewMeta* meta = reinterpret_cast<ViewMeta*>(smi + Cfg::META_OFF);  // [NB][VC]
     uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);   // full[NB], empty[NB]
     volatile int* abortw = smi + Cfg::ABORT_OFF;
@@ -926,8 +928,8 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 failed = true;
                 break;
             }
-            if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD, NS>(J, win, meta, bars, produced,
-                                                                     gc + (unsigned)produced, lane, table2)) {
+            if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD, NS, NSL>(J, win, meta, bars, produced,
+                                                                          gc + (unsigned)produced, lane, table2)) {
                 failed = true;
                 if (lane == 0) *abortw = 1;
                 break;
@@ -968,8 +970,10 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
             if (!failed && !__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) failed = true;
             if (!failed) {
                 const int nv = min(VC, nviews - k * VC);
-                if (NQ == 0 || !(regime & 1)) ws_consume<NQ, 0, VC, WIN, PAD, CHECKED, NS>(acc, lin, fix, win, meta, b, nv, viol);
-                else ws_consume<NQ, 1, VC, WIN, PAD, CHECKED, NS>(acc, lin, fix, win, meta, b, nv, viol);
+                if (NQ == 0 || !(regime & 1))
+                    ws_consume<NQ, 0, VC, WIN, PAD, CHECKED, NS, NSL>(acc, lin, fix, win, meta, b, nv, viol);
+                else
+                    ws_consume<NQ, 1, VC, WIN, PAD, CHECKED, NS, NSL>(acc, lin, fix, win, meta, b, nv, viol);
             } else if (lane == 0) {
                 *abortw = 1;
             }
@@ -989,7 +993,7 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                         failed = true;
                         break;
                     }
-                    int* xs = win + b * VC * NS * WIN;   // [NS][16 slots][256 threads]
+                    int* xs = win + b * VC * NSL * WIN;   // [NS][16 slots][256 threads]
 #pragma unroll
                     for (int sl = 0; sl < NS; sl++)
 #pragma unroll
@@ -1080,12 +1084,13 @@ __global__ void __launch_bounds__(288, MINB) k_bp_ref_ws(BackprojLaunch p, int s
                                                  J.out + p.out_slice_stride);
 }
 
-template <int VC, int NB, int PAD, int NQ, int MINB>
+// NSL = 2: jobs may cover slice pairs (TileJob::pair), in a layout with two windows per view
+template <int VC, int NB, int PAD, int NQ, int MINB, int NSL = 1>
 __global__ void __launch_bounds__(288, MINB) k_bp_ref_ws_persistent(const TileJob* jobs, int njobs,
                                                                     unsigned* counter) {
     extern __shared__ __align__(128) int smi[];
     __shared__ int s_item;
-    ws_init<VC, NB, PAD, 1>(smi);
+    ws_init<VC, NB, PAD, NSL>(smi);
     unsigned gc = 0;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
@@ -1094,7 +1099,13 @@ __global__ void __launch_bounds__(288, MINB) k_bp_ref_ws_persistent(const TileJo
         __syncthreads();
         if (it >= njobs) break;
         const TileJob J = jobs[it];
-        if (!bp_ref_tile_ws<VC, NB, PAD, NQ, false>(J, smi, gc, nullptr)) return;   // CTA-uniform
+        bool ok;
+        if (NSL > 1 && J.pair)
+            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, (NSL > 1 ? 2 : 1), NSL>(
+                J, smi, gc, nullptr, J.table + (size_t)J.nviews * J.table_stride, J.out + (size_t)J.ixdimp * J.ixdimp);
+        else
+            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, 1, NSL>(J, smi, gc, nullptr);
+        if (!ok) return;   // CTA-uniform
         gc += (unsigned)((J.nviews + VC - 1) / VC);
     }
 }
@@ -1858,10 +1869,10 @@ static cudaError_t go_pipe_persistent(const TileJob* jobs, int njobs, unsigned* 
     return cudaGetLastError();
 }
 
-template <int VC, int NB, int PAD, int NQ, int MINB>
+template <int VC, int NB, int PAD, int NQ, int MINB, int NSL = 1>
 static cudaError_t go_ws_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
-    using Cfg = WsCfg<VC, NB, PAD, 1>;
-    auto kern = k_bp_ref_ws_persistent<VC, NB, PAD, NQ, MINB>;
+    using Cfg = WsCfg<VC, NB, PAD, NSL>;
+    auto kern = k_bp_ref_ws_persistent<VC, NB, PAD, NQ, MINB, NSL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
@@ -1906,7 +1917,8 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 13: return go_pipe_persistent<4, 4, 4, 4, 4, 2, PAD, 2>(jobs, njobs, counter, s);
     case 14: return go_pipe_persistent<2, 4, 4, 4, 5, 2, PAD, 3>(jobs, njobs, counter, s);
     case 15: return go_pipe_persistent<2, 4, 4, 4, 6, 2, PAD, 3>(jobs, njobs, counter, s);
-    case 16: case 18: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
+    case 16: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
+    case 18: return go_ws_persistent<4, 2, PAD, 8, 2, 2>(jobs, njobs, counter, s);
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }

@@ -106,6 +106,8 @@ struct TileJob {
     int* out;                 // the slice (ixdimp^2 int32)
     long long table_stride;
     int nviews, ixdimp, X0, Y0;
+    int pair;                 // 1: also the next slice (tables at table + nviews * table_stride,
+                              // output at out + ixdimp^2), which shares the geometry
 };
 // tile shape of the persistent kernel of an int-table variant (0..4), and the default variant
 void persistent_tile_xy(int variant, int* tx, int* ty);

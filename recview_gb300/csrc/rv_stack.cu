@@ -596,7 +596,10 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
             fl.table_fmt = q->fmt;
             w.filters.push_back(fl);
             const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
-            for (int sl = pt.s0; sl < pt.s1; sl++)
+            // the slice-pair kernel takes two consecutive slices of a part per job (they share
+            // the geometry and their tables follow each other in the pool)
+            const int step = q->variant == 18 ? 2 : 1;
+            for (int sl = pt.s0; sl < pt.s1; sl += step)
                 for (int t = 0; t < ntx * nty; t++) {
                     TileJob J{};
                     J.table = reinterpret_cast<const int*>((pt.off + (size_t)(sl - pt.s0) * V * ts) * 4);
@@ -607,6 +610,7 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
                     J.ixdimp = st->d.ixdimp;
                     J.X0 = (t % ntx) * tx;
                     J.Y0 = (t / ntx) * ty;
+                    J.pair = (step == 2 && sl + 1 < pt.s1) ? 1 : 0;
                     tiles.push_back(J);
                 }
             q->total_updates += (double)(pt.s1 - pt.s0) * V * npix;
@@ -701,7 +705,7 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
     // keeps the fastest for the captured graph
     if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
-    const int cands[] = {16, 17, 11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
+    const int cands[] = {18, 16, 17, 11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
     float best = 3.0e38f;
     int bestv = q->variant;
     for (int v : cands) {
