@@ -78,6 +78,70 @@ cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+
+// The general radix-2 Stockham passes l = 1 .. np-2 (source/cfft.cpp:210-245, 310-345): pass l
+// reads x[j], x[j + n/2] for butterfly j = m 2^l + q and writes y[2m 2^l + q] = x[j] + w b,
+// y[(2m+1) 2^l + q] = x[j] - w b (b = x[j + n/2], w = pass l's twiddle q).  Two consecutive
+// passes l, l+1 (2^(l+1) <= n/4) close over groups of four: butterflies g and g + n/4 of pass l
+// (g < n/4) produce exactly the inputs of butterflies 2m 2^l + q and 2m 2^l + 2^l + q of pass
+// l+1, so one thread runs both passes of a group in registers -- the same operations in the same
+// order, with half the shared-memory round trips and barriers.  An odd pass left over runs alone.
+template <int BPT>
+__device__ __forceinline__ void fft_general_passes(float2* buf, const float2* __restrict__ tw, int np, int half,
+                                                   int tid, int NT) {
+    int l = 1;
+    if (BPT >= 2) {
+        constexpr int G = BPT >= 2 ? BPT / 2 : 1;   // groups of four per thread
+        const int quarter = half >> 1;
+        for (; l + 1 < np - 1; l += 2) {
+            const int al = 1 << l, mask = al - 1;
+            float2 u0[G], u1[G], v0[G], v1[G];
+#pragma unroll
+            for (int i = 0; i < G; i++) {
+                const int g = tid + i * NT;
+                const int q = g & mask;
+                const float2 w = __ldg(tw + al + q);                  // pass l
+                const float2 x0 = buf[g], x1 = cmul(buf[g + half], w);
+                const float2 x2 = buf[g + quarter], x3 = cmul(buf[g + quarter + half], w);
+                u0[i] = cadd(x0, x1);
+                u1[i] = csub(x0, x1);
+                v0[i] = cmul(cadd(x2, x3), __ldg(tw + 2 * al + q));        // pass l+1, butterfly 2m 2^l + q
+                v1[i] = cmul(csub(x2, x3), __ldg(tw + 2 * al + al + q));   // ... 2m 2^l + 2^l + q
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < G; i++) {
+                const int g = tid + i * NT;
+                const int o = 4 * (g >> l) * al + (g & mask);   // y'[2m 2^(l+1) + q]
+                buf[o] = cadd(u0[i], v0[i]);
+                buf[o + 2 * al] = csub(u0[i], v0[i]);
+                buf[o + al] = cadd(u1[i], v1[i]);
+                buf[o + 3 * al] = csub(u1[i], v1[i]);
+            }
+            __syncthreads();
+        }
+    }
+    for (; l < np - 1; l++) {
+        const int al = 1 << l, mask = al - 1;
+        float2 a[BPT], b[BPT];
+#pragma unroll
+        for (int i = 0; i < BPT; i++) {
+            const int j = tid + i * NT;
+            a[i] = buf[j];
+            b[i] = cmul(buf[j + half], __ldg(tw + al + (j & mask)));
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < BPT; i++) {
+            const int j = tid + i * NT;
+            const int o = 2 * j - (j & mask);
+            buf[o] = cadd(a[i], b[i]);
+            buf[o + al] = csub(a[i], b[i]);
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // R5+R6+R7: filter one row per CTA.  Shared memory: buf[n] complex (in-place radix-2 passes with
 // a register hand-off between read and write phases) and strip[ixdim] shorts; the twiddles come
@@ -147,24 +211,7 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         buf[2 * j + 1] = csub(a[i], b[i]);
     }
     __syncthreads();
-    for (int l = 1; l < np - 1; l++) {
-        const int al = 1 << l, mask = al - 1;
-#pragma unroll
-        for (int i = 0; i < BPT; i++) {
-            const int j = tid + i * NT;
-            a[i] = buf[j];
-            b[i] = cmul(buf[j + half], __ldg(tw + al + (j & mask)));
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < BPT; i++) {
-            const int j = tid + i * NT;
-            const int o = 2 * j - (j & mask);
-            buf[o] = cadd(a[i], b[i]);
-            buf[o + al] = csub(a[i], b[i]);
-        }
-        __syncthreads();
-    }
+    fft_general_passes<BPT>(buf, tw, np, half, tid, NT);
     // last forward pass writes reversed (source/cfft.cpp:246-265); the filter multiply
     // (source/general.cpp:2128, CCmplx::operator*=(float)) is applied on the way out.
 #pragma unroll
@@ -200,24 +247,7 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         buf[2 * j + 1] = csub(a[i], b[i]);
     }
     __syncthreads();
-    for (int l = 1; l < np - 1; l++) {
-        const int al = 1 << l, mask = al - 1;
-#pragma unroll
-        for (int i = 0; i < BPT; i++) {
-            const int j = tid + i * NT;
-            a[i] = buf[j];
-            b[i] = cmul(buf[j + half], __ldg(tw + al + (j & mask)));
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < BPT; i++) {
-            const int j = tid + i * NT;
-            const int o = 2 * j - (j & mask);
-            buf[o] = cadd(a[i], b[i]);
-            buf[o + al] = csub(a[i], b[i]);
-        }
-        __syncthreads();
-    }
+    fft_general_passes<BPT>(buf, tw, np, half, tid, NT);
     // last inverse pass with the two halves swapped (source/cfft.cpp:355-368)
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
