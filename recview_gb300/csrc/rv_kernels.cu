@@ -33,28 +33,78 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(
 // expression in the reference (int*float, ushort+float, float-ushort); only the log ratio is in
 // double.  Fast path: FP32 log with an error bound of 7e-3 on v = 3000*log(I0/S) + 0.5; samples
 // whose v lies within 0.02 of an integer are recomputed in FP64 exactly as the reference does.
+// FP64 is slow on this GPU and a divergent FP64 branch costs its whole warp, so the row kernels
+// take the fast path for every sample first (norm_fast flags the ~4% it cannot decide) and run
+// the FP64 recheck (norm_exact) afterwards over a compacted list, 32 flagged samples per warp.
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ short norm_sample(int raw, int f0, int f1, int dark, float t0, int pixmin,
-                                             int zernike) {
+__device__ __forceinline__ float norm_incident(int f0, int f1, int dark, float t0) {
     const float prod = fmul((float)(f1 - f0), t0);
     const float s1 = fadd((float)f0, prod);
-    const float dinc = fsub(s1, (float)dark);
+    return fsub(s1, (float)dark);
+}
+// the sample, or (when *recheck is set) a placeholder to be replaced by norm_exact
+__device__ __forceinline__ short norm_fast(int raw, int f0, int f1, int dark, float t0, int pixmin, bool* recheck) {
+    *recheck = false;
+    const float dinc = norm_incident(f0, f1, dark, t0);
     if (!(dinc > 0.0f)) return 0;
     const int s = raw - dark;
     if (s < pixmin) return 0;
-    if (zernike) {
-        const double v = __dadd_rn(__ddiv_rn(__dmul_rn((double)dinc, 1000.0), (double)s), 0.5);
-        return (short)__double2int_rz(v);
-    }
     const float ratio = __fdiv_rn(dinc, (float)s);
     const float w = fadd(fmul(logf(ratio), 3000.0f), 0.5f);
     const float dist = fabsf(w - rintf(w));
     if (dist > 0.02f) return (short)__float2int_rz(w);
+    *recheck = true;
+    return 0;
+}
+// a sample that norm_fast flagged (so dinc > 0 and s >= pixmin): the reference's FP64 value
+__device__ __forceinline__ short norm_exact(int raw, int f0, int f1, int dark, float t0) {
+    const float dinc = norm_incident(f0, f1, dark, t0);
+    const int s = raw - dark;
     const double vd = __dadd_rn(__dmul_rn(log(__ddiv_rn((double)dinc, (double)s)), 3000.0), 0.5);
     return (short)__double2int_rz(vd);
 }
+// the Zernike-phase form (always FP64 in the reference)
+__device__ __forceinline__ short norm_zernike(int raw, int f0, int f1, int dark, float t0, int pixmin) {
+    const float dinc = norm_incident(f0, f1, dark, t0);
+    if (!(dinc > 0.0f)) return 0;
+    const int s = raw - dark;
+    if (s < pixmin) return 0;
+    const double v = __dadd_rn(__ddiv_rn(__dmul_rn((double)dinc, 1000.0), (double)s), 0.5);
+    return (short)__double2int_rz(v);
+}
+
+// Normalises row `job` into out[0..W) (out[x] = sample x - sh, zero outside) with the deferred
+// FP64 recheck; relist (>= W ints of shared memory) and *count (a shared counter, zero on entry)
+// hold the flagged positions.  Ends with a block barrier.
+__device__ __forceinline__ void normalise_row(const uint16_t* r, const uint16_t* f0, const uint16_t* f1,
+                                              const uint16_t* dk, int W, int sh, bool zero, float t0, int pixmin,
+                                              int zernike, short* out, int* relist, int* count) {
+    const int tid = threadIdx.x, NT = blockDim.x;
+    for (int x = tid; x < W; x += NT) {
+        short v = 0;
+        const int j = x - sh;  // drift shift (source/general.cpp:2505-2517)
+        if (!zero && j >= 0 && j < W) {
+            if (zernike) {
+                v = norm_zernike(r[j], f0[j], f1[j], dk[j], t0, pixmin);
+            } else {
+                bool re;
+                v = norm_fast(r[j], f0[j], f1[j], dk[j], t0, pixmin, &re);
+                if (re) relist[atomicAdd(count, 1)] = x;
+            }
+        }
+        out[x] = v;
+    }
+    __syncthreads();
+    const int n = *count;
+    for (int i = tid; i < n; i += NT) {
+        const int x = relist[i], j = x - sh;
+        out[x] = norm_exact(r[j], f0[j], f1[j], dk[j], t0);
+    }
+    __syncthreads();
+}
 
 __global__ void k_normalise(NormLaunch p) {
+    extern __shared__ int sm_norm[];   // [0]: recheck count, [1 ..]: flagged positions
     const RowJob job = p.jobs[blockIdx.x];
     const int W = p.ixdim;
     const uint16_t* r = p.raw + (size_t)job.src_row * W;
@@ -63,18 +113,17 @@ __global__ void k_normalise(NormLaunch p) {
     const uint16_t* dk = p.raw + (size_t)job.dark_row * W;
     short* out = p.out + (size_t)job.dst * W;
     const int sh = p.shift ? p.shift[blockIdx.x] : 0;
-    for (int x = threadIdx.x; x < W; x += blockDim.x) {
-        short v = 0;
-        const int j = x - sh;  // drift shift (source/general.cpp:2505-2517)
-        if (!job.zero && j >= 0 && j < W)
-            v = norm_sample(r[j], f0[j], f1[j], dk[j], job.t0, p.pixmin, p.zernike);
-        out[x] = v;
-    }
+    if (threadIdx.x == 0) sm_norm[0] = 0;
+    __syncthreads();
+    normalise_row(r, f0, f1, dk, W, sh, job.zero != 0, job.t0, p.pixmin, p.zernike, out, sm_norm + 1, sm_norm);
 }
 
 cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
     if (p.njobs <= 0) return cudaSuccess;
-    k_normalise<<<p.njobs, 256, 0, s>>>(p);  // one CTA per row
+    const size_t smem = ((size_t)p.ixdim + 1) * sizeof(int);
+    cudaError_t e = cudaFuncSetAttribute(k_normalise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_normalise<<<p.njobs, 256, smem, s>>>(p);  // one CTA per row
     return cudaGetLastError();
 }
 
@@ -163,18 +212,19 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
 
     // ---- sinogram row (R1 on the fly for raw frames) -------------------------------------------
     if (p.raw) {
+        // the FFT buffer is free until the placement: it holds the recheck list meanwhile
+        __shared__ int s_nre;
+        if (tid == 0) s_nre = 0;
+        __syncthreads();
         const uint16_t* base = static_cast<const uint16_t*>(p.src);
-        const uint16_t* r = base + (size_t)job.src_row * W;
-        const uint16_t* f0 = base + (size_t)job.flat0_row * W;
-        const uint16_t* f1 = base + (size_t)job.flat1_row * W;
-        const uint16_t* dk = base + (size_t)job.dark_row * W;
-        for (int x = tid; x < W; x += NT)
-            strip[x] = job.zero ? (short)0 : norm_sample(r[x], f0[x], f1[x], dk[x], job.t0, p.pixmin, 0);
+        normalise_row(base + (size_t)job.src_row * W, base + (size_t)job.flat0_row * W,
+                      base + (size_t)job.flat1_row * W, base + (size_t)job.dark_row * W, W, 0, job.zero != 0, job.t0,
+                      p.pixmin, 0, strip, reinterpret_cast<int*>(buf), &s_nre);
     } else {
         const short* r = static_cast<const short*>(p.src) + (size_t)job.src_row * W;
         for (int x = tid; x < W; x += NT) strip[x] = job.zero ? (short)0 : r[x];
+        __syncthreads();
     }
-    __syncthreads();
     // ---- R5: placement with edge padding and integer zoom (source/general.cpp:2105-2126) ------
     {
         const int z = p.d.iIntpDim;
