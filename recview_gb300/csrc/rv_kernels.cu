@@ -80,7 +80,35 @@ __device__ __forceinline__ void normalise_row(const uint16_t* r, const uint16_t*
                                               const uint16_t* dk, int W, int sh, bool zero, float t0, int pixmin,
                                               int zernike, short* out, int* relist, int* count) {
     const int tid = threadIdx.x, NT = blockDim.x;
-    for (int x = tid; x < W; x += NT) {
+    const bool vec = sh == 0 && !zernike && (W & 3) == 0 &&
+                     ((reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(f0) | reinterpret_cast<uintptr_t>(f1) |
+                       reinterpret_cast<uintptr_t>(dk) | reinterpret_cast<uintptr_t>(out)) & 7) == 0;
+    if (vec) {
+        // four samples per thread and step, all four rows loaded before any arithmetic
+        for (int x4 = tid; x4 < (W >> 2); x4 += NT) {
+            const uint2 vr = __ldg(reinterpret_cast<const uint2*>(r) + x4);
+            const uint2 v0 = __ldg(reinterpret_cast<const uint2*>(f0) + x4);
+            const uint2 v1 = __ldg(reinterpret_cast<const uint2*>(f1) + x4);
+            const uint2 vd = __ldg(reinterpret_cast<const uint2*>(dk) + x4);
+            short o[4] = {0, 0, 0, 0};
+            if (!zero) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int sft = 16 * (k & 1);
+                    const unsigned wr = k < 2 ? vr.x : vr.y, w0 = k < 2 ? v0.x : v0.y;
+                    const unsigned w1 = k < 2 ? v1.x : v1.y, wd = k < 2 ? vd.x : vd.y;
+                    bool re;
+                    o[k] = norm_fast((int)((wr >> sft) & 0xffffu), (int)((w0 >> sft) & 0xffffu),
+                                     (int)((w1 >> sft) & 0xffffu), (int)((wd >> sft) & 0xffffu), t0, pixmin, &re);
+                    if (re) relist[atomicAdd(count, 1)] = 4 * x4 + k;
+                }
+            }
+            reinterpret_cast<uint2*>(out)[x4] =
+                make_uint2((unsigned)(unsigned short)o[0] | ((unsigned)(unsigned short)o[1] << 16),
+                           (unsigned)(unsigned short)o[2] | ((unsigned)(unsigned short)o[3] << 16));
+        }
+    }
+    for (int x = vec ? W : tid; x < W; x += NT) {
         short v = 0;
         const int j = x - sh;  // drift shift (source/general.cpp:2505-2517)
         if (!zero && j >= 0 && j < W) {
@@ -231,14 +259,18 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         const int ic = p.ic_per_job ? job.ic : p.ic;
         const int idx0 = (0 - ic) * z + (half - 1);
         const int idx1 = (W - 1 - ic) * z + (half - 1) + 1;
+        // z = 2^iZooming: C's truncating division by z as shifts (a negative numerator is biased
+        // by z - 1 first)
+        const int lz = __ffs(z) - 1;
+        auto divz = [&](int x) { return (x + ((x >> 31) & (z - 1))) >> lz; };
         for (int m = tid; m < n; m += NT) {
             float v;
             if (m < idx0) v = strip[0];
             else if (m >= idx1) v = strip[W - 1];
             else {
-                const int k = (m - idx0) / z, j = (m - idx0) - k * z;
+                const int k = (m - idx0) >> lz, j = (m - idx0) & (z - 1);
                 if (j == 0) v = strip[k];
-                else v = (float)((int)strip[k] * (z - j) / z + (int)strip[k + 1] * j / z);
+                else v = (float)(divz((int)strip[k] * (z - j)) + divz((int)strip[k + 1] * j));
             }
             buf[m] = make_float2(v, 0.0f);
         }
