@@ -682,23 +682,24 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_pipe_persistent(c
 }
 
 // ---- warp-specialised producer, ray-aligned lane footprints ------------------------------------
-// Two changes to the warp-decoupled pipeline above, each bit-identical.
+// Changes to the warp-decoupled pipeline above, each bit-identical.
 //
-// Producer warp.  A ninth warp only fills window buffers: it waits for a buffer's empty barrier,
-// records the views' windows and issues their TMA copies, so the eight consumer warps never wait
-// for a fill that a busy consumer has not issued yet, and all of them do the same work.
+// Producer warp.  One extra warp only fills window buffers: it waits for a buffer's empty
+// barrier, records the views' windows and issues their TMA copies, so the CW consumer warps never
+// wait for a fill that a busy consumer has not issued yet, and all of them do the same work.
 //
 // Ray-aligned footprints (NQ > 0).  A warp's 32 lookups of one view cost one shared-memory
 // wavefront per distinct word in its busiest bank.  A compact 8x4 pixel block spreads the lanes'
 // indices over ~100 words (2.3 wavefronts per gather).  Here every register of a warp holds 32
 // pixels along one line of the view's iso-index direction (x*fcos + y*fsin = const), so its
 // indices fall within a few dozen consecutive words (~1.3 wavefronts).
-// Layouts: a 64x64 tile, 8 consumer warps, 16 accumulators per thread in slots s = 2q + p
-// (q 0..7, p 0..1); w = warp, j = lane.  A regime is an orientation and a shear k in [-NQ, NQ]:
-//     V (|fcos| >= |fsin|):  x = (w + sh(j) + 8q) mod 64,  y = j + 32p,   sh(j) = round(j k / NQ)
-//     H (|fsin| >  |fcos|):  x = j + 32p,  y = (w + sh(j) + 8q) mod 64
-// Each maps (w, j, q, p) one-to-one onto the tile, and a thread's 16 pixels are 8 sheared x 2
-// fixed coordinates, so the per-view products cost 8 + 2*2 (V) or 2 + 8*2 (H) FP32 operations.
+// Layouts: a 64x64 tile, CW consumer warps (8 or 16), Q = 64 / CW sheared coordinates per thread,
+// 2Q accumulators per thread and slice in slots s = 2q + p (q < Q, p 0..1); w = warp, j = lane.
+// A regime is an orientation and a shear k in [-NQ, NQ]:
+//     V (|fcos| >= |fsin|):  x = (w + sh(j) + CW q) mod 64,  y = j + 32p,   sh(j) = round(j k / NQ)
+//     H (|fsin| >  |fcos|):  x = j + 32p,  y = (w + sh(j) + CW q) mod 64
+// Each maps (w, j, q, p) one-to-one onto the tile, and a thread's pixels are Q sheared x 2 fixed
+// coordinates, so the per-view products cost Q + 2*2 (V) or 2 + 2Q (H) FP32 operations.
 // The regime of a chunk follows from the geometry of its first view (every consumer computes
 // the same value).  When it changes, the accumulators move through the buffer just consumed,
 // between barriers of the consumer warps: written at (slot, thread), read back from the old owner
@@ -706,33 +707,42 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_ref_pipe_persistent(c
 // so that exchange is free of bank conflicts.  Every pixel still sums the same int32 entries over
 // the same views.
 //
-// Failure protocol.  The consumer barriers of an exchange need all eight consumer warps, so a
-// warp whose bounded wait ran out does not leave the loop: it raises the CTA's abort word (the
-// others then skip their waits), skips the rest of its work, and the consumers leave together at
-// the next exchange or after the last chunk; the producer stops at the abort word or at its own
-// bounded wait.  All 288 threads then meet at one block barrier.
-__device__ __forceinline__ bool consumers_bar_or(bool pred) {   // named barrier 1: the 256 consumers
+// Slice pairs (NS = 2).  Two slices that share the geometry share every index: a pixel's second
+// gather is one more shared load at a fixed offset (the second slice's window follows the first)
+// and one more add.
+//
+// Failure protocol.  The consumer barriers of an exchange need all consumer warps, so a warp
+// whose bounded wait ran out does not leave the loop: it raises the CTA's abort word (the others
+// then skip their waits), skips the rest of its work, and the consumers leave together at the
+// next exchange or after the last chunk; the producer stops at the abort word or at its own
+// bounded wait.  All threads then meet at one block barrier.
+template <int CW>
+__device__ __forceinline__ bool consumers_bar_or(bool pred) {   // named barrier 1: the consumers
     unsigned r;
     asm volatile(
-        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, 256, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
         : "=r"(r)
-        : "r"((unsigned)pred)
+        : "r"((unsigned)pred), "n"(32 * CW)
         : "memory");
     return r != 0;
 }
-__device__ __forceinline__ void consumers_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+template <int CW>
+__device__ __forceinline__ void consumers_bar() {
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * CW) : "memory");
+}
 
-template <int VC, int NB, int PAD, int NS = 1>
+template <int VC, int NB, int PAD, int NS = 1, int CW = 8>
 struct WsCfg {
     using Pipe = PipeCfg<2, 4, 4, 4, VC, NB, PAD>;   // 64x64 tile: the same window size
-    static constexpr int NT = 288;                   // 8 consumer warps + 1 producer warp
+    static constexpr int NT = 32 * CW + 32;          // CW consumer warps + 1 producer warp
+    static constexpr int Q = 64 / CW, S = 2 * Q;     // sheared coordinates and pixels per thread
     static constexpr int TX = Pipe::TX, TY = Pipe::TY, ALIGN = Pipe::ALIGN, WIN = Pipe::WIN;
     static constexpr int META_OFF = NB * VC * NS * WIN;      // words: windows [NB][VC][NS][WIN]
     static constexpr int BAR_OFF = META_OFF + NB * VC * 8;   // view records [NB][VC]
     static constexpr int ABORT_OFF = BAR_OFF + 4 * NB;       // after full[NB], empty[NB]
     static constexpr size_t SMEM = (size_t)ABORT_OFF * 4 + 16;
-    static constexpr bool EXCHANGE_FITS = VC * WIN >= 16 * 256;   // one buffer holds the exchange
-    static_assert(TX == 64 && TY == 64 && Pipe::NT == 256, "8 consumer warps tile 64x64 pixels");
+    static constexpr bool EXCHANGE_FITS = VC * WIN >= 4096;   // one buffer holds a slice's exchange
+    static_assert(TX == 64 && TY == 64 && (CW == 8 || CW == 16), "8 or 16 consumer warps tile 64x64 pixels");
 };
 
 // regime = orientation (bit 0: H) | (k + NQ) << 1, from a view's fcos, fsin; any value gives the
@@ -753,22 +763,17 @@ __device__ __forceinline__ int ray_shift(int j, int regime) {
     return NQ > 0 ? (2 * j * k + NQ + 128 * NQ) / D - 64 : 0;
 }
 // the thread's sheared (lin) and fixed (fix) absolute pixel coordinates under a regime
-template <int NQ>
-__device__ __forceinline__ void ray_coords(int regime, int X0, int Y0, int warp, int lane, float (&lin)[8],
+template <int NQ, int CW>
+__device__ __forceinline__ void ray_coords(int regime, int X0, int Y0, int warp, int lane, float (&lin)[64 / CW],
                                            float (&fix)[2]) {
     const int sh = ray_shift<NQ>(lane, regime);
     const int lb = (regime & 1) ? Y0 : X0, fb = (regime & 1) ? X0 : Y0;
 #pragma unroll
-    for (int q = 0; q < 8; q++) lin[q] = (float)(lb + ((warp + sh + 8 * q) & 63));
+    for (int q = 0; q < 64 / CW; q++) lin[q] = (float)(lb + ((warp + sh + CW * q) & 63));
 #pragma unroll
     for (int p = 0; p < 2; p++) fix[p] = (float)(fb + lane + 32 * p);
 }
 
-// acc[sl][s] += the table entry of slot s's pixel in slice sl, for one view of a staged chunk.
-// fx2(i) gives fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of the two pixels of slot pair i
-// (slots ws_slot<COMPACT>(i, 0) and (i, 1)), formed with the paired FP32 instructions (each lane
-// rounds like the scalar operation).  The NS slices share the index, so a second slice costs one
-// more shared load (its window sits WIN words further) and one add.
 __device__ __forceinline__ float2 bcast2(float v) { return make_float2(v, v); }
 // Paired FP32 additions (two lanes per instruction), each lane rounded like the scalar addition.
 // Only additions are paired: the compiler fuses a paired multiply into a following paired add
@@ -795,13 +800,16 @@ __device__ __forceinline__ float2 add2_rz(float2 a, float2 b) {
     return upk2(d);
 }
 
+// slot of half h of slot pair i.  Ray layouts: slot 2q + p, pairs (q, q+1) at even q;
+// compact (8 consumer warps): slot 4r + c, pairs (c, c+1)
 template <bool COMPACT>
 __device__ __forceinline__ constexpr int ws_slot(int i, int h) {
-    // ray layouts: slot 2q + p, pairs (q, q+1) at even q;  compact: slot 4r + c, pairs (c, c+1)
     return COMPACT ? 4 * (i >> 1) + 2 * (i & 1) + h : 4 * (i >> 1) + (i & 1) + 2 * h;
 }
-template <int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, bool COMPACT, typename FX2>
-__device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, const ViewMeta* meta, int b, int vv,
+// acc[sl][s] += the table entry of slot s's pixel in slice sl, for one view of a staged chunk.
+// fx2(i) gives fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of the two pixels of slot pair i.
+template <int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, bool COMPACT, int S, typename FX2>
+__device__ __forceinline__ void ws_gather(int (&acc)[NS][S], const int* win, const ViewMeta* meta, int b, int vv,
                                           unsigned offb, unsigned& viol, FX2 fx2) {
     const unsigned base = smem_u32(win + (b * VC + vv) * NSL * WIN) + (offb & ~3u);
     int cw0 = 0, cnw = 0;
@@ -812,7 +820,7 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, co
     if (offb & 1u) {
         const float2 mag = make_float2(8388608.0f, 8388608.0f);
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
+        for (int i = 0; i < S / 2; i++) {
             const float2 fx = fx2(i);
             const float2 t = add2_rz(fx, mag);
 #pragma unroll
@@ -832,7 +840,7 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, co
         }
     } else {
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
+        for (int i = 0; i < S / 2; i++) {
             const float2 fx = fx2(i);
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -850,13 +858,14 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][16], const int* win, co
     }
 }
 
-
-// one chunk of views: NQ == 0 compact blocks (colf/rowf in lin[0..3] / lin[4..7]), else the
-// ray layout of orientation O.  Products and y terms are scalar (fl(x fcos), fl(fl(y fsin) +
-// foffset)); the per-pixel sums are paired.
-template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL>
-__device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin)[8], const float (&fix)[2],
-                                           const int* win, const ViewMeta* meta, int b, int nv, unsigned& viol) {
+// one chunk of views: NQ == 0 compact blocks (8 consumer warps; colf/rowf in lin[0..3] /
+// lin[4..7]), else the ray layout of orientation O.  Products and y terms are scalar
+// (fl(x fcos), fl(fl(y fsin) + foffset)); the per-pixel sums are paired.
+template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, int CW>
+__device__ __forceinline__ void ws_consume(int (&acc)[NS][128 / CW], const float (&lin)[64 / CW],
+                                           const float (&fix)[2], const int* win, const ViewMeta* meta, int b,
+                                           int nv, unsigned& viol) {
+    constexpr int Q = 64 / CW, S = 2 * Q;
     for (int vv = 0; vv < nv; vv++) {
         const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
         const unsigned offb = __float_as_uint(g.w);
@@ -865,36 +874,36 @@ __device__ __forceinline__ void ws_consume(int (&acc)[NS][16], const float (&lin
 #pragma unroll
             for (int k = 0; k < 2; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
 #pragma unroll
-            for (int r = 0; r < 4; r++) Yb[r] = bcast2(faddr(fmulr(lin[4 + r], g.y), g.z));
-            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, true>(acc, win, meta, b, vv, offb, viol,
-                                                       [&](int i) { return add2_rn(X[i & 1], Yb[i >> 1]); });
+            for (int r = 0; r < 4; r++) Yb[r] = bcast2(faddr(fmulr(lin[(4 + r) % Q], g.y), g.z));
+            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, true, S>(acc, win, meta, b, vv, offb, viol,
+                                                               [&](int i) { return add2_rn(X[i & 1], Yb[i >> 1]); });
         } else if (O == 0) {   // V: x = lin[q], y = fix[p]
-            float2 X[4];
+            float2 X[Q / 2];
 #pragma unroll
-            for (int k = 0; k < 4; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
+            for (int k = 0; k < Q / 2; k++) X[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
             const float2 Y0 = bcast2(faddr(fmulr(fix[0], g.y), g.z)), Y1 = bcast2(faddr(fmulr(fix[1], g.y), g.z));
-            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, false>(acc, win, meta, b, vv, offb, viol,
-                                                        [&](int i) { return add2_rn(X[i >> 1], (i & 1) ? Y1 : Y0); });
+            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, false, S>(
+                acc, win, meta, b, vv, offb, viol, [&](int i) { return add2_rn(X[i >> 1], (i & 1) ? Y1 : Y0); });
         } else {   // H: x = fix[p], y = lin[q]
-            float2 Y[4];
+            float2 Y[Q / 2];
 #pragma unroll
-            for (int k = 0; k < 4; k++)
+            for (int k = 0; k < Q / 2; k++)
                 Y[k] = make_float2(faddr(fmulr(lin[2 * k], g.y), g.z), faddr(fmulr(lin[2 * k + 1], g.y), g.z));
             const float2 X0 = bcast2(fmulr(fix[0], g.x)), X1 = bcast2(fmulr(fix[1], g.x));
-            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, false>(acc, win, meta, b, vv, offb, viol,
-                                                        [&](int i) { return add2_rn((i & 1) ? X1 : X0, Y[i >> 1]); });
+            ws_gather<VC, WIN, PAD, CHECKED, NS, NSL, false, S>(
+                acc, win, meta, b, vv, offb, viol, [&](int i) { return add2_rn((i & 1) ? X1 : X0, Y[i >> 1]); });
         }
     }
 }
 
-template <int VC, int NB, int PAD, int NS>
+template <int VC, int NB, int PAD, int NS, int CW>
 __device__ __forceinline__ void ws_init(int* smi) {
-    using Cfg = WsCfg<VC, NB, PAD, NS>;
+    using Cfg = WsCfg<VC, NB, PAD, NS, CW>;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);
     if (threadIdx.x == 0) {
         for (int b = 0; b < NB; b++) {
             mbar_init(smem_u32(&bars[b]), 1);
-            mbar_init(smem_u32(&bars[NB + b]), 8);   // one arrival per consumer warp
+            mbar_init(smem_u32(&bars[NB + b]), CW);   // one arrival per consumer warp
         }
         smi[Cfg::ABORT_OFF] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -902,15 +911,17 @@ __device__ __forceinline__ void ws_init(int* smi) {
 }
 
 // One 64x64 tile of NS slices (NS = 2: J and a second slice with the same geometry, tables
-// table2, output out2); gc as in bp_ref_tile_pipe.  Returns false (for the whole CTA) after a
-// bounded wait ran out.  Warps 0-7 consume, warp 8 produces.
-template <int VC, int NB, int PAD, int NQ, bool CHECKED, int NS = 1, int NSL = NS>
+// table2, output out2) in a buffer layout of NSL windows per view; gc as in bp_ref_tile_pipe.
+// Returns false (for the whole CTA) after a bounded wait ran out.  Warps 0 .. CW-1 consume, warp
+// CW produces.
+template <int VC, int NB, int PAD, int NQ, bool CHECKED, int NS = 1, int NSL = NS, int CW = 8>
 __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter,
                                                const int* table2 = nullptr, int* out2 = nullptr) {
-    using Cfg = WsCfg<VC, NB, PAD, NSL>;
+    using Cfg = WsCfg<VC, NB, PAD, NSL, CW>;
+    constexpr int WIN = Cfg::WIN, Q = Cfg::Q, S = Cfg::S, NC = 32 * CW;
     static_assert(NS <= NSL, "the buffer layout holds NSL windows per view");
     static_assert(NQ == 0 || Cfg::EXCHANGE_FITS, "the accumulator exchange needs 4096 words per slice in one buffer");
-    constexpr int WIN = Cfg::WIN;
+    static_assert(NQ > 0 || CW == 8, "the compact layout is laid out for 8 consumer warps");
     int* win = smi;                                                     // [NB][VC][NSL][WIN]
     ViewMeta* meta = reinterpret_cast<ViewMeta*>(smi + Cfg::META_OFF);  // [NB][VC]
     uint64_t* bars = reinterpret_cast<uint64_t*>(smi + Cfg::BAR_OFF);   // full[NB], empty[NB]
@@ -922,7 +933,7 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
     const int nchunks = (nviews + VC - 1) / VC;
     bool failed = false;   // warp-uniform
     int produced = 0;      // producer: chunks of this tile whose fill has been issued
-    if (warp == 8) {
+    if (warp == CW) {
         for (; produced < nchunks; produced++) {
             if (__any_sync(0xffffffffu, *abortw != 0)) {
                 failed = true;
@@ -937,12 +948,12 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
         }
     } else {
         unsigned viol = 0;
-        int acc[NS][16];
+        int acc[NS][S];
 #pragma unroll
         for (int sl = 0; sl < NS; sl++)
 #pragma unroll
-            for (int s = 0; s < 16; s++) acc[sl][s] = 0;
-        float lin[8], fix[2];
+            for (int s = 0; s < S; s++) acc[sl][s] = 0;
+        float lin[Q], fix[2];
         int regime = 0;
         float2 gnext = make_float2(0.0f, 0.0f);   // fcos, fsin of the first view of chunk k + 1
         if (NQ > 0) {
@@ -954,13 +965,13 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 const float4 g1 = __ldg(J.geom + VC);
                 gnext = make_float2(g1.x, g1.y);
             }
-            ray_coords<NQ>(regime, X0, Y0, warp, lane, lin, fix);
+            ray_coords<NQ, CW>(regime, X0, Y0, warp, lane, lin, fix);
         } else {
             const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
 #pragma unroll
-            for (int c = 0; c < 4; c++) lin[c] = (float)(X0 + tx + 16 * c);
+            for (int c = 0; c < 4; c++) lin[c % Q] = (float)(X0 + tx + 16 * c);
 #pragma unroll
-            for (int r = 0; r < 4; r++) lin[4 + r] = (float)(Y0 + ty + 16 * r);
+            for (int r = 0; r < 4; r++) lin[(4 + r) % Q] = (float)(Y0 + ty + 16 * r);
             fix[0] = fix[1] = 0.0f;
         }
         for (int k = 0; k < nchunks; k++) {
@@ -971,9 +982,9 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
             if (!failed) {
                 const int nv = min(VC, nviews - k * VC);
                 if (NQ == 0 || !(regime & 1))
-                    ws_consume<NQ, 0, VC, WIN, PAD, CHECKED, NS, NSL>(acc, lin, fix, win, meta, b, nv, viol);
+                    ws_consume<NQ, 0, VC, WIN, PAD, CHECKED, NS, NSL, CW>(acc, lin, fix, win, meta, b, nv, viol);
                 else
-                    ws_consume<NQ, 1, VC, WIN, PAD, CHECKED, NS, NSL>(acc, lin, fix, win, meta, b, nv, viol);
+                    ws_consume<NQ, 1, VC, WIN, PAD, CHECKED, NS, NSL, CW>(acc, lin, fix, win, meta, b, nv, viol);
             } else if (lane == 0) {
                 *abortw = 1;
             }
@@ -989,33 +1000,33 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 }
                 if (next != regime) {
                     // every consumer is done reading buffer b and none has released it: exchange
-                    if (consumers_bar_or(failed)) {
+                    if (consumers_bar_or<CW>(failed)) {
                         failed = true;
                         break;
                     }
-                    int* xs = win + b * VC * NSL * WIN;   // [NS][16 slots][256 threads]
+                    int* xs = win + b * VC * NSL * WIN;   // [NS][S slots][NC threads]
 #pragma unroll
                     for (int sl = 0; sl < NS; sl++)
 #pragma unroll
-                        for (int s = 0; s < 16; s++) xs[(sl * 16 + s) * 256 + tid] = acc[sl][s];
-                    consumers_bar();
+                        for (int s = 0; s < S; s++) xs[(sl * S + s) * NC + tid] = acc[sl][s];
+                    consumers_bar<CW>();
                     const int on = next & 1, oo = regime & 1;
                     const int shn = ray_shift<NQ>(lane, next);
 #pragma unroll
-                    for (int q = 0; q < 8; q++)
+                    for (int q = 0; q < Q; q++)
 #pragma unroll
                         for (int p = 0; p < 2; p++) {
-                            const int u = (warp + shn + 8 * q) & 63, f = lane + 32 * p;   // new layout
+                            const int u = (warp + shn + CW * q) & 63, f = lane + 32 * p;   // new layout
                             const int xr = on ? f : u, yr = on ? u : f;
-                            const int a = oo ? xr : yr, c = oo ? yr : xr;                  // old fixed / sheared
+                            const int a = oo ? xr : yr, c = oo ? yr : xr;                   // old fixed / sheared
                             const int jj = a & 31, pp = a >> 5;
-                            const int m = (c - ray_shift<NQ>(jj, regime)) & 63;             // old w + 8 q
-                            const int src = ((m >> 3) * 2 + pp) * 256 + (m & 7) * 32 + jj;
+                            const int m = (c - ray_shift<NQ>(jj, regime)) & 63;              // old w + CW q
+                            const int src = ((m / CW) * 2 + pp) * NC + (m % CW) * 32 + jj;
 #pragma unroll
-                            for (int sl = 0; sl < NS; sl++) acc[sl][2 * q + p] = xs[sl * 4096 + src];
+                            for (int sl = 0; sl < NS; sl++) acc[sl][2 * q + p] = xs[sl * S * NC + src];
                         }
                     regime = next;
-                    ray_coords<NQ>(regime, X0, Y0, warp, lane, lin, fix);
+                    ray_coords<NQ, CW>(regime, X0, Y0, warp, lane, lin, fix);
                     // these generic accesses come before the next TMA fill of buffer b
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 }
@@ -1030,13 +1041,13 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
             const int sh = NQ > 0 ? ray_shift<NQ>(lane, regime) : 0;
             const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
 #pragma unroll
-            for (int s = 0; s < 16; s++) {
+            for (int s = 0; s < S; s++) {
                 int x, y;
                 if (NQ == 0) {
                     x = X0 + tx + 16 * (s & 3);
                     y = Y0 + ty + 16 * (s >> 2);
                 } else {
-                    const int u = (warp + sh + 8 * (s >> 1)) & 63, f = lane + 32 * (s & 1);
+                    const int u = (warp + sh + CW * (s >> 1)) & 63, f = lane + 32 * (s & 1);
                     x = X0 + ((regime & 1) ? f : u);
                     y = Y0 + ((regime & 1) ? u : f);
                 }
@@ -1051,7 +1062,7 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
         if (tid == 0) atomicOr(&g_kernel_status, 1u);
         // the producer's fills up to chunk `produced`: give them a bounded chance to land before
         // the CTA can leave
-        if (warp == 8) {
+        if (warp == CW) {
             for (int c = produced > NB ? produced - NB : 0; c < produced; c++) {
                 const unsigned g = gc + (unsigned)c;
                 mbar_wait_bounded(smem_u32(&bars[g % NB]), (g / NB) & 1u);
@@ -1064,10 +1075,10 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
 
 // grid (tiles, slices / NS): CTA row y covers slices slice0 + NS y (.. + NS - 1); NS = 2 needs
 // slices that share the geometry (geom_slice_stride 0)
-template <int VC, int NB, int PAD, int NQ, int MINB, bool CHECKED, int NS = 1>
-__global__ void __launch_bounds__(288, MINB) k_bp_ref_ws(BackprojLaunch p, int slice0) {
+template <int VC, int NB, int PAD, int NQ, int MINB, bool CHECKED, int NS = 1, int CW = 8>
+__global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws(BackprojLaunch p, int slice0) {
     extern __shared__ __align__(128) int smi[];
-    ws_init<VC, NB, PAD, NS>(smi);
+    ws_init<VC, NB, PAD, NS, CW>(smi);
     __syncthreads();
     const int tiles_x = (p.ixdimp + 63) / 64;
     const int sl = slice0 + NS * (int)blockIdx.y;
@@ -1080,17 +1091,18 @@ __global__ void __launch_bounds__(288, MINB) k_bp_ref_ws(BackprojLaunch p, int s
     J.ixdimp = p.ixdimp;
     J.X0 = (blockIdx.x % tiles_x) * 64;
     J.Y0 = (blockIdx.x / tiles_x) * 64;
-    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED, NS>(J, smi, 0u, p.status_counter, J.table + p.slice_table_stride,
-                                                 J.out + p.out_slice_stride);
+    J.pair = NS > 1;
+    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED, NS, NS, CW>(J, smi, 0u, p.status_counter,
+                                                         J.table + p.slice_table_stride, J.out + p.out_slice_stride);
 }
 
 // NSL = 2: jobs may cover slice pairs (TileJob::pair), in a layout with two windows per view
-template <int VC, int NB, int PAD, int NQ, int MINB, int NSL = 1>
-__global__ void __launch_bounds__(288, MINB) k_bp_ref_ws_persistent(const TileJob* jobs, int njobs,
-                                                                    unsigned* counter) {
+template <int VC, int NB, int PAD, int NQ, int MINB, int NSL = 1, int CW = 8>
+__global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws_persistent(const TileJob* jobs, int njobs,
+                                                                             unsigned* counter) {
     extern __shared__ __align__(128) int smi[];
     __shared__ int s_item;
-    ws_init<VC, NB, PAD, NSL>(smi);
+    ws_init<VC, NB, PAD, NSL, CW>(smi);
     unsigned gc = 0;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
@@ -1101,10 +1113,10 @@ __global__ void __launch_bounds__(288, MINB) k_bp_ref_ws_persistent(const TileJo
         const TileJob J = jobs[it];
         bool ok;
         if (NSL > 1 && J.pair)
-            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, (NSL > 1 ? 2 : 1), NSL>(
+            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, (NSL > 1 ? 2 : 1), NSL, CW>(
                 J, smi, gc, nullptr, J.table + (size_t)J.nviews * J.table_stride, J.out + (size_t)J.ixdimp * J.ixdimp);
         else
-            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, 1, NSL>(J, smi, gc, nullptr);
+            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, 1, NSL, CW>(J, smi, gc, nullptr);
         if (!ok) return;   // CTA-uniform
         gc += (unsigned)((J.nviews + VC - 1) / VC);
     }
@@ -1704,7 +1716,8 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //         of 1/8), 2 buffers x 6 views, 3 CTAs/SM;  17: the same with compact 8x4 lane blocks,
 //         2 buffers x 4 views, 4 CTAs/SM;  18: variant 16's layout over slice pairs (two
 //         slices sharing the geometry per CTA: one index per pixel and view, two gathers),
-//         2 buffers x 4 views x 2 slices, 2 CTAs/SM
+//         2 buffers x 4 views x 2 slices, 2 CTAs/SM;  19: variant 18 with 16 consumer warps
+//         (8 pixels x 2 slices per thread)
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -1759,11 +1772,11 @@ static cudaError_t go_pipe(const BackprojLaunch& p, cudaStream_t s, bool checked
     return launch_k(k_bp_ref_pipe<WX, WY, RX, RY, VC, NB, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
-template <int VC, int NB, int PAD, int NQ, int MINB, int NS = 1>
+template <int VC, int NB, int PAD, int NQ, int MINB, int NS = 1, int CW = 8>
 static cudaError_t go_ws_rows(const BackprojLaunch& p, cudaStream_t s, bool checked, int slice0, int rows) {
-    using Cfg = WsCfg<VC, NB, PAD, NS>;
+    using Cfg = WsCfg<VC, NB, PAD, NS, CW>;
     const int tiles = ((p.ixdimp + 63) / 64) * ((p.ixdimp + 63) / 64);
-    auto kern = checked ? k_bp_ref_ws<VC, NB, PAD, NQ, MINB, true, NS> : k_bp_ref_ws<VC, NB, PAD, NQ, MINB, false, NS>;
+    auto kern = checked ? k_bp_ref_ws<VC, NB, PAD, NQ, MINB, true, NS, CW> : k_bp_ref_ws<VC, NB, PAD, NQ, MINB, false, NS, CW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
     if (e != cudaSuccess) return e;
     kern<<<dim3(tiles, rows), Cfg::NT, Cfg::SMEM, s>>>(p, slice0);
@@ -1777,10 +1790,10 @@ static cudaError_t go_ws(const BackprojLaunch& p, cudaStream_t s, bool checked) 
 
 // slice pairs (two slices per CTA sharing the index arithmetic) when the slices share the
 // geometry; an odd last slice, or per-slice geometry, runs one slice per CTA (variant 16's form)
-template <int VC, int NB, int PAD, int NQ, int MINB>
+template <int VC, int NB, int PAD, int NQ, int MINB, int CW = 8>
 static cudaError_t go_ws_pairs(const BackprojLaunch& p, cudaStream_t s, bool checked) {
     if (p.geom_slice_stride != 0 || p.nslices < 2) return go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, 0, p.nslices);
-    cudaError_t e = go_ws_rows<VC, NB, PAD, NQ, MINB, 2>(p, s, checked, 0, p.nslices / 2);
+    cudaError_t e = go_ws_rows<VC, NB, PAD, NQ, MINB, 2, CW>(p, s, checked, 0, p.nslices / 2);
     if (e == cudaSuccess && (p.nslices & 1)) e = go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, p.nslices - 1, 1);
     return e;
 }
@@ -1815,6 +1828,7 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 16: return go_ws<6, 2, PAD, 8, 3>(p, s, checked);
     case 17: return go_ws<4, 2, PAD, 0, 4>(p, s, checked);
     case 18: return go_ws_pairs<4, 2, PAD, 8, 2>(p, s, checked);
+    case 19: return go_ws_pairs<4, 2, PAD, 8, 2, 16>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -1869,10 +1883,10 @@ static cudaError_t go_pipe_persistent(const TileJob* jobs, int njobs, unsigned* 
     return cudaGetLastError();
 }
 
-template <int VC, int NB, int PAD, int NQ, int MINB, int NSL = 1>
+template <int VC, int NB, int PAD, int NQ, int MINB, int NSL = 1, int CW = 8>
 static cudaError_t go_ws_persistent(const TileJob* jobs, int njobs, unsigned* counter, cudaStream_t s) {
-    using Cfg = WsCfg<VC, NB, PAD, NSL>;
-    auto kern = k_bp_ref_ws_persistent<VC, NB, PAD, NQ, MINB, NSL>;
+    using Cfg = WsCfg<VC, NB, PAD, NSL, CW>;
+    auto kern = k_bp_ref_ws_persistent<VC, NB, PAD, NQ, MINB, NSL, CW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
@@ -1919,6 +1933,7 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 15: return go_pipe_persistent<2, 4, 4, 4, 6, 2, PAD, 3>(jobs, njobs, counter, s);
     case 16: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
     case 18: return go_ws_persistent<4, 2, PAD, 8, 2, 2>(jobs, njobs, counter, s);
+    case 19: return go_ws_persistent<4, 2, PAD, 8, 2, 2, 16>(jobs, njobs, counter, s);
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
@@ -1979,7 +1994,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 18 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 19 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;

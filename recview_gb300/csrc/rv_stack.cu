@@ -598,7 +598,7 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
             const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
             // the slice-pair kernel takes two consecutive slices of a part per job (they share
             // the geometry and their tables follow each other in the pool)
-            const int step = q->variant == 18 ? 2 : 1;
+            const int step = (q->variant == 18 || q->variant == 19) ? 2 : 1;
             for (int sl = pt.s0; sl < pt.s1; sl += step)
                 for (int t = 0; t < ntx * nty; t++) {
                     TileJob J{};
@@ -705,7 +705,7 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
     // keeps the fastest for the captured graph
     if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
-    const int cands[] = {18, 16, 17, 11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
+    const int cands[] = {18, 19, 16, 17, 11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
     float best = 3.0e38f;
     int bestv = q->variant;
     for (int v : cands) {
