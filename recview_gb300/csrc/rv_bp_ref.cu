@@ -430,12 +430,12 @@ __device__ __forceinline__ void pipe_init_barriers(int* smi) {
 // TMA bulk copy per view on the buffer's full barrier.  Returns false (warp-uniform) when the wait
 // for the empty barrier ran out.
 // NS = 2 stages, for every view, the windows of two slices that share the geometry (the same
-// window bounds, tables J.table and table2) one after the other: window (b, vv, s) at
+// window bounds, tables J.table + s * slice_tab_stride) one after the other: window (b, vv, s) at
 // ((b * VC + vv) * NS + s) * WIN.
 // NSL (>= NS) is the number of window slots per view in the buffer layout.
 template <int TX, int TY, int WIN, int ALIGN, int VC, int NB, int PAD, int NS = 1, int NSL = NS>
 __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* meta, uint64_t* bars, int c,
-                                          unsigned g, int lane, const int* table2 = nullptr) {
+                                          unsigned g, int lane, long long slice_tab_stride = 0) {
     const int X0 = J.X0, Y0 = J.Y0;
     const int nviews = J.nviews;
     const int nstore = PAD ? ((17 * J.ixdimp + 3) & ~3) : 16 * J.ixdimp;
@@ -509,7 +509,7 @@ __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* 
             if (m.b <= m.a) continue;
 #pragma unroll
             for (int sl = 0; sl < NS; sl++) {
-                const int* src = (sl ? table2 : J.table) + (size_t)(v0 + vv) * J.table_stride + m.a;
+                const int* src = J.table + sl * slice_tab_stride + (size_t)(v0 + vv) * J.table_stride + m.a;
                 const unsigned dst = smem_u32(win + ((b * VC + vv) * NSL + sl) * WIN + (m.a - m.w0));
                 tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
             }
@@ -806,6 +806,15 @@ template <bool COMPACT>
 __device__ __forceinline__ constexpr int ws_slot(int i, int h) {
     return COMPACT ? 4 * (i >> 1) + 2 * (i & 1) + h : 4 * (i >> 1) + (i & 1) + 2 * h;
 }
+// acc[sl][s] += the entry at byte address a of slice sl's window (the NS windows of a view follow
+// each other WIN words apart, so every slice after the first is one load with a fixed offset)
+template <int NS, int WIN, int S>
+__device__ __forceinline__ void ws_add_slices(int (&acc)[NS][S], int s, unsigned a) {
+    acc[0][s] += lds_s32(a);
+    if (NS > 1) acc[1 % NS][s] += lds_s32_off<4 * WIN * (NS > 1 ? 1 : 0)>(a);
+    if (NS > 2) acc[2 % NS][s] += lds_s32_off<4 * WIN * (NS > 2 ? 2 : 0)>(a);
+    if (NS > 3) acc[3 % NS][s] += lds_s32_off<4 * WIN * (NS > 3 ? 3 : 0)>(a);
+}
 // acc[sl][s] += the table entry of slot s's pixel in slice sl, for one view of a staged chunk.
 // fx2(i) gives fl(fl(x fcos) + fl(fl(y fsin) + foffset)) of the two pixels of slot pair i.
 template <int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, bool COMPACT, int S, typename FX2>
@@ -833,9 +842,7 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][S], const int* win, con
                     const int sw = PAD ? v + (v >> 4) : v;
                     if ((h ? fx.y : fx.x) < 0.0f || sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
                 }
-                const unsigned a = base + 4u * st;
-                acc[0][s] += lds_s32(a);
-                if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
+                ws_add_slices<NS, WIN>(acc, s, base + 4u * st);
             }
         }
     } else {
@@ -850,9 +857,7 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][S], const int* win, con
                 if (CHECKED) {
                     if (sw < cw0 || sw >= cw0 + cnw) { viol++; continue; }
                 }
-                const unsigned a = base + 4u * (unsigned)sw;
-                acc[0][s] += lds_s32(a);
-                if (NS > 1) acc[NS - 1][s] += lds_s32_off<4 * WIN>(a);
+                ws_add_slices<NS, WIN>(acc, s, base + 4u * (unsigned)sw);
             }
         }
     }
@@ -910,16 +915,17 @@ __device__ __forceinline__ void ws_init(int* smi) {
     }
 }
 
-// One 64x64 tile of NS slices (NS = 2: J and a second slice with the same geometry, tables
-// table2, output out2) in a buffer layout of NSL windows per view; gc as in bp_ref_tile_pipe.
+// One 64x64 tile of NS slices that share the geometry (slice sl: tables J.table + sl * tstride,
+// output J.out + sl * ostride) in a buffer layout of NSL windows per view; gc as in
+// bp_ref_tile_pipe.
 // Returns false (for the whole CTA) after a bounded wait ran out.  Warps 0 .. CW-1 consume, warp
 // CW produces.
 template <int VC, int NB, int PAD, int NQ, bool CHECKED, int NS = 1, int NSL = NS, int CW = 8>
 __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsigned gc, unsigned* status_counter,
-                                               const int* table2 = nullptr, int* out2 = nullptr) {
+                                               long long tstride = 0, long long ostride = 0) {
     using Cfg = WsCfg<VC, NB, PAD, NSL, CW>;
     constexpr int WIN = Cfg::WIN, Q = Cfg::Q, S = Cfg::S, NC = 32 * CW;
-    static_assert(NS <= NSL, "the buffer layout holds NSL windows per view");
+    static_assert(NS <= NSL && NSL <= 4, "the buffer layout holds NSL <= 4 windows per view");
     static_assert(NQ == 0 || Cfg::EXCHANGE_FITS, "the accumulator exchange needs 4096 words per slice in one buffer");
     static_assert(NQ > 0 || CW == 8, "the compact layout is laid out for 8 consumer warps");
     int* win = smi;                                                     // [NB][VC][NSL][WIN]
@@ -940,7 +946,7 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 break;
             }
             if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD, NS, NSL>(J, win, meta, bars, produced,
-                                                                          gc + (unsigned)produced, lane, table2)) {
+                                                                          gc + (unsigned)produced, lane, tstride)) {
                 failed = true;
                 if (lane == 0) *abortw = 1;
                 break;
@@ -1052,8 +1058,8 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                     y = Y0 + ((regime & 1) ? u : f);
                 }
                 if (x < ixdimp && y < ixdimp) {
-                    J.out[(size_t)y * ixdimp + x] = acc[0][s];
-                    if (NS > 1) out2[(size_t)y * ixdimp + x] = acc[NS - 1][s];
+#pragma unroll
+                    for (int sl = 0; sl < NS; sl++) J.out[sl * ostride + (size_t)y * ixdimp + x] = acc[sl][s];
                 }
             }
         }
@@ -1073,7 +1079,7 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
     return true;
 }
 
-// grid (tiles, slices / NS): CTA row y covers slices slice0 + NS y (.. + NS - 1); NS = 2 needs
+// grid (tiles, slices / NS): CTA row y covers slices slice0 + NS y (.. + NS - 1); NS > 1 needs
 // slices that share the geometry (geom_slice_stride 0)
 template <int VC, int NB, int PAD, int NQ, int MINB, bool CHECKED, int NS = 1, int CW = 8>
 __global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws(BackprojLaunch p, int slice0) {
@@ -1092,8 +1098,8 @@ __global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws(BackprojLaunch
     J.X0 = (blockIdx.x % tiles_x) * 64;
     J.Y0 = (blockIdx.x / tiles_x) * 64;
     J.pair = NS > 1;
-    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED, NS, NS, CW>(J, smi, 0u, p.status_counter,
-                                                         J.table + p.slice_table_stride, J.out + p.out_slice_stride);
+    bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED, NS, NS, CW>(J, smi, 0u, p.status_counter, p.slice_table_stride,
+                                                         p.out_slice_stride);
 }
 
 // NSL = 2: jobs may cover slice pairs (TileJob::pair), in a layout with two windows per view
@@ -1114,7 +1120,7 @@ __global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws_persistent(con
         bool ok;
         if (NSL > 1 && J.pair)
             ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, (NSL > 1 ? 2 : 1), NSL, CW>(
-                J, smi, gc, nullptr, J.table + (size_t)J.nviews * J.table_stride, J.out + (size_t)J.ixdimp * J.ixdimp);
+                J, smi, gc, nullptr, (long long)J.nviews * J.table_stride, (long long)J.ixdimp * J.ixdimp);
         else
             ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, 1, NSL, CW>(J, smi, gc, nullptr);
         if (!ok) return;   // CTA-uniform
@@ -1717,7 +1723,8 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //         2 buffers x 4 views, 4 CTAs/SM;  18: variant 16's layout over slice pairs (two
 //         slices sharing the geometry per CTA: one index per pixel and view, two gathers),
 //         2 buffers x 4 views x 2 slices, 2 CTAs/SM;  19: variant 18 with 16 consumer warps
-//         (8 pixels x 2 slices per thread)
+//         (8 pixels x 2 slices per thread);  20: four slices per CTA sharing the index, 16
+//         consumer warps (8 pixels x 4 slices per thread), 2 buffers x 4 views x 4 slices, 1 CTA/SM
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -1798,6 +1805,19 @@ static cudaError_t go_ws_pairs(const BackprojLaunch& p, cudaStream_t s, bool che
     return e;
 }
 
+// groups of four slices per CTA (one index per pixel and view, four gathers), then pairs and a
+// single slice for the rest; per-slice geometry runs one slice per CTA
+template <int VC, int NB, int PAD, int NQ, int MINB, int CW>
+static cudaError_t go_ws_quads(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    if (p.geom_slice_stride != 0 || p.nslices < 4) return go_ws_pairs<4, 2, PAD, 8, 2>(p, s, checked);
+    const int q4 = p.nslices / 4;
+    cudaError_t e = go_ws_rows<VC, NB, PAD, NQ, MINB, 4, CW>(p, s, checked, 0, q4);
+    const int rest = p.nslices - 4 * q4;
+    if (e == cudaSuccess && rest >= 2) e = go_ws_rows<4, 2, PAD, 8, 2, 2>(p, s, checked, 4 * q4, 1);
+    if (e == cudaSuccess && (rest & 1)) e = go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, p.nslices - 1, 1);
+    return e;
+}
+
 template <int WX, int WY, int RX, int RY, int VC, int MINB>
 static cudaError_t go_pair(const BackprojLaunch& p, cudaStream_t s, bool checked) {
     using Cfg = PairCfg<WX, WY, RX, RY, VC>;
@@ -1829,6 +1849,7 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 17: return go_ws<4, 2, PAD, 0, 4>(p, s, checked);
     case 18: return go_ws_pairs<4, 2, PAD, 8, 2>(p, s, checked);
     case 19: return go_ws_pairs<4, 2, PAD, 8, 2, 16>(p, s, checked);
+    case 20: return go_ws_quads<4, 2, PAD, 8, 1, 16>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
 }
@@ -1934,6 +1955,7 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 16: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
     case 18: return go_ws_persistent<4, 2, PAD, 8, 2, 2>(jobs, njobs, counter, s);
     case 19: return go_ws_persistent<4, 2, PAD, 8, 2, 2, 16>(jobs, njobs, counter, s);
+    case 20: return go_ws_persistent<4, 2, PAD, 8, 2, 2>(jobs, njobs, counter, s);
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
@@ -1994,7 +2016,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 19 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 20 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;

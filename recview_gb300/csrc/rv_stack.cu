@@ -598,7 +598,7 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
             const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
             // the slice-pair kernel takes two consecutive slices of a part per job (they share
             // the geometry and their tables follow each other in the pool)
-            const int step = (q->variant == 18 || q->variant == 19) ? 2 : 1;
+            const int step = (q->variant >= 18 && q->variant <= 20) ? 2 : 1;
             for (int sl = pt.s0; sl < pt.s1; sl += step)
                 for (int t = 0; t < ntx * nty; t++) {
                     TileJob J{};
