@@ -37,10 +37,10 @@ sys.path.insert(0, str(ROOT))
 W_DET, N_VIEWS, N_SLICES = 2048, 1800, 64
 PUBLISHED_TAU_NS = 0.029  # RTX A4000, 2048^2 x 1800 views (reference README, Build-220422)
 WORKLOAD = "fbp-2048det-1800views-64slices-raw-uint16"
-# DRAM bytes (read + write) per pixel-view update of k_bp_ref, from one ncu capture of the default
-# variant on 2 slices of this geometry (profiles/k_bp_ref_2048x1800x2.md); the traffic grows in
-# proportion to the slices processed, so a full launch moves this times its updates.
-BP_DRAM_BYTES_PER_UPDATE = 1.1223e-1
+# DRAM bytes (read + write) per pixel-view update of the REF back-projection, from one ncu capture
+# of the default variant on 2 slices of this geometry; the traffic grows in proportion to the
+# slices processed, so a full launch moves this times its updates.
+BP_DRAM_BYTES_PER_UPDATE = 2.2244e-1
 
 
 def parse():
@@ -364,7 +364,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "roofline": {"bound": "smem", "achieved": smem_achieved, "peak": smem_gbs, "unit": "GB/s",
                          "frac": smem_achieved / smem_gbs if smem_gbs else None,
                          "traffic": BP_DRAM_BYTES_PER_UPDATE * updates_step if mode == abi.MODE_REF else None,
-                         "kernel": "k_bp_ref", "bytes_per_update": 4,
+                         "kernel": "k_bp_ref_ws" if bp_variant >= 16 else "k_bp_ref", "bytes_per_update": 4,
                          "peak_source": "measured in this run (RvProbeThroughput: conflict-free 32-bit shared loads)",
                          "updates_per_s_bp": upd_bp,
                          "fp32": {"achieved_tflops": 4.0 * upd_bp / 1e12, "peak_tflops": fp32_tflops,
