@@ -389,6 +389,13 @@ int RvGetBackprojectionVariant(int* variant, int* format);
  * on the current device. */
 int RvProbeThroughput(double* out, int n);
 
+/* Failure-detection self-check (no reference counterpart): one CTA waits, with the kernels'
+ * bounded mbarrier wait (2^log2_tries tries of at most ~1 us each, log2_tries 8..16), on a
+ * barrier that nothing completes.  Returns RV_ERR_KERNEL_STATUS when the wait ran out and was
+ * reported, as it must (the status is cleared; the context stays usable); *elapsed_ms gets the
+ * kernel's duration. */
+int RvTestBoundedWait(int log2_tries, double* elapsed_ms);
+
 /* ---- Offset-CT (360-degree scan with the rotation axis near one edge of the frame) ----------
  * Replaces the offset-CT tail of CGazoDoc::GenerateSinogram (source/gazoDoc.cpp:3535-3665):
  * every SAMPLE view i below nof = GetSinogramYdim(TRUE) (the first frame beyond 180 degrees,

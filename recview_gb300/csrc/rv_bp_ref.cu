@@ -67,18 +67,22 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned byt
 __device__ __forceinline__ void mbar_arrive(unsigned bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
+// One try: the thread may be suspended until the phase completes, for at most about the
+// explicit suspend-time hint (1 us), so 2^20 tries bound a wait to about a second.
+constexpr unsigned kTryWaitHintNs = 1000;
 __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "n"(kTryWaitHintNs)
         : "memory");
     return ok != 0;
 }
-// bounded wait: every spin has an iteration limit (each try_wait itself blocks for a while)
+// bounded wait: every spin has an iteration limit (2^LOG2 tries)
+template <int LOG2 = 20>
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
-    for (int i = 0; i < (1 << 20); i++)
+    for (int i = 0; i < (1 << LOG2); i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -2004,6 +2008,55 @@ unsigned int take_kernel_status(cudaStream_t s) {
 }
 
 }  // namespace rv
+
+namespace rv {
+// Failure-detection check: one CTA waits on an mbarrier that nothing completes, with the same
+// bounded wait as the kernels (2^LOG2 tries of at most ~1 us), then reports the timeout through
+// g_kernel_status and returns; the context stays usable.
+template <int LOG2>
+__global__ void k_wait_runs_out(unsigned* tries_out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);   // one arrival expected, none comes
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded<LOG2>(smem_u32(&bar), 0u));
+    if (!ok && threadIdx.x == 0) {
+        atomicOr(&g_kernel_status, 1u);
+        *tries_out = 1u << LOG2;
+    }
+}
+}  // namespace rv
+
+// Runs the bounded-wait check (log2_tries 8..16) and returns RV_ERR_KERNEL_STATUS when the wait
+// ran out as it must, after clearing the status; *elapsed_ms gets the kernel's duration.
+extern "C" int RvTestBoundedWait(int log2_tries, double* elapsed_ms) {
+    if (log2_tries < 8 || log2_tries > 16) return RV_ERR_BAD_ARGUMENT;
+    unsigned* d_tries = nullptr;
+    if (cudaMalloc(&d_tries, sizeof(unsigned)) != cudaSuccess) return RV_ERR_DEVICE_OOM;
+    cudaMemset(d_tries, 0, sizeof(unsigned));
+    rv::take_kernel_status(0);   // start from a clear status
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, 0);
+    switch (log2_tries) {
+    case 8: rv::k_wait_runs_out<8><<<1, 32>>>(d_tries); break;
+    case 12: rv::k_wait_runs_out<12><<<1, 32>>>(d_tries); break;
+    default: rv::k_wait_runs_out<16><<<1, 32>>>(d_tries); break;
+    }
+    cudaEventRecord(e1, 0);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (elapsed_ms) *elapsed_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d_tries);
+    if (e != cudaSuccess) return RV_ERR_LAUNCH;
+    return rv::take_kernel_status(0) ? RV_ERR_KERNEL_STATUS : 0;
+}
 
 extern "C" int RvSetCheckedBackprojection(int enable) {
     if (enable && !rv::g_counter) {
