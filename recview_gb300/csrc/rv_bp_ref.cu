@@ -1150,15 +1150,16 @@ struct LinElem<RV_MODE_LIN_F16> { static constexpr int ES = 4; };
 template <>
 struct LinElem<RV_MODE_LIN_BF16> { static constexpr int ES = 4; };
 
-template <int MODE>
+// the pair at byte address addr + OFF (OFF in the instruction)
+template <int MODE, int OFF = 0>
 __device__ __forceinline__ float2 lin_pair(unsigned addr) {
     if (MODE == RV_MODE_LIN) {
         float2 v;
-        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(addr), "n"(OFF));
         return v;
     } else {
         unsigned w;
-        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(addr));
+        asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(w) : "r"(addr), "n"(OFF));
         if (MODE == RV_MODE_LIN_F16) {
             __half2 h = *reinterpret_cast<__half2*>(&w);
             return __half22float2(h);
@@ -1167,19 +1168,22 @@ __device__ __forceinline__ float2 lin_pair(unsigned addr) {
     }
 }
 
-template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE>
+// NS windows per view (slices that share the geometry, one after the other), NS scales per view
+template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE, int NS = 1>
 struct LinCfg {
-    static constexpr int VC_ = VC, NB_ = NB, RX_ = RX, RY_ = RY;
+    static constexpr int VC_ = VC, NB_ = NB, RX_ = RX, RY_ = RY, NS_ = NS;
     static constexpr int NT = 32 * WX * WY, NW = NT / 32;
     static constexpr int GX = 8 * WX, GY = 4 * WY, TX = GX * RX, TY = GY * RY;
     static constexpr int ES = LinElem<MODE>::ES;
     // detector-pixel span of a tile + margins (2 below, 3 above) + 4-pair alignment, in pairs
     static constexpr int WINP = ((isqrt_ceil((TX - 1) * (TX - 1) + (TY - 1) * (TY - 1)) + 2 + 3 + 4 + 4) + 15) / 16 * 16;
     static constexpr int WIN_BYTES = WINP * ES;
-    static constexpr int META_OFF = NB * VC * WIN_BYTES;                  // bytes
+    static constexpr int META_OFF = NB * VC * NS * WIN_BYTES;             // bytes
     static constexpr int BAR_OFF = META_OFF + NB * VC * (int)sizeof(ViewMeta);
     static constexpr size_t SMEM = (size_t)BAR_OFF + (size_t)2 * NB * 8;
-    static constexpr size_t SMEM_WS = SMEM + 16;   // + the abort word of the producer-warp form
+    static constexpr int SCL_OFF = BAR_OFF + 2 * NB * 8;                  // float scales [NB][VC][NS]
+    static constexpr int ABORT_OFF = SCL_OFF + NB * VC * NS * 4;
+    static constexpr size_t SMEM_WS = (size_t)ABORT_OFF + 16;   // the producer-warp form
 };
 
 // Per-CTA state of a LIN tile: the slice's pair rows, scales and FP64 geometry, and the tile.
@@ -1189,15 +1193,17 @@ struct LinTile {
     const LinGeom* geom;
     int X0, Y0, nviews, ixdimp;
     long long row_stride;
+    long long slice_row_bytes;    // bytes between the rows of consecutive slices
 };
-__device__ __forceinline__ LinTile lin_tile(const BackprojLaunch& p, int TX, int TY, int ES) {
+__device__ __forceinline__ LinTile lin_tile(const BackprojLaunch& p, int TX, int TY, int ES, int slice) {
     LinTile t;
     const int tiles_x = (p.ixdimp + TX - 1) / TX;
     t.X0 = (blockIdx.x % tiles_x) * TX;
     t.Y0 = (blockIdx.x / tiles_x) * TY;
-    t.rows = static_cast<const unsigned char*>(p.rows16) + (size_t)blockIdx.y * p.slice_row_stride * ES;
-    t.scales = p.row_scale ? p.row_scale + (size_t)blockIdx.y * p.nviews : nullptr;
-    t.geom = p.geom64 + (size_t)blockIdx.y * p.geom_slice_stride;
+    t.rows = static_cast<const unsigned char*>(p.rows16) + (size_t)slice * p.slice_row_stride * ES;
+    t.scales = p.row_scale ? p.row_scale + (size_t)slice * p.nviews : nullptr;
+    t.geom = p.geom64 + (size_t)slice * p.geom_slice_stride;
+    t.slice_row_bytes = p.slice_row_stride * ES;
     t.nviews = p.nviews;
     t.ixdimp = p.ixdimp;
     t.row_stride = p.row_stride;
@@ -1209,8 +1215,9 @@ __device__ __forceinline__ LinTile lin_tile(const BackprojLaunch& p, int TX, int
 // bounded wait ran out.
 template <typename Cfg>
 __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, ViewMeta* meta, uint64_t* bars, int c,
-                                         int lane) {
+                                         int lane, float* scl = nullptr) {
     constexpr int NB = Cfg::NB_, VC = Cfg::VC_, TX = Cfg::TX, TY = Cfg::TY, WINP = Cfg::WINP, ES = Cfg::ES;
+    constexpr int NS = Cfg::NS_;
     const unsigned g = (unsigned)c;
     const int b = (int)(g % NB);
     if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
@@ -1235,22 +1242,30 @@ __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, V
         m.go = (float)(base - (double)w0);   // window-relative u at the tile origin
         m.off = __float_as_uint(T.scales ? T.scales[v0 + lane] : 1.0f);
         meta[b * VC + lane] = m;
+        if (NS > 1 && scl) {   // every slice's scale of this view (slice sl's scales follow at sl * nviews)
+#pragma unroll
+            for (int sl = 0; sl < NS; sl++)
+                scl[(b * VC + lane) * NS + sl] = T.scales ? T.scales[(size_t)sl * T.nviews + v0 + lane] : 1.0f;
+        }
     }
     __syncwarp();
     for (int vv = 0; vv < nv; vv++) {
         const ViewMeta m = meta[b * VC + vv];
         if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
-        int4* w4 = reinterpret_cast<int4*>(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES);
         const int bytes_a = (m.b > m.a ? m.a - m.w0 : m.nwin) * ES, bytes_b = (m.b > m.a ? m.b - m.w0 : m.nwin) * ES;
-        for (int e = lane; e < bytes_a / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
-        for (int e = bytes_b / 16 + lane; e < Cfg::WIN_BYTES / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) {
+            int4* w4 = reinterpret_cast<int4*>(smb + (size_t)((b * VC + vv) * NS + sl) * Cfg::WIN_BYTES);
+            for (int e = lane; e < bytes_a / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+            for (int e = bytes_b / 16 + lane; e < Cfg::WIN_BYTES / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        }
     }
     __syncwarp();
     if (lane == 0) {
         unsigned bytes = 0;
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[b * VC + vv];
-            if (m.b > m.a) bytes += (unsigned)((m.b - m.a) * ES);
+            if (m.b > m.a) bytes += (unsigned)(NS * (m.b - m.a) * ES);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const unsigned bar = smem_u32(&bars[b]);
@@ -1258,9 +1273,12 @@ __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, V
         for (int vv = 0; vv < nv; vv++) {
             const ViewMeta m = meta[b * VC + vv];
             if (m.b <= m.a) continue;
-            const unsigned char* src = T.rows + ((size_t)(v0 + vv) * T.row_stride + m.a) * ES;
-            const unsigned dst = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
-            tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
+#pragma unroll
+            for (int sl = 0; sl < NS; sl++) {
+                const unsigned char* src = T.rows + sl * T.slice_row_bytes + ((size_t)(v0 + vv) * T.row_stride + m.a) * ES;
+                const unsigned dst = smem_u32(smb + (size_t)((b * VC + vv) * NS + sl) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
+                tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
+            }
         }
     }
     __syncwarp();
@@ -1269,21 +1287,36 @@ __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, V
 
 // acc += the interpolated, scaled row value of every pixel of the thread, for the nv views of
 // buffer b
+// one slice's update of a pixel: acc += (scaled) r + f * slope, from the pair at addr + sl windows
+template <typename Cfg, int MODE, int SL>
+__device__ __forceinline__ void lin_slice(float& acc, unsigned addr, float f, float sc) {
+    const float2 q = lin_pair<MODE, SL * Cfg::WIN_BYTES>(addr);
+    const float v = fmaf(f, q.y, q.x);
+    if (MODE == RV_MODE_LIN) acc += v;
+    else acc = fmaf(v, sc, acc);
+}
+
+// acc[sl] += the interpolated, scaled row value of every pixel of the thread in slice sl, for the
+// nv views of buffer b.  The NS slices share the geometry, so each pixel's detector coordinate,
+// window index and fraction are computed once (scl: the per-slice scales when NS > 1).
 template <typename Cfg, int MODE>
-__device__ __forceinline__ void lin_consume(float (&acc)[Cfg::RY_][Cfg::RX_], const float (&colf)[Cfg::RX_],
+__device__ __forceinline__ void lin_consume(float (&acc)[Cfg::NS_][Cfg::RY_][Cfg::RX_], const float (&colf)[Cfg::RX_],
                                             const float (&rowf)[Cfg::RY_], const unsigned char* smb,
-                                            const ViewMeta* meta, int b, int nv) {
-    constexpr int RX = Cfg::RX_, RY = Cfg::RY_, VC = Cfg::VC_, ES = Cfg::ES;
+                                            const ViewMeta* meta, int b, int nv, const float* scl = nullptr) {
+    constexpr int RX = Cfg::RX_, RY = Cfg::RY_, VC = Cfg::VC_, ES = Cfg::ES, NS = Cfg::NS_;
     for (int vv = 0; vv < nv; vv++) {
         const float4 gm = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
-        const float sc = __uint_as_float(__float_as_uint(gm.w));
+        float sc[NS];
+        sc[0] = __uint_as_float(__float_as_uint(gm.w));
+#pragma unroll
+        for (int sl = 1; sl < NS; sl++) sc[sl] = scl[(b * VC + vv) * NS + sl];
         float xv[RX], yv[RY];
 #pragma unroll
         for (int c = 0; c < RX; c++) xv[c] = colf[c] * gm.x;
 #pragma unroll
         for (int r = 0; r < RY; r++) yv[r] = fmaf(rowf[r], gm.y, gm.z);
         // address of pair 0 minus the 2^23 bit pattern (unsigned wrap-around)
-        const unsigned base = smem_u32(smb + (size_t)(b * VC + vv) * Cfg::WIN_BYTES) - (unsigned)ES * kMagicBits;
+        const unsigned base = smem_u32(smb + (size_t)(b * VC + vv) * NS * Cfg::WIN_BYTES) - (unsigned)ES * kMagicBits;
 #pragma unroll
         for (int r = 0; r < RY; r++)
 #pragma unroll
@@ -1292,26 +1325,30 @@ __device__ __forceinline__ void lin_consume(float (&acc)[Cfg::RY_][Cfg::RX_], co
                 const float t = __fadd_rz(u, 8388608.0f);
                 const unsigned bits = __float_as_uint(t);
                 const float f = u - (t - 8388608.0f);
-                const float2 q = lin_pair<MODE>(base + (unsigned)ES * bits);
-                const float v = fmaf(f, q.y, q.x);
-                if (MODE == RV_MODE_LIN) acc[r][c] += v;
-                else acc[r][c] = fmaf(v, sc, acc[r][c]);
+                const unsigned a = base + (unsigned)ES * bits;
+                lin_slice<Cfg, MODE, 0>(acc[0][r][c], a, f, sc[0]);
+                if (NS > 1) lin_slice<Cfg, MODE, (NS > 1 ? 1 : 0)>(acc[1 % NS][r][c], a, f, sc[1 % NS]);
+                if (NS > 2) lin_slice<Cfg, MODE, (NS > 2 ? 2 : 0)>(acc[2 % NS][r][c], a, f, sc[2 % NS]);
+                if (NS > 3) lin_slice<Cfg, MODE, (NS > 3 ? 3 : 0)>(acc[3 % NS][r][c], a, f, sc[3 % NS]);
             }
     }
 }
 
 template <typename Cfg>
-__device__ __forceinline__ void lin_store(const BackprojLaunch& p, const LinTile& T, const float (&acc)[Cfg::RY_][Cfg::RX_],
-                                          int tx, int ty) {
-    float* out = static_cast<float*>(p.out) + (size_t)blockIdx.y * p.out_slice_stride;
+__device__ __forceinline__ void lin_store(const BackprojLaunch& p, const LinTile& T, int slice,
+                                          const float (&acc)[Cfg::NS_][Cfg::RY_][Cfg::RX_], int tx, int ty) {
 #pragma unroll
-    for (int r = 0; r < Cfg::RY_; r++) {
-        const int y = T.Y0 + ty + Cfg::GY * r;
-        if (y >= T.ixdimp) continue;
+    for (int sl = 0; sl < Cfg::NS_; sl++) {
+        float* out = static_cast<float*>(p.out) + (size_t)(slice + sl) * p.out_slice_stride;
 #pragma unroll
-        for (int c = 0; c < Cfg::RX_; c++) {
-            const int x = T.X0 + tx + Cfg::GX * c;
-            if (x < T.ixdimp) out[(size_t)y * T.ixdimp + x] = acc[r][c];
+        for (int r = 0; r < Cfg::RY_; r++) {
+            const int y = T.Y0 + ty + Cfg::GY * r;
+            if (y >= T.ixdimp) continue;
+#pragma unroll
+            for (int c = 0; c < Cfg::RX_; c++) {
+                const int x = T.X0 + tx + Cfg::GX * c;
+                if (x < T.ixdimp) out[(size_t)y * T.ixdimp + x] = acc[sl][r][c];
+            }
         }
     }
 }
@@ -1332,7 +1369,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const LinTile T = lin_tile(p, Cfg::TX, Cfg::TY, Cfg::ES);
+    const LinTile T = lin_tile(p, Cfg::TX, Cfg::TY, Cfg::ES, blockIdx.y);
     const int tx = (warp % WX) * 8 + (lane & 7), ty = (warp / WX) * 4 + (lane >> 3);
     const int nchunks = (T.nviews + VC - 1) / VC;
     // coordinates relative to the tile origin (small, so FP32 keeps ~1e-6 px); the tile-origin term
@@ -1342,11 +1379,11 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
     for (int c = 0; c < RX; c++) colf[c] = (float)(tx + Cfg::GX * c);
 #pragma unroll
     for (int r = 0; r < RY; r++) rowf[r] = (float)(ty + Cfg::GY * r);
-    float acc[RY][RX];
+    float acc[1][RY][RX];
 #pragma unroll
     for (int r = 0; r < RY; r++)
 #pragma unroll
-        for (int c = 0; c < RX; c++) acc[r][c] = 0.0f;
+        for (int c = 0; c < RX; c++) acc[0][r][c] = 0.0f;
     bool ok = true;
     int produced = 0;
     if (warp == 0)
@@ -1371,22 +1408,24 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_lin_pipe(BackprojLaun
                 mbar_wait_bounded(smem_u32(&bars[(unsigned)c % NB]), ((unsigned)c / NB) & 1u);
         return;
     }
-    lin_store<Cfg>(p, T, acc, tx, ty);
+    lin_store<Cfg>(p, T, blockIdx.y, acc, tx, ty);
 }
 
 // A ninth warp only produces (as the REF kernel's variant 16); the eight consumer warps do the
-// same work and never wait for a fill a busy consumer has not issued.  A consumer whose bounded
-// wait ran out raises the abort word and leaves its loop (the consumers share no barrier here);
-// all 288 threads meet at one block barrier at the end.
-template <int VC, int NB, int MODE, int MINB>
-__global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p) {
-    using Cfg = LinCfg<2, 4, 4, 4, VC, NB, MODE>;
+// same work and never wait for a fill a busy consumer has not issued.  NS > 1: the CTA takes NS
+// slices that share the geometry (slice0 + NS * blockIdx.y ..) and shares each pixel's index
+// arithmetic between them.  A consumer whose bounded wait ran out raises the abort word and
+// leaves its loop (the consumers share no barrier here); all 288 threads meet at one block
+// barrier at the end.
+template <int VC, int NB, int MODE, int MINB, int NS = 1>
+__global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p, int slice0) {
+    using Cfg = LinCfg<2, 4, 4, 4, VC, NB, MODE, NS>;
     static_assert(Cfg::NT == 256, "8 consumer warps");
-    constexpr int ABORT_OFF = Cfg::BAR_OFF + 2 * NB * 8;   // bytes
     extern __shared__ __align__(128) unsigned char smb[];
     ViewMeta* meta = reinterpret_cast<ViewMeta*>(smb + Cfg::META_OFF);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smb + Cfg::BAR_OFF);
-    volatile int* abortw = reinterpret_cast<volatile int*>(smb + ABORT_OFF);
+    float* scl = reinterpret_cast<float*>(smb + Cfg::SCL_OFF);
+    volatile int* abortw = reinterpret_cast<volatile int*>(smb + Cfg::ABORT_OFF);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
         for (int b = 0; b < NB; b++) {
@@ -1397,14 +1436,15 @@ __global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const LinTile T = lin_tile(p, Cfg::TX, Cfg::TY, Cfg::ES);
+    const int slice = slice0 + NS * (int)blockIdx.y;
+    const LinTile T = lin_tile(p, Cfg::TX, Cfg::TY, Cfg::ES, slice);
     const int nchunks = (T.nviews + VC - 1) / VC;
     bool failed = false;
     int produced = 0;
     if (warp == 8) {
         for (; produced < nchunks; produced++) {
             if (__any_sync(0xffffffffu, *abortw != 0)) { failed = true; break; }
-            if (!lin_fill<Cfg>(T, smb, meta, bars, produced, lane)) {
+            if (!lin_fill<Cfg>(T, smb, meta, bars, produced, lane, scl)) {
                 failed = true;
                 if (lane == 0) *abortw = 1;
                 break;
@@ -1417,11 +1457,13 @@ __global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p) {
         for (int c = 0; c < 4; c++) colf[c] = (float)(tx + Cfg::GX * c);
 #pragma unroll
         for (int r = 0; r < 4; r++) rowf[r] = (float)(ty + Cfg::GY * r);
-        float acc[4][4];
+        float acc[NS][4][4];
 #pragma unroll
-        for (int r = 0; r < 4; r++)
+        for (int sl = 0; sl < NS; sl++)
 #pragma unroll
-            for (int c = 0; c < 4; c++) acc[r][c] = 0.0f;
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[sl][r][c] = 0.0f;
         for (int k = 0; k < nchunks; k++) {
             const unsigned g = (unsigned)k;
             const int b = (int)(g % NB);
@@ -1431,11 +1473,11 @@ __global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p) {
                 if (lane == 0) *abortw = 1;
                 break;
             }
-            lin_consume<Cfg, MODE>(acc, colf, rowf, smb, meta, b, min(VC, T.nviews - k * VC));
+            lin_consume<Cfg, MODE>(acc, colf, rowf, smb, meta, b, min(VC, T.nviews - k * VC), scl);
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
         }
-        if (!failed) lin_store<Cfg>(p, T, acc, tx, ty);
+        if (!failed) lin_store<Cfg>(p, T, slice, acc, tx, ty);
     }
     if (__syncthreads_or(failed)) {
         if (tid == 0) atomicOr(&g_kernel_status, 1u);
@@ -1457,26 +1499,43 @@ static cudaError_t go_lin(const BackprojLaunch& p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int MODE, int VC, int NB, int MINB>
-static cudaError_t go_lin_ws(const BackprojLaunch& p, cudaStream_t s) {
-    using Cfg = LinCfg<2, 4, 4, 4, VC, NB, MODE>;
-    auto kern = k_bp_lin_ws<VC, NB, MODE, MINB>;
+template <int MODE, int VC, int NB, int MINB, int NS = 1>
+static cudaError_t go_lin_ws_rows(const BackprojLaunch& p, cudaStream_t s, int slice0, int rows) {
+    using Cfg = LinCfg<2, 4, 4, 4, VC, NB, MODE, NS>;
+    auto kern = k_bp_lin_ws<VC, NB, MODE, MINB, NS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM_WS);
     if (e != cudaSuccess) return e;
     const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
-    kern<<<dim3(tiles, p.nslices), 288, Cfg::SMEM_WS, s>>>(p);
+    kern<<<dim3(tiles, rows), 288, Cfg::SMEM_WS, s>>>(p, slice0);
     return cudaGetLastError();
 }
 
+template <int MODE, int VC, int NB, int MINB>
+static cudaError_t go_lin_ws(const BackprojLaunch& p, cudaStream_t s) {
+    return go_lin_ws_rows<MODE, VC, NB, MINB>(p, s, 0, p.nslices);
+}
+
+// slice pairs when the slices share the geometry (an odd last slice, or per-slice geometry, runs
+// one slice per CTA)
+template <int MODE>
+static cudaError_t go_lin_ws_pairs(const BackprojLaunch& p, cudaStream_t s) {
+    if (p.geom_slice_stride != 0 || p.nslices < 2) return go_lin_ws<MODE, 8, 2, 4>(p, s);
+    cudaError_t e = go_lin_ws_rows<MODE, 8, 2, 2, 2>(p, s, 0, p.nslices / 2);
+    if (e == cudaSuccess && (p.nslices & 1)) e = go_lin_ws_rows<MODE, 8, 2, 4>(p, s, p.nslices - 1, 1);
+    return e;
+}
+
 // LIN kernel form (RV_LIN_VARIANT): 0 = warp 0 also produces, 2 buffers x 8 views; 1 = a
-// dedicated producer warp, 2 x 8; 2 = producer warp, 3 x 8, 3 CTAs/SM; 3 = producer warp, 2 x 16
+// dedicated producer warp, 2 x 8; 2 = producer warp, 3 x 8, 3 CTAs/SM; 3 = producer warp, 2 x 16;
+// 4 (default) = producer warp and slice pairs
 template <int MODE>
 static cudaError_t dispatch_lin(const BackprojLaunch& p, cudaStream_t s) {
-    static const int v = env_int("RV_LIN_VARIANT", 1);
+    static const int v = env_int("RV_LIN_VARIANT", 4);
     switch (v) {
     case 0: return go_lin<MODE>(p, s);
     case 2: return go_lin_ws<MODE, 8, 3, 3>(p, s);
     case 3: return go_lin_ws<MODE, 16, 2, 3>(p, s);
+    case 4: return go_lin_ws_pairs<MODE>(p, s);
     default: return go_lin_ws<MODE, 8, 2, 4>(p, s);
     }
 }

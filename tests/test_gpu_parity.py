@@ -269,11 +269,13 @@ def test_stack_host_pipeline_pieces(gpu, oracle, monkeypatch, pieces, budget_mb)
     st.close()
 
 
+@pytest.mark.parametrize("S", [2, 3], ids=lambda s: f"S{s}")
 @pytest.mark.parametrize("mode,tol", [(abi.MODE_LIN, 1e-5), (abi.MODE_LIN_F16, 1e-3), (abi.MODE_LIN_BF16, 8e-3)])
-def test_stack_lin_modes_vs_fp64(gpu, oracle, mode, tol):
+def test_stack_lin_modes_vs_fp64(gpu, oracle, mode, tol, S):
     """LIN modes: FP32 interpolation/accumulation with FP32/FP16/BF16 filtered rows; relative L2
-    error against the FP64 end-to-end oracle, inside the reconstruction circle."""
-    W, V, S, cen = 256, 300, 2, 127.6
+    error against the FP64 end-to-end oracle, inside the reconstruction circle.  Two slices run
+    as one slice pair; three as a pair plus a single slice (each with its own row scales)."""
+    W, V, cen = 256, 300, 127.6
     raw, bInc, fdeg, fexp, _ = phantom.raw_stack(80, W, V, S, cen, n_ellipsoids=12, nflat_before=1, nflat_after=1)
     d = dims(W)
     F = oracle.set_filter(abi.FILT_SHEPP, d.ndim)
