@@ -351,13 +351,15 @@ static int ensure_host_buffers(RvStack* st, size_t in_b, size_t out_b) {
 }
 
 static int piece_slices(const RvStack* st) {
-    int pieces = 8;
+    int pieces = 16;
     if (const char* e = getenv("RV_STACK_PIECES")) pieces = atoi(e);
     const int S = st->desc.nslices;
     if (pieces < 1) pieces = 1;
     int p = (S + pieces - 1) / pieces;
     if (p > st->batch) p = st->batch;
     if (p < 1) p = 1;
+    // an even piece runs entirely as slice pairs in the back-projection
+    if ((p & 1) && p > 1 && p + 1 <= st->batch && st->batch % (p + 1) == 0) p++;
     while (st->batch % p) p--;   // a piece never straddles two table batches (slots s mod batch)
     return p;
 }
