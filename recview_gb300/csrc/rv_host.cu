@@ -123,7 +123,7 @@ struct DevBuf {
 
 struct RiContext {
     int device = -1;
-    DevBuf out, table, rows, jobs, geom, filt, tw, raw, sino_out, shift;
+    DevBuf out, table, rows, jobs, geom, filt, tw, raw, sino_out, shift, rowptr;
     void* h_stage = nullptr;   // pinned staging for row gathers
     size_t h_stage_bytes = 0;
     int tw_np = -1;
@@ -143,7 +143,7 @@ struct RiContext {
         return true;
     }
     void release() {
-        DevBuf* all[] = {&out, &table, &rows, &jobs, &geom, &filt, &tw, &raw, &sino_out, &shift};
+        DevBuf* all[] = {&out, &table, &rows, &jobs, &geom, &filt, &tw, &raw, &sino_out, &shift, &rowptr};
         for (DevBuf* b : all) b->release();
         if (h_stage) cudaFreeHost(h_stage);
         h_stage = nullptr;
@@ -283,13 +283,23 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
             fail(ri, RV_ERR_DEVICE_OOM, "Out of CUDA device memory (filtered views)");
             return;
         }
-        if (!c->stage(nv * row_bytes + nv * sizeof(RowJob))) {
-            fail(ri, RV_ERR_PINNED_ALLOC, "pinned staging buffer");
+        // where the device reads pageable host memory directly (shared page tables), the filter
+        // takes each view's row from the caller's row pointer; otherwise the rows are gathered
+        // into pinned staging and copied
+        const bool direct = host_direct_access();
+        const size_t gather_bytes = direct ? (size_t)nv * sizeof(short*) : (size_t)nv * row_bytes;
+        if (!c->stage(gather_bytes + nv * sizeof(RowJob)) || (direct && !c->rowptr.ensure(gather_bytes))) {
+            fail(ri, direct ? RV_ERR_DEVICE_OOM : RV_ERR_PINNED_ALLOC, "row staging");
             return;
         }
         char* hs = static_cast<char*>(c->h_stage);
-        for (int v = 0; v < nv; v++) memcpy(hs + v * row_bytes, ri->iSinogr[sidxs[v]], row_bytes);
-        RowJob* hj = reinterpret_cast<RowJob*>(hs + nv * row_bytes);
+        if (direct) {
+            const short** hp = reinterpret_cast<const short**>(hs);
+            for (int v = 0; v < nv; v++) hp[v] = ri->iSinogr[sidxs[v]];
+        } else {
+            for (int v = 0; v < nv; v++) memcpy(hs + v * row_bytes, ri->iSinogr[sidxs[v]], row_bytes);
+        }
+        RowJob* hj = reinterpret_cast<RowJob*>(hs + gather_bytes);
         for (int v = 0; v < nv; v++) {
             RowJob j{};
             j.src_row = v;
@@ -297,8 +307,8 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
             hj[v] = j;
         }
         if (!upload_twiddles(c, d.ndimp, s)) { ri->iStatus = RECONST_INFO_ERROR; return; }
-        if (!cuda_ok(cudaMemcpyAsync(c->rows.p, hs, nv * row_bytes, cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D,
-                     "sinogram rows") ||
+        if (!cuda_ok(cudaMemcpyAsync(direct ? c->rowptr.p : c->rows.p, hs, gather_bytes, cudaMemcpyHostToDevice, s),
+                     RV_ERR_COPY_H2D, "sinogram rows") ||
             !cuda_ok(cudaMemcpyAsync(c->jobs.p, hj, nv * sizeof(RowJob), cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D,
                      "row jobs") ||
             !cuda_ok(cudaMemcpyAsync(c->filt.p, ri->fFilter, (size_t)d.ndim * sizeof(float), cudaMemcpyHostToDevice, s),
@@ -308,6 +318,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         }
         FilterLaunch fl{};
         fl.src = c->rows.p;
+        fl.row_ptr = direct ? static_cast<const short* const*>(c->rowptr.p) : nullptr;
         fl.raw = 0;
         fl.jobs = static_cast<const RowJob*>(c->jobs.p);
         fl.njobs = nv;
@@ -375,8 +386,12 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
             return;
         }
     }
-    // ---- copy the slice back (source/cudaReconstHost.cpp:811) --------------------------------
-    if (!cuda_ok(cudaMemcpyAsync(ri->iReconst, c->out.p, (size_t)ixdimp * ixdimp * sizeof(int), cudaMemcpyDeviceToHost, s),
+    // ---- copy the slice back (source/cudaReconstHost.cpp:811): by a kernel that writes the
+    // caller's buffer directly where the device can, else a device-to-host copy -------------------
+    const size_t out_bytes = (size_t)ixdimp * ixdimp * sizeof(int);
+    const bool direct_out = host_direct_access() && !(out_bytes & 15) && !(reinterpret_cast<uintptr_t>(ri->iReconst) & 15);
+    if (!cuda_ok(direct_out ? launch_copy16(ri->iReconst, c->out.p, out_bytes, s)
+                            : cudaMemcpyAsync(ri->iReconst, c->out.p, out_bytes, cudaMemcpyDeviceToHost, s),
                  RV_ERR_COPY_D2H, "slice copy") ||
         !cuda_ok(cudaStreamSynchronize(s), RV_ERR_LAUNCH, "slice")) {
         ri->iStatus = RECONST_INFO_ERROR;

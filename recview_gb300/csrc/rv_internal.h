@@ -68,8 +68,16 @@ struct FilterLaunch {
     long long table_stride;   // ints between table slots
     long long row_stride;     // pairs between LIN rows (lin_pair_stride)
     int table_fmt;            // REF table format, see ref_table_fmt()
+    const short* const* row_ptr;  // sinogram mode: if set, row j is row_ptr[job.src_row] (it may be
+                                  // host memory the device reads directly) instead of src + j * ixdim
 };
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
+// 1 when kernels on the current device may read and write pageable host memory directly (the
+// host's page tables are shared with the GPU, as on Grace-based systems); RV_NO_HOST_DIRECT=1
+// turns the direct paths off
+bool host_direct_access();
+// dst (host or device) <- src (device), n bytes, by a kernel; both 16-byte aligned, n % 16 == 0
+cudaError_t launch_copy16(void* dst, const void* src, size_t n, cudaStream_t s);
 
 // ---- back-projection ---------------------------------------------------------------------
 // LIN geometry of one view in FP64: detector coordinate u = x c + y s + off (zoomed pixels)

@@ -12,6 +12,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "rv_internal.h"
 
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
                       base + (size_t)job.flat1_row * W, base + (size_t)job.dark_row * W, W, 0, job.zero != 0, job.t0,
                       p.pixmin, 0, strip, reinterpret_cast<int*>(buf), &s_nre);
     } else {
-        const short* r = static_cast<const short*>(p.src) + (size_t)job.src_row * W;
+        const short* r = p.row_ptr ? p.row_ptr[job.src_row] : static_cast<const short*>(p.src) + (size_t)job.src_row * W;
         for (int x = tid; x < W; x += NT) strip[x] = job.zero ? (short)0 : r[x];
         __syncthreads();
     }
@@ -446,6 +447,37 @@ cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {
     default: return cudaErrorInvalidValue;
     }
     return e;
+}
+
+// plain 16-byte copy (grid-stride): writes host memory directly where the device can
+__global__ void k_copy16(int4* __restrict__ dst, const int4* __restrict__ src, size_t n16) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+cudaError_t launch_copy16(void* dst, const void* src, size_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if ((n & 15) || (reinterpret_cast<uintptr_t>(dst) & 15) || (reinterpret_cast<uintptr_t>(src) & 15))
+        return cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_copy16<<<2 * sms, 512, 0, s>>>(static_cast<int4*>(dst), static_cast<const int4*>(src), n / 16);
+    return cudaGetLastError();
+}
+
+bool host_direct_access() {
+    static int cached[64];   // per device: 0 unknown, 1 yes, 2 no
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (!cached[dev]) {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+        const char* off = getenv("RV_NO_HOST_DIRECT");
+        cached[dev] = (pageable && host_tables && !(off && atoi(off))) ? 1 : 2;
+    }
+    return cached[dev] == 1;
 }
 
 cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s) {

@@ -351,3 +351,30 @@ def test_centre_sweep(gpu, oracle, seed, W, V, cen):
         want = oracle.tv_score(oracle.reconstruct(ri))
         assert abs(scores[i] - want) <= 1e-9 * want
     assert abs(best.value - cen) <= 0.25, (best.value, cen)
+
+
+def test_dropin_staged_copies_equal_direct(gpu, oracle, tmp_path):
+    """Where the device reads pageable host memory directly, CudaReconstHost takes the sinogram
+    rows from the caller's row pointers and writes the slice with a kernel; RV_NO_HOST_DIRECT=1
+    forces the staged copies.  Both give the oracle's slice (the staged run in a subprocess,
+    since the choice is made once per process)."""
+    import subprocess
+    import sys
+    ri = fbp_case(41, 256, 240, 127.3, 2, oracle=oracle)
+    want = oracle.reconstruct(ri, threads=8)
+    assert np.array_equal(_gpu_slice(ri), want)
+    script = (
+        "import numpy as np, sys\n"
+        "sys.path.insert(0, '.')\n"
+        "import recview_gb300 as rv\n"
+        "from tests.rvtest import Oracle, fbp_case\n"
+        "o = Oracle()\n"
+        "ri = fbp_case(41, 256, 240, 127.3, 2, oracle=o)\n"
+        "ri.reset_output()\n"
+        f"np.save(r'{tmp_path / 'staged.npy'}', rv.reconstruct_slice(ri).copy())\n"
+    )
+    import os
+    env = dict(os.environ, RV_NO_HOST_DIRECT="1")
+    r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert np.array_equal(np.load(tmp_path / "staged.npy"), want)
