@@ -1063,7 +1063,11 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 }
                 if (x < ixdimp && y < ixdimp) {
 #pragma unroll
-                    for (int sl = 0; sl < NS; sl++) J.out[sl * ostride + (size_t)y * ixdimp + x] = acc[sl][s];
+                    for (int sl = 0; sl < NS; sl++) {
+                        int* o = J.out + sl * ostride + (size_t)y * ixdimp + x;
+                        if (J.accumulate) atomicAdd(o, acc[sl][s]);   // int sums: any order gives the same slice
+                        else *o = acc[sl][s];
+                    }
                 }
             }
         }
@@ -1102,6 +1106,15 @@ __global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws(BackprojLaunch
     J.X0 = (blockIdx.x % tiles_x) * 64;
     J.Y0 = (blockIdx.x / tiles_x) * 64;
     J.pair = NS > 1;
+    J.accumulate = 0;
+    if (gridDim.z > 1) {   // view group blockIdx.z of gridDim.z: partial sums added into the slice
+        const int v0 = (int)(((long long)p.nviews * blockIdx.z) / gridDim.z);
+        const int v1 = (int)(((long long)p.nviews * (blockIdx.z + 1)) / gridDim.z);
+        J.table += (size_t)v0 * p.table_stride;
+        J.geom += v0;
+        J.nviews = v1 - v0;
+        J.accumulate = 1;
+    }
     bp_ref_tile_ws<VC, NB, PAD, NQ, CHECKED, NS, NS, CW>(J, smi, 0u, p.status_counter, p.slice_table_stride,
                                                          p.out_slice_stride);
 }
@@ -1842,6 +1855,24 @@ static cudaError_t go_pipe(const BackprojLaunch& p, cudaStream_t s, bool checked
     return launch_k(k_bp_ref_pipe<WX, WY, RX, RY, VC, NB, PAD, MINB, false>, grid, Cfg::NT, Cfg::SMEM, p, s);
 }
 
+// Number of view groups for a launch of `ctas` tile CTAs on `slots` resident CTA slots: the
+// last wave of a small launch (one slice: 1024 tiles on 456 slots) would run mostly empty, so
+// the views are split into g groups whose partial sums are added into the slice, choosing g
+// (1..8, at least 16 views per group) for the least time ceil(ctas g / slots) / g.
+static int view_groups(long long ctas, int slots, int nviews) {
+    if (slots <= 0 || ctas <= 0 || ctas >= 8LL * slots) return 1;
+    int best = 1;
+    double best_t = (double)((ctas + slots - 1) / slots);
+    for (int g = 2; g <= 8 && nviews / g >= 16; g++) {
+        const double t = (double)((ctas * g + slots - 1) / slots) / g;
+        if (t < 0.97 * best_t) {
+            best_t = t;
+            best = g;
+        }
+    }
+    return best;
+}
+
 template <int VC, int NB, int PAD, int NQ, int MINB, int NS = 1, int CW = 8>
 static cudaError_t go_ws_rows(const BackprojLaunch& p, cudaStream_t s, bool checked, int slice0, int rows) {
     using Cfg = WsCfg<VC, NB, PAD, NS, CW>;
@@ -1849,7 +1880,17 @@ static cudaError_t go_ws_rows(const BackprojLaunch& p, cudaStream_t s, bool chec
     auto kern = checked ? k_bp_ref_ws<VC, NB, PAD, NQ, MINB, true, NS, CW> : k_bp_ref_ws<VC, NB, PAD, NQ, MINB, false, NS, CW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::SMEM);
     if (e != cudaSuccess) return e;
-    kern<<<dim3(tiles, rows), Cfg::NT, Cfg::SMEM, s>>>(p, slice0);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::NT, Cfg::SMEM) != cudaSuccess) per_sm = 0;
+    const int groups = view_groups((long long)tiles * rows, sms * per_sm, p.nviews);
+    if (groups > 1) {   // the groups add into zeroed slices
+        e = cudaMemsetAsync(static_cast<int*>(p.out) + (size_t)slice0 * p.out_slice_stride, 0,
+                            (size_t)rows * NS * p.out_slice_stride * sizeof(int), s);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<dim3(tiles, rows, groups), Cfg::NT, Cfg::SMEM, s>>>(p, slice0);
     return cudaGetLastError();
 }
 

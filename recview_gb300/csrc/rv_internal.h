@@ -116,6 +116,8 @@ struct TileJob {
     int nviews, ixdimp, X0, Y0;
     int pair;                 // 1: also the next slice (tables at table + nviews * table_stride,
                               // output at out + ixdimp^2), which shares the geometry
+    int accumulate;           // 1: add the tile's sums into out atomically (a group of views of
+                              // the slice; out zeroed before), 0: store them
 };
 // tile shape of the persistent kernel of an int-table variant (0..4), and the default variant
 void persistent_tile_xy(int variant, int* tx, int* ty);
