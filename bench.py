@@ -385,6 +385,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         if not args.no_forms and world == 1 and mode == abi.MODE_REF:
             line["forms"] = forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev)
             line["queue"] = queue_summary(dev, args.seed)
+            line["dropin"] = dropin_summary(raw, bInc, fdeg, fexp, center, F)
         if not args.no_centre and world == 1 and NET_FILE.exists():
             # the centre-search part of the metric: the shipped network on fresh scans (C5 shapes)
             from recview_gb300 import centre as cs
@@ -397,6 +398,43 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                      "network": str(NET_FILE.relative_to(ROOT)), **summ}
         print(json.dumps(line), flush=True)
     st.close()
+
+
+def dropin_summary(raw, bInc, fdeg, fexp, center, F, reps: int = 20) -> dict:
+    """The reference's own entry points, one slice per call with host buffers, as RecView drives
+    its CUDA back-end: CudaSinogramHost normalises a detector row's frames in place, then
+    CudaReconstHost reconstructs the slice (same geometry and data as the stack, slice 0)."""
+    import time
+    import recview_gb300 as rv
+    from recview_gb300.reconst import ReconInfo
+    nfr = raw.shape[0]
+    frames = np.ascontiguousarray(raw[:, 0, :].cpu().numpy())          # [nframes + 1, W] uint16 bits
+    out = {}
+    ri = ReconInfo(frames.copy(), fdeg, bInc, center=0, fexp=fexp, maxSinogrLen=nfr)
+    rv.normalise(ri)                                                    # warm-up
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ri.rows[:] = frames
+        rv.normalise(ri)
+    t_norm = (time.perf_counter() - t0) / reps
+    sino = ri.rows.copy()
+    rr = ReconInfo(sino, fdeg, bInc, center=center, fFilter=F, maxSinogrLen=nfr, nviews=nfr - 1)
+    for _ in range(3):
+        rr.reset_output()
+        rv.reconstruct_slice(rr)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        rr.reset_output()
+        rv.reconstruct_slice(rr)
+    t_rec = (time.perf_counter() - t0) / reps
+    upd = float(W_DET) * W_DET * N_VIEWS
+    out["reconstruct_ms_per_slice"] = t_rec * 1e3
+    out["reconstruct_tau_ns"] = t_rec * 1e9 / upd
+    out["normalise_ms_per_slice"] = t_norm * 1e3
+    out["slices_per_s"] = 1.0 / (t_rec + t_norm)
+    out["host_direct"] = bool(rv.lib().RvHostDirectAccess())
+    out["note"] = "CudaSinogramHost + CudaReconstHost per slice, host buffers, host wall clock"
+    return out
 
 
 def forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, steps: int = 3) -> dict:

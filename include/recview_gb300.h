@@ -389,6 +389,12 @@ int RvGetBackprojectionVariant(int* variant, int* format);
  * on the current device. */
 int RvProbeThroughput(double* out, int n);
 
+/* 1 when kernels on the current device read and write pageable host memory directly (the GPU
+ * shares the host's page tables, as on Grace-based systems) and RV_NO_HOST_DIRECT is not set:
+ * CudaReconstHost then takes the caller's sinogram rows and slice buffer without staged copies
+ * (no reference counterpart). */
+int RvHostDirectAccess(void);
+
 /* Failure-detection self-check (no reference counterpart): one CTA waits, with the kernels'
  * bounded mbarrier wait (2^log2_tries tries of at most ~1 us each, log2_tries 8..16), on a
  * barrier that nothing completes.  Returns RV_ERR_KERNEL_STATUS when the wait ran out and was

@@ -223,6 +223,7 @@ PROTOTYPES = {
     "RvGetWindowViolations": (C.c_ulonglong, []),
     "RvProbeThroughput": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "RvTestBoundedWait": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "RvHostDirectAccess": (C.c_int, []),
     "RvRescaleSlices": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
                                   c_int_p, C.c_void_p]),
     "RvGetAxis": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,

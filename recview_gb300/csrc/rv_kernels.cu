@@ -554,6 +554,8 @@ __global__ void k_probe_lds(int* sink, int iters) {
 }
 }  // namespace rv
 
+extern "C" int RvHostDirectAccess(void) { return rv::host_direct_access() ? 1 : 0; }
+
 extern "C" int RvProbeThroughput(double* out, int n) {
     if (!out || n < 2) return RV_ERR_BAD_ARGUMENT;
     int dev = 0, sms = 0;
