@@ -521,35 +521,50 @@ extern "C" void CudaSinogramHost(RECONST_INFO* ri, int idev, bool bReport) {
             fail(ri, RV_ERR_DEVICE_OOM, "Out of CUDA device memory (sinogram)");
             return;
         }
-        if (!c->stage(nrows * row_bytes)) {
-            fail(ri, RV_ERR_PINNED_ALLOC, "pinned staging buffer");
+        // where the device reads and writes pageable host memory directly, the kernel works on
+        // the caller's rows in place through a table of their pointers; otherwise every row is
+        // staged in and the sample rows copied back
+        const bool direct = host_direct_access();
+        const size_t stage_bytes = direct ? nrows * sizeof(short*) : nrows * row_bytes;
+        if (!c->stage(stage_bytes) || (direct && !c->rowptr.ensure(stage_bytes))) {
+            fail(ri, direct ? RV_ERR_DEVICE_OOM : RV_ERR_PINNED_ALLOC, "row staging");
             return;
         }
         char* hs = static_cast<char*>(c->h_stage);
-        for (size_t r = 0; r < nrows; r++) memcpy(hs + r * row_bytes, ri->iSinogr[r], row_bytes);
+        if (direct) {
+            short** hp = reinterpret_cast<short**>(hs);
+            for (size_t r = 0; r < nrows; r++) hp[r] = ri->iSinogr[r];
+        } else {
+            for (size_t r = 0; r < nrows; r++) memcpy(hs + r * row_bytes, ri->iSinogr[r], row_bytes);
+        }
         cudaStream_t s = 0;
-        bool ok = cuda_ok(cudaMemcpyAsync(c->raw.p, hs, nrows * row_bytes, cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D, "raw rows") &&
+        bool ok = cuda_ok(cudaMemcpyAsync(direct ? c->rowptr.p : c->raw.p, hs, stage_bytes, cudaMemcpyHostToDevice, s),
+                          RV_ERR_COPY_H2D, "raw rows") &&
                   cuda_ok(cudaMemcpyAsync(c->jobs.p, jobs.data(), nj * sizeof(RowJob), cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D, "jobs") &&
                   cuda_ok(cudaMemcpyAsync(c->shift.p, shifts.data(), nj * sizeof(int), cudaMemcpyHostToDevice, s), RV_ERR_COPY_H2D, "shifts");
         if (ok) {
             NormLaunch nl{};
             nl.raw = static_cast<const uint16_t*>(c->raw.p);
             nl.out = static_cast<short*>(c->sino_out.p);
+            nl.row_ptr = direct ? static_cast<const uint16_t* const*>(c->rowptr.p) : nullptr;
             nl.jobs = static_cast<const RowJob*>(c->jobs.p);
             nl.njobs = nj;
             nl.ixdim = W;
             nl.pixmin = pixmin;
             nl.zernike = (ri->dReconFlags & RV_RQFLAGS_ZERNIKE) ? 1 : 0;
             nl.shift = static_cast<const int*>(c->shift.p);
-            ok = cuda_ok(launch_normalise(nl, s), RV_ERR_LAUNCH, "normalise kernel") &&
-                 cuda_ok(cudaMemcpyAsync(hs, c->sino_out.p, nrows * row_bytes, cudaMemcpyDeviceToHost, s), RV_ERR_COPY_D2H, "rows") &&
-                 cuda_ok(cudaStreamSynchronize(s), RV_ERR_LAUNCH, "normalise");
+            ok = cuda_ok(launch_normalise(nl, s), RV_ERR_LAUNCH, "normalise kernel");
+            if (ok && !direct)
+                ok = cuda_ok(cudaMemcpyAsync(hs, c->sino_out.p, nrows * row_bytes, cudaMemcpyDeviceToHost, s), RV_ERR_COPY_D2H,
+                             "rows");
+            if (ok) ok = cuda_ok(cudaStreamSynchronize(s), RV_ERR_LAUNCH, "normalise");
         }
         if (!ok) {
             ri->iStatus = RECONST_INFO_ERROR;
             return;
         }
-        for (int q = 0; q < nj; q++) memcpy(ri->iSinogr[jobs[q].dst], hs + (size_t)jobs[q].dst * row_bytes, row_bytes);
+        if (!direct)
+            for (int q = 0; q < nj; q++) memcpy(ri->iSinogr[jobs[q].dst], hs + (size_t)jobs[q].dst * row_bytes, row_bytes);
     }
     if (error) {
         fail(ri, RV_ERR_BAD_ARGUMENT, "CudaSinogramHost: no flat frame brackets a sample frame");

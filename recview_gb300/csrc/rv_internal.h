@@ -152,6 +152,9 @@ struct NormLaunch {
     int pixmin;
     int zernike;
     const int* shift;         // per job drift shift in pixels (may be null)
+    const uint16_t* const* row_ptr;  // if set: row r is row_ptr[r] for every role (it may be host
+                                     // memory the device reads and writes directly), and the
+                                     // result replaces row_ptr[dst] in place; raw/out unused
 };
 cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s);
 

@@ -85,12 +85,14 @@ __device__ __forceinline__ void normalise_row(const uint16_t* r, const uint16_t*
                      ((reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(f0) | reinterpret_cast<uintptr_t>(f1) |
                        reinterpret_cast<uintptr_t>(dk) | reinterpret_cast<uintptr_t>(out)) & 7) == 0;
     if (vec) {
-        // four samples per thread and step, all four rows loaded before any arithmetic
+        // four samples per thread and step, all four rows loaded before any arithmetic.  Plain
+        // (generic) loads: the rows may be shared memory (an in-place row's copy) or the caller's
+        // host memory, where the read-only global path does not apply.
         for (int x4 = tid; x4 < (W >> 2); x4 += NT) {
-            const uint2 vr = __ldg(reinterpret_cast<const uint2*>(r) + x4);
-            const uint2 v0 = __ldg(reinterpret_cast<const uint2*>(f0) + x4);
-            const uint2 v1 = __ldg(reinterpret_cast<const uint2*>(f1) + x4);
-            const uint2 vd = __ldg(reinterpret_cast<const uint2*>(dk) + x4);
+            const uint2 vr = reinterpret_cast<const uint2*>(r)[x4];
+            const uint2 v0 = reinterpret_cast<const uint2*>(f0)[x4];
+            const uint2 v1 = reinterpret_cast<const uint2*>(f1)[x4];
+            const uint2 vd = reinterpret_cast<const uint2*>(dk)[x4];
             short o[4] = {0, 0, 0, 0};
             if (!zero) {
 #pragma unroll
@@ -133,14 +135,30 @@ __device__ __forceinline__ void normalise_row(const uint16_t* r, const uint16_t*
 }
 
 __global__ void k_normalise(NormLaunch p) {
-    extern __shared__ int sm_norm[];   // [0]: recheck count, [1 ..]: flagged positions
+    extern __shared__ int sm_norm[];   // [0]: recheck count, [1 .. W]: flagged positions, then
+                                       // (row-pointer mode) a copy of the sample row
     const RowJob job = p.jobs[blockIdx.x];
     const int W = p.ixdim;
-    const uint16_t* r = p.raw + (size_t)job.src_row * W;
-    const uint16_t* f0 = p.raw + (size_t)job.flat0_row * W;
-    const uint16_t* f1 = p.raw + (size_t)job.flat1_row * W;
-    const uint16_t* dk = p.raw + (size_t)job.dark_row * W;
-    short* out = p.out + (size_t)job.dst * W;
+    const uint16_t *r, *f0, *f1, *dk;
+    short* out;
+    if (p.row_ptr) {
+        // the result replaces the sample row in place: read that row into shared memory first
+        // (a drift shift reads other positions of it)
+        uint16_t* rowcopy = reinterpret_cast<uint16_t*>(sm_norm + ((W + 4) & ~3));   // 16-byte aligned
+        const uint16_t* src = p.row_ptr[job.src_row];
+        for (int x = threadIdx.x; x < W; x += blockDim.x) rowcopy[x] = src[x];
+        r = rowcopy;
+        f0 = p.row_ptr[job.flat0_row];
+        f1 = p.row_ptr[job.flat1_row];
+        dk = p.row_ptr[job.dark_row];
+        out = reinterpret_cast<short*>(const_cast<uint16_t*>(p.row_ptr[job.dst]));
+    } else {
+        r = p.raw + (size_t)job.src_row * W;
+        f0 = p.raw + (size_t)job.flat0_row * W;
+        f1 = p.raw + (size_t)job.flat1_row * W;
+        dk = p.raw + (size_t)job.dark_row * W;
+        out = p.out + (size_t)job.dst * W;
+    }
     const int sh = p.shift ? p.shift[blockIdx.x] : 0;
     if (threadIdx.x == 0) sm_norm[0] = 0;
     __syncthreads();
@@ -149,7 +167,8 @@ __global__ void k_normalise(NormLaunch p) {
 
 cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
     if (p.njobs <= 0) return cudaSuccess;
-    const size_t smem = ((size_t)p.ixdim + 1) * sizeof(int);
+    const size_t smem = p.row_ptr ? (((size_t)p.ixdim + 4) & ~(size_t)3) * sizeof(int) + (((size_t)p.ixdim * 2 + 15) & ~(size_t)15)
+                                  : ((size_t)p.ixdim + 1) * sizeof(int);
     cudaError_t e = cudaFuncSetAttribute(k_normalise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_normalise<<<p.njobs, 256, smem, s>>>(p);  // one CTA per row

@@ -378,3 +378,39 @@ def test_dropin_staged_copies_equal_direct(gpu, oracle, tmp_path):
     r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert np.array_equal(np.load(tmp_path / "staged.npy"), want)
+
+
+def test_sinogram_staged_copies_equal_direct(gpu, oracle, tmp_path):
+    """CudaSinogramHost normalises the caller's rows in place through their pointers where the
+    device reads pageable host memory; RV_NO_HOST_DIRECT=1 stages them.  Both equal the oracle
+    (drift list, so the shifted reads of the in-place row are covered)."""
+    import os
+    import subprocess
+    import sys
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(61, 160, 90, 2, 79.4, n_ellipsoids=8, nflat_before=2, nflat_after=2)
+    np.save(tmp_path / "raw.npy", raw)
+    drift = np.arange(raw.shape[0]) % 9 - 4
+    r = raw.copy()
+    ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=2, maxSinogrLen=raw.shape[0],
+                   dReconFlags=abi.RQFLAGS_DRIFTLIST, piDrift=drift)
+    oracle.generate_sinogram(ri)
+    want = r
+    for off in ("0", "1"):
+        script = (
+            "import numpy as np, sys\n"
+            "sys.path.insert(0, '.')\n"
+            "import recview_gb300 as rv\n"
+            "from recview_gb300 import abi, phantom\n"
+            "from recview_gb300.reconst import ReconInfo\n"
+            f"raw = np.load(r'{tmp_path / 'raw.npy'}')\n"
+            f"_, bInc, fdeg, fexp, _ = phantom.raw_stack(61, 160, 90, 2, 79.4, n_ellipsoids=8, nflat_before=2, nflat_after=2)\n"
+            "r = raw.copy()\n"
+            "ri = ReconInfo(r.view(np.int16), fdeg, bInc, center=0, fexp=fexp, iMultiplex=2, maxSinogrLen=raw.shape[0],\n"
+            "               dReconFlags=abi.RQFLAGS_DRIFTLIST, piDrift=np.arange(raw.shape[0]) % 9 - 4)\n"
+            "rv.normalise(ri)\n"
+            f"np.save(r'{tmp_path}' + '/out{off}.npy', r)\n"
+        )
+        env = dict(os.environ, RV_NO_HOST_DIRECT=off)
+        p = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=600)
+        assert p.returncode == 0, p.stderr[-2000:]
+        assert np.array_equal(np.load(tmp_path / f"out{off}.npy"), want), off
