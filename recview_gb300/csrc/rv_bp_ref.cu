@@ -1046,30 +1046,54 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 if (lane == 0) mbar_arrive(smem_u32(&bars[NB + b]));
             }
         }
-        if (!failed) {
+        // Output: the accumulators go through shared memory into row order, then every row of
+        // the tile leaves as coalesced 16-byte stores (8-byte-aligned-free fallback: 4-byte
+        // stores, still row order).  All consumers are past their last chunk (the barrier), the
+        // producer has issued its last fill, so the window buffers are free.
+        if (!consumers_bar_or<CW>(failed)) {
             if (CHECKED && viol) atomicAdd(status_counter, viol);
+            constexpr int RS = 68;                                  // row stride in words (16-byte rows)
+            int* stg = win;                                         // [NS][64][RS]
+            static_assert(NS * 64 * RS <= NB * VC * NSL * WIN, "the output staging fits the buffers");
             const int sh = NQ > 0 ? ray_shift<NQ>(lane, regime) : 0;
             const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
 #pragma unroll
             for (int s = 0; s < S; s++) {
                 int x, y;
                 if (NQ == 0) {
-                    x = X0 + tx + 16 * (s & 3);
-                    y = Y0 + ty + 16 * (s >> 2);
+                    x = tx + 16 * (s & 3);
+                    y = ty + 16 * (s >> 2);
                 } else {
                     const int u = (warp + sh + CW * (s >> 1)) & 63, f = lane + 32 * (s & 1);
-                    x = X0 + ((regime & 1) ? f : u);
-                    y = Y0 + ((regime & 1) ? u : f);
+                    x = (regime & 1) ? f : u;
+                    y = (regime & 1) ? u : f;
                 }
-                if (x < ixdimp && y < ixdimp) {
 #pragma unroll
-                    for (int sl = 0; sl < NS; sl++) {
-                        int* o = J.out + sl * ostride + (size_t)y * ixdimp + x;
-                        if (J.accumulate) atomicAdd(o, acc[sl][s]);   // int sums: any order gives the same slice
-                        else *o = acc[sl][s];
-                    }
+                for (int sl = 0; sl < NS; sl++) stg[(sl * 64 + y) * RS + x] = acc[sl][s];
+            }
+            consumers_bar<CW>();
+            const bool vec = !J.accumulate && (ixdimp & 3) == 0 && !(reinterpret_cast<uintptr_t>(J.out) & 15) &&
+                             !(ostride & 3);
+            for (int e = tid; e < NS * 64 * 16; e += NC) {   // 16 four-pixel groups per row
+                const int sl = e >> 10, y = (e >> 4) & 63, x = (e & 15) * 4;
+                const int gy = Y0 + y, gx = X0 + x;
+                if (gy >= ixdimp || gx >= ixdimp) continue;
+                const int4 v = *reinterpret_cast<const int4*>(stg + (sl * 64 + y) * RS + x);
+                int* o = J.out + sl * ostride + (size_t)gy * ixdimp + gx;
+                if (vec) {
+                    *reinterpret_cast<int4*>(o) = v;
+                } else {
+                    const int w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if (gx + i < ixdimp) {
+                            if (J.accumulate) atomicAdd(o + i, w4[i]);   // int sums: any order gives the same slice
+                            else o[i] = w4[i];
+                        }
                 }
             }
+        } else {
+            failed = true;
         }
     }
     if (__syncthreads_or(failed)) {
