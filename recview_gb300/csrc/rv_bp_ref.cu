@@ -870,6 +870,35 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][S], const int* win, con
 // one chunk of views: NQ == 0 compact blocks (8 consumer warps; colf/rowf in lin[0..3] /
 // lin[4..7]), else the ray layout of orientation O.  Products and y terms are scalar
 // (fl(x fcos), fl(fl(y fsin) + foffset)); the per-pixel sums are paired.
+// Two views at once (both on the fast path): each pixel's two gathers are added in one
+// three-operand integer add.
+template <int WIN, int PAD, int NS, int S, typename FA, typename FB>
+__device__ __forceinline__ void ws_gather_two(int (&acc)[NS][S], unsigned baseA, unsigned baseB, FA fa, FB fb) {
+    const float2 mag = make_float2(8388608.0f, 8388608.0f);
+#pragma unroll
+    for (int i = 0; i < S / 2; i++) {
+        const float2 tA = add2_rz(fa(i), mag), tB = add2_rz(fb(i), mag);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int s = ws_slot<false>(i, h);
+            unsigned bA = __float_as_uint(h ? tA.y : tA.x), bB = __float_as_uint(h ? tB.y : tB.x);
+            if (PAD) {
+                bA += bA >> 4;
+                bB += bB >> 4;
+            }
+            const unsigned aA = baseA + 4u * bA, aB = baseB + 4u * bB;
+            acc[0][s] += lds_s32(aA) + lds_s32(aB);
+            if (NS > 1) acc[1 % NS][s] += lds_s32_off<4 * WIN * (NS > 1 ? 1 : 0)>(aA) + lds_s32_off<4 * WIN * (NS > 1 ? 1 : 0)>(aB);
+            if (NS > 2) acc[2 % NS][s] += lds_s32_off<4 * WIN * (NS > 2 ? 2 : 0)>(aA) + lds_s32_off<4 * WIN * (NS > 2 ? 2 : 0)>(aB);
+            if (NS > 3) acc[3 % NS][s] += lds_s32_off<4 * WIN * (NS > 3 ? 3 : 0)>(aA) + lds_s32_off<4 * WIN * (NS > 3 ? 3 : 0)>(aB);
+        }
+    }
+}
+
+// one chunk of views: NQ == 0 compact blocks (8 consumer warps; colf/rowf in lin[0..3] /
+// lin[4..7]), else the ray layout of orientation O.  Products and y terms are scalar
+// (fl(x fcos), fl(fl(y fsin) + foffset)); the per-pixel sums are paired.  Ray layouts take two
+// fast-path views at a time where they can.
 template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, int CW>
 __device__ __forceinline__ void ws_consume(int (&acc)[NS][128 / CW], const float (&lin)[64 / CW],
                                            const float (&fix)[2], const int* win, const ViewMeta* meta, int b,
@@ -878,6 +907,41 @@ __device__ __forceinline__ void ws_consume(int (&acc)[NS][128 / CW], const float
     for (int vv = 0; vv < nv; vv++) {
         const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
         const unsigned offb = __float_as_uint(g.w);
+        if (NQ > 0 && !CHECKED && vv + 1 < nv) {
+            const float4 g2 = *reinterpret_cast<const float4*>(&meta[b * VC + vv + 1]);
+            const unsigned offb2 = __float_as_uint(g2.w);
+            if (offb & offb2 & 1u) {
+                const unsigned baseA = smem_u32(win + (b * VC + vv) * NSL * WIN) + (offb & ~3u);
+                const unsigned baseB = smem_u32(win + (b * VC + vv + 1) * NSL * WIN) + (offb2 & ~3u);
+                if (O == 0) {   // V: x = lin[q], y = fix[p]
+                    float2 XA[Q / 2], XB[Q / 2];
+#pragma unroll
+                    for (int k = 0; k < Q / 2; k++) {
+                        XA[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
+                        XB[k] = make_float2(fmulr(lin[2 * k], g2.x), fmulr(lin[2 * k + 1], g2.x));
+                    }
+                    const float2 YA0 = bcast2(faddr(fmulr(fix[0], g.y), g.z)), YA1 = bcast2(faddr(fmulr(fix[1], g.y), g.z));
+                    const float2 YB0 = bcast2(faddr(fmulr(fix[0], g2.y), g2.z)), YB1 = bcast2(faddr(fmulr(fix[1], g2.y), g2.z));
+                    ws_gather_two<WIN, PAD, NS, S>(acc, baseA, baseB,
+                                                   [&](int i) { return add2_rn(XA[i >> 1], (i & 1) ? YA1 : YA0); },
+                                                   [&](int i) { return add2_rn(XB[i >> 1], (i & 1) ? YB1 : YB0); });
+                } else {   // H: x = fix[p], y = lin[q]
+                    float2 YA[Q / 2], YB[Q / 2];
+#pragma unroll
+                    for (int k = 0; k < Q / 2; k++) {
+                        YA[k] = make_float2(faddr(fmulr(lin[2 * k], g.y), g.z), faddr(fmulr(lin[2 * k + 1], g.y), g.z));
+                        YB[k] = make_float2(faddr(fmulr(lin[2 * k], g2.y), g2.z), faddr(fmulr(lin[2 * k + 1], g2.y), g2.z));
+                    }
+                    const float2 XA0 = bcast2(fmulr(fix[0], g.x)), XA1 = bcast2(fmulr(fix[1], g.x));
+                    const float2 XB0 = bcast2(fmulr(fix[0], g2.x)), XB1 = bcast2(fmulr(fix[1], g2.x));
+                    ws_gather_two<WIN, PAD, NS, S>(acc, baseA, baseB,
+                                                   [&](int i) { return add2_rn((i & 1) ? XA1 : XA0, YA[i >> 1]); },
+                                                   [&](int i) { return add2_rn((i & 1) ? XB1 : XB0, YB[i >> 1]); });
+                }
+                vv++;
+                continue;
+            }
+        }
         if (NQ == 0) {   // slot s = 4 r + c: x = lin[c], y = lin[4 + r]
             float2 X[2], Yb[4];
 #pragma unroll
