@@ -40,7 +40,7 @@ WORKLOAD = "fbp-2048det-1800views-64slices-raw-uint16"
 # DRAM bytes (read + write) per pixel-view update of the REF back-projection, from one ncu capture
 # of the default variant on 2 slices of this geometry; the traffic grows in proportion to the
 # slices processed, so a full launch moves this times its updates.
-BP_DRAM_BYTES_PER_UPDATE = 2.2244e-1
+BP_DRAM_BYTES_PER_UPDATE = 6.768e-2
 
 
 def parse():
