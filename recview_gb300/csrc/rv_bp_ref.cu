@@ -1883,7 +1883,7 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //        buffers x views per chunk;  12: 128x128, 512 threads, 3 buffers x 4 views;
 //     13: 128x64, 512 threads, 2 x 4;  14, 15: 64x64, 2 buffers x 5 / 6 views, 3 CTAs/SM
 //     16: 64x64, 8 consumer warps + 1 producer warp, ray-aligned lane footprints (shear steps
-//         of 1/8), 2 buffers x 6 views, 3 CTAs/SM;  17: the same with compact 8x4 lane blocks,
+//         of 1/12), 2 buffers x 6 views, 3 CTAs/SM;  17: the same with compact 8x4 lane blocks,
 //         2 buffers x 4 views, 4 CTAs/SM;  18: variant 16's layout over slice pairs (two
 //         slices sharing the geometry per CTA: one index per pixel and view, two gathers),
 //         2 buffers x 4 views x 2 slices, 2 CTAs/SM;  19: variant 18 with 16 consumer warps
@@ -1991,9 +1991,9 @@ static cudaError_t go_ws(const BackprojLaunch& p, cudaStream_t s, bool checked) 
 // geometry; an odd last slice, or per-slice geometry, runs one slice per CTA (variant 16's form)
 template <int VC, int NB, int PAD, int NQ, int MINB, int CW = 8>
 static cudaError_t go_ws_pairs(const BackprojLaunch& p, cudaStream_t s, bool checked) {
-    if (p.geom_slice_stride != 0 || p.nslices < 2) return go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, 0, p.nslices);
+    if (p.geom_slice_stride != 0 || p.nslices < 2) return go_ws_rows<6, 2, PAD, 12, 3>(p, s, checked, 0, p.nslices);
     cudaError_t e = go_ws_rows<VC, NB, PAD, NQ, MINB, 2, CW>(p, s, checked, 0, p.nslices / 2);
-    if (e == cudaSuccess && (p.nslices & 1)) e = go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, p.nslices - 1, 1);
+    if (e == cudaSuccess && (p.nslices & 1)) e = go_ws_rows<6, 2, PAD, 12, 3>(p, s, checked, p.nslices - 1, 1);
     return e;
 }
 
@@ -2001,12 +2001,12 @@ static cudaError_t go_ws_pairs(const BackprojLaunch& p, cudaStream_t s, bool che
 // single slice for the rest; per-slice geometry runs one slice per CTA
 template <int VC, int NB, int PAD, int NQ, int MINB, int CW>
 static cudaError_t go_ws_quads(const BackprojLaunch& p, cudaStream_t s, bool checked) {
-    if (p.geom_slice_stride != 0 || p.nslices < 4) return go_ws_pairs<4, 2, PAD, 8, 2>(p, s, checked);
+    if (p.geom_slice_stride != 0 || p.nslices < 4) return go_ws_pairs<4, 2, PAD, 12, 2>(p, s, checked);
     const int q4 = p.nslices / 4;
     cudaError_t e = go_ws_rows<VC, NB, PAD, NQ, MINB, 4, CW>(p, s, checked, 0, q4);
     const int rest = p.nslices - 4 * q4;
-    if (e == cudaSuccess && rest >= 2) e = go_ws_rows<4, 2, PAD, 8, 2, 2>(p, s, checked, 4 * q4, 1);
-    if (e == cudaSuccess && (rest & 1)) e = go_ws_rows<6, 2, PAD, 8, 3>(p, s, checked, p.nslices - 1, 1);
+    if (e == cudaSuccess && rest >= 2) e = go_ws_rows<4, 2, PAD, 12, 2, 2>(p, s, checked, 4 * q4, 1);
+    if (e == cudaSuccess && (rest & 1)) e = go_ws_rows<6, 2, PAD, 12, 3>(p, s, checked, p.nslices - 1, 1);
     return e;
 }
 
@@ -2037,9 +2037,9 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 13: return go_pipe<4, 4, 4, 4, 4, 2, PAD, 2>(p, s, checked);
     case 14: return go_pipe<2, 4, 4, 4, 5, 2, PAD, 3>(p, s, checked);
     case 15: return go_pipe<2, 4, 4, 4, 6, 2, PAD, 3>(p, s, checked);
-    case 16: return go_ws<6, 2, PAD, 8, 3>(p, s, checked);
+    case 16: return go_ws<6, 2, PAD, 12, 3>(p, s, checked);
     case 17: return go_ws<4, 2, PAD, 0, 4>(p, s, checked);
-    case 18: return go_ws_pairs<4, 2, PAD, 8, 2>(p, s, checked);
+    case 18: return go_ws_pairs<4, 2, PAD, 12, 2>(p, s, checked);
     case 19: return go_ws_pairs<4, 2, PAD, 8, 2, 16>(p, s, checked);
     case 20: return go_ws_quads<4, 2, PAD, 8, 1, 16>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
@@ -2144,10 +2144,10 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 13: return go_pipe_persistent<4, 4, 4, 4, 4, 2, PAD, 2>(jobs, njobs, counter, s);
     case 14: return go_pipe_persistent<2, 4, 4, 4, 5, 2, PAD, 3>(jobs, njobs, counter, s);
     case 15: return go_pipe_persistent<2, 4, 4, 4, 6, 2, PAD, 3>(jobs, njobs, counter, s);
-    case 16: return go_ws_persistent<6, 2, PAD, 8, 3>(jobs, njobs, counter, s);
-    case 18: return go_ws_persistent<4, 2, PAD, 8, 2, 2>(jobs, njobs, counter, s);
+    case 16: return go_ws_persistent<6, 2, PAD, 12, 3>(jobs, njobs, counter, s);
+    case 18: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);
     case 19: return go_ws_persistent<4, 2, PAD, 8, 2, 2, 16>(jobs, njobs, counter, s);
-    case 20: return go_ws_persistent<4, 2, PAD, 8, 2, 2>(jobs, njobs, counter, s);
+    case 20: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
