@@ -273,49 +273,42 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         for (int x = tid; x < W; x += NT) strip[x] = job.zero ? (short)0 : r[x];
         __syncthreads();
     }
-    // ---- R5: placement with edge padding and integer zoom (source/general.cpp:2105-2126) ------
-    {
-        const int z = p.d.iIntpDim;
-        const int ic = p.ic_per_job ? job.ic : p.ic;
-        const int idx0 = (0 - ic) * z + (half - 1);
-        const int idx1 = (W - 1 - ic) * z + (half - 1) + 1;
-        // z = 2^iZooming: C's truncating division by z as shifts (a negative numerator is biased
-        // by z - 1 first)
-        const int lz = __ffs(z) - 1;
-        auto divz = [&](int x) { return (x + ((x >> 31) & (z - 1))) >> lz; };
-        for (int m = tid; m < n; m += NT) {
-            float v;
-            if (m < idx0) v = strip[0];
-            else if (m >= idx1) v = strip[W - 1];
-            else {
-                const int k = (m - idx0) >> lz, j = (m - idx0) & (z - 1);
-                if (j == 0) v = strip[k];
-                else v = (float)(divz((int)strip[k] * (z - j)) + divz((int)strip[k + 1] * j));
-            }
-            buf[m] = make_float2(v, 0.0f);
-        }
-    }
-    __syncthreads();
+    // ---- R5: placement with edge padding and integer zoom (source/general.cpp:2105-2126), taken
+    // straight into the first forward pass (CFft::FFT1Rev, source/cfft.cpp:193-209): butterfly j
+    // combines placed samples half-1-j and n-1-j, whose imaginary parts are zero, so the placed
+    // row never goes through shared memory.
+    const int z = p.d.iIntpDim;
+    const int ic = p.ic_per_job ? job.ic : p.ic;
+    const int idx0 = (0 - ic) * z + (half - 1);
+    const int idx1 = (W - 1 - ic) * z + (half - 1) + 1;
+    // z = 2^iZooming: C's truncating division by z as shifts (a negative numerator is biased
+    // by z - 1 first)
+    const int lz = __ffs(z) - 1;
+    auto divz = [&](int x) { return (x + ((x >> 31) & (z - 1))) >> lz; };
+    auto placed = [&](int m) -> float {
+        if (m < idx0) return strip[0];
+        if (m >= idx1) return strip[W - 1];
+        const int k = (m - idx0) >> lz, j = (m - idx0) & (z - 1);
+        if (j == 0) return strip[k];
+        return (float)(divz((int)strip[k] * (z - j)) + divz((int)strip[k + 1] * j));
+    };
 
     float2 a[BPT], b[BPT];
     // ---- forward transform (CFft::FFT1Rev) ----------------------------------------------------
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
-        a[i] = buf[half - 1 - j];
-        b[i] = buf[n - 1 - j];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < BPT; i++) {
-        const int j = tid + i * NT;
-        buf[2 * j] = cadd(a[i], b[i]);
-        buf[2 * j + 1] = csub(a[i], b[i]);
+        const float pa = placed(half - 1 - j), pb = placed(n - 1 - j);
+        buf[2 * j] = make_float2(fadd(pa, pb), 0.0f);        // imaginary part 0 + 0
+        buf[2 * j + 1] = make_float2(fsub(pa, pb), 0.0f);    // and 0 - 0
     }
     __syncthreads();
     fft_general_passes<BPT>(buf, tw, np, half, tid, NT);
     // last forward pass writes reversed (source/cfft.cpp:246-265); the filter multiply
-    // (source/general.cpp:2128, CCmplx::operator*=(float)) is applied on the way out.
+    // (source/general.cpp:2128, CCmplx::operator*=(float)) is applied on the way out, and the
+    // first inverse pass (CFft::FFT1, source/cfft.cpp:279-296) follows in registers: butterfly j
+    // of the last forward pass writes positions n-j and half-j (0 and half for j = 0), which are
+    // exactly the two inputs of the first inverse butterfly half-j (0).
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
@@ -330,39 +323,34 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         const int om = (j == 0) ? half : half - j;
         const float2 vp = cadd(a[i], b[i]), vm = csub(a[i], b[i]);
         const float fp = __ldg(p.filt + op), fm = __ldg(p.filt + om);
-        buf[op] = make_float2(fmul(vp.x, fp), fmul(vp.y, fp));
-        buf[om] = make_float2(fmul(vm.x, fm), fmul(vm.y, fm));
-    }
-    __syncthreads();
-    // ---- inverse transform (CFft::FFT1) --------------------------------------------------------
-#pragma unroll
-    for (int i = 0; i < BPT; i++) {
-        const int j = tid + i * NT;
-        a[i] = buf[j];
-        b[i] = buf[j + half];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < BPT; i++) {
-        const int j = tid + i * NT;
-        buf[2 * j] = cadd(a[i], b[i]);
-        buf[2 * j + 1] = csub(a[i], b[i]);
+        const float2 yp = make_float2(fmul(vp.x, fp), fmul(vp.y, fp));   // spectrum at op
+        const float2 ym = make_float2(fmul(vm.x, fm), fmul(vm.y, fm));   // spectrum at om
+        // inverse butterfly k reads x[k] and x[k + half]: k = om (x[k] = ym, x[k + half] = yp), or
+        // k = 0 for j = 0 (x[0] = yp, x[half] = ym)
+        const int k = (j == 0) ? 0 : om;
+        const float2 lo = (j == 0) ? yp : ym, hi = (j == 0) ? ym : yp;
+        buf[2 * k] = cadd(lo, hi);
+        buf[2 * k + 1] = csub(lo, hi);
     }
     __syncthreads();
     fft_general_passes<BPT>(buf, tw, np, half, tid, NT);
-    // last inverse pass with the two halves swapped (source/cfft.cpp:355-368)
+    // last inverse pass with the two halves swapped (source/cfft.cpp:355-368).  Only real parts
+    // are used from here on, so the pass forms Re(x w) alone and stores floats.
+    float* re = reinterpret_cast<float*>(buf);
+    float ar[BPT], br[BPT];
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
-        a[i] = buf[j];
-        b[i] = cmul(buf[j + half], __ldg(tw + half + j));
+        const float2 x = buf[j + half], w = __ldg(tw + half + j);
+        ar[i] = buf[j].x;
+        br[i] = fsub(fmul(x.x, w.x), fmul(x.y, w.y));   // Re of cmul(x, w)
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
-        buf[j] = csub(a[i], b[i]);
-        buf[j + half] = cadd(a[i], b[i]);
+        re[j] = fsub(ar[i], br[i]);
+        re[j + half] = fadd(ar[i], br[i]);
     }
     __syncthreads();
 
@@ -370,15 +358,15 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
     // the 1/16 sub-sample int table (source/general.cpp:2130-2137).
     const float inv_n = 1.0f / (float)n;
     const int ixdimp = p.d.ixdimp;
-    const int rbase = n - 1 - p.d.ihoffset;  // q[j] = buf[rbase - j].x / n
+    const int rbase = n - 1 - p.d.ihoffset;  // q[j] = re[rbase - j] / n
     if (p.table) {
         int* tab = p.table + (size_t)job.dst * p.table_stride;
         for (int j = tid; j < ixdimp; j += NT) {
-            const float qj = fmul(buf[rbase - j].x, inv_n);
+            const float qj = fmul(re[rbase - j], inv_n);
             const float p0 = fmul(qj, 100.0f);
             float p1p0 = 0.0f;
             if (j != ixdimp - 1) {
-                const float qn = fmul(buf[rbase - j - 1].x, inv_n);
+                const float qn = fmul(re[rbase - j - 1], inv_n);
                 p1p0 = fmul(fmul(fsub(qn, qj), 0.0625f), 100.0f);  // (q1-q0)/16*100
             }
             if (p.table_fmt == kTabPair) {
@@ -413,7 +401,7 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         if (p.mode != RV_MODE_LIN) {
             __shared__ float red[32];
             float m = 0.0f;
-            for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(buf[rbase - j].x));
+            for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(re[rbase - j]));
             for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
             if ((tid & 31) == 0) red[tid >> 5] = m;
             __syncthreads();
@@ -432,8 +420,8 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         for (int j = tid; j < ps; j += NT) {
             float v0 = 0.0f, dv = 0.0f;
             if (j < ixdimp) {
-                v0 = fmul(fmul(buf[rbase - j].x, inv_n), 100.0f);
-                if (j + 1 < ixdimp) dv = fsub(fmul(fmul(buf[rbase - j - 1].x, inv_n), 100.0f), v0);
+                v0 = fmul(fmul(re[rbase - j], inv_n), 100.0f);
+                if (j + 1 < ixdimp) dv = fsub(fmul(fmul(re[rbase - j - 1], inv_n), 100.0f), v0);
             }
             const size_t at = (size_t)job.dst * p.row_stride + j;
             if (p.mode == RV_MODE_LIN) static_cast<float2*>(p.rows16)[at] = make_float2(v0, dv);
