@@ -176,21 +176,91 @@ cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
 }
 
 
+// Shared-memory position of transform element a: bits 1-3 of a are flipped by bits 4-6, so the
+// strided stores of the early fused passes (a warp writing elements 2^(l+3) apart) and 16-byte
+// stores of adjacent pairs spread over all banks, while runs of 16 consecutive elements (every
+// load) stay conflict-free.  Elements 2i and 2i+1 stay adjacent.
+__device__ __forceinline__ int fsw(int a) { return a ^ ((a >> 3) & 14); }
+// stores elements 2i and 2i+1 as one 16-byte word
+__device__ __forceinline__ void st_pair(float2* buf, int i, float2 lo, float2 hi) {
+    reinterpret_cast<float4*>(buf)[fsw(2 * i) >> 1] = make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
 // The general radix-2 Stockham passes l = 1 .. np-2 (source/cfft.cpp:210-245, 310-345): pass l
 // reads x[j], x[j + n/2] for butterfly j = m 2^l + q and writes y[2m 2^l + q] = x[j] + w b,
-// y[(2m+1) 2^l + q] = x[j] - w b (b = x[j + n/2], w = pass l's twiddle q).  Two consecutive
-// passes l, l+1 (2^(l+1) <= n/4) close over groups of four: butterflies g and g + n/4 of pass l
-// (g < n/4) produce exactly the inputs of butterflies 2m 2^l + q and 2m 2^l + 2^l + q of pass
-// l+1, so one thread runs both passes of a group in registers -- the same operations in the same
-// order, with half the shared-memory round trips and barriers.  An odd pass left over runs alone.
+// y[(2m+1) 2^l + q] = x[j] - w b (b = x[j + n/2], w = pass l's twiddle q).
+// Three consecutive passes l, l+1, l+2 (2^(l+2) <= n/2) close over groups of eight: the inputs
+// x[g + k n/8] (g < n/8, k = 0..7) of pass l feed butterflies c, c + 2^l, c + n/4, c + n/4 + 2^l
+// of pass l+1 (c = 2g - q), whose outputs are the inputs of butterflies B + t 2^l (t = 0..3,
+// B = 4m 2^l + q) of pass l+2, which write o + t 2^l and o + 4 2^l + t 2^l (o = 8m 2^l + q).
+// One thread runs all three passes of a group in registers -- the same operations in the same
+// order -- so two of every three shared-memory round trips and barriers go.  Two passes left
+// over run as a pair over groups of four (c and c + n/4 only), one alone.
 template <int BPT>
 __device__ __forceinline__ void fft_general_passes(float2* buf, const float2* __restrict__ tw, int np, int half,
                                                    int tid, int NT) {
     int l = 1;
-    if (BPT >= 2) {
+    if (BPT >= 4) {   // (smaller rows keep every thread busy with pairs)
+        constexpr int G = BPT >= 4 ? BPT / 4 : 1;   // groups of eight per thread
+        const int eighth = half >> 2;
+        for (; l + 2 < np - 1; l += 3) {
+            const int al = 1 << l, mask = al - 1;
+            float2 t0[G], t1[G], t2[G], t3[G], t4[G], t5[G], t6[G], t7[G];
+#pragma unroll
+            for (int i = 0; i < G; i++) {
+                const int g = tid + i * NT;
+                const int q = g & mask;
+                const float2 w1 = __ldg(tw + al + q);                                  // pass l
+                const float2 w2a = __ldg(tw + 2 * al + q), w2b = __ldg(tw + 3 * al + q);   // pass l+1
+                float2 P[4], M[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const float2 x = buf[fsw(g + k * eighth)], xb = cmul(buf[fsw(g + k * eighth + half)], w1);
+                    P[k] = cadd(x, xb);
+                    M[k] = csub(x, xb);
+                }
+                const float2 b0 = cmul(P[2], w2a), b1 = cmul(M[2], w2b);
+                const float2 b2 = cmul(P[3], w2a), b3 = cmul(M[3], w2b);
+                const float2 R0 = cadd(P[0], b0), S0 = csub(P[0], b0);
+                const float2 R1 = cadd(M[0], b1), S1 = csub(M[0], b1);
+                const float2 R2 = cadd(P[1], b2), S2 = csub(P[1], b2);
+                const float2 R3 = cadd(M[1], b3), S3 = csub(M[1], b3);
+                // pass l+2: butterfly B + t al reads (R0, R2), (R1, R3), (S0, S2), (S1, S3)
+                const float2 c0 = cmul(R2, __ldg(tw + 4 * al + q));
+                const float2 c1 = cmul(R3, __ldg(tw + 5 * al + q));
+                const float2 c2 = cmul(S2, __ldg(tw + 6 * al + q));
+                const float2 c3 = cmul(S3, __ldg(tw + 7 * al + q));
+                t0[i] = cadd(R0, c0);
+                t4[i] = csub(R0, c0);
+                t1[i] = cadd(R1, c1);
+                t5[i] = csub(R1, c1);
+                t2[i] = cadd(S0, c2);
+                t6[i] = csub(S0, c2);
+                t3[i] = cadd(S1, c3);
+                t7[i] = csub(S1, c3);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < G; i++) {
+                const int g = tid + i * NT;
+                const int o = 8 * (g >> l) * al + (g & mask);
+                buf[fsw(o)] = t0[i];
+                buf[fsw(o + al)] = t1[i];
+                buf[fsw(o + 2 * al)] = t2[i];
+                buf[fsw(o + 3 * al)] = t3[i];
+                buf[fsw(o + 4 * al)] = t4[i];
+                buf[fsw(o + 5 * al)] = t5[i];
+                buf[fsw(o + 6 * al)] = t6[i];
+                buf[fsw(o + 7 * al)] = t7[i];
+            }
+            __syncthreads();
+        }
+    }
+    if (BPT >= 2) {   // pairs of passes over groups of four
         constexpr int G = BPT >= 2 ? BPT / 2 : 1;   // groups of four per thread
         const int quarter = half >> 1;
-        for (; l + 1 < np - 1; l += 2) {
+        // after the triples at most one pair is left (BPT >= 4); smaller rows take all pairs here
+        for (int it = 0; l + 1 < np - 1 && (BPT < 4 || it == 0); l += 2, it++) {
             const int al = 1 << l, mask = al - 1;
             float2 u0[G], u1[G], v0[G], v1[G];
 #pragma unroll
@@ -198,8 +268,8 @@ __device__ __forceinline__ void fft_general_passes(float2* buf, const float2* __
                 const int g = tid + i * NT;
                 const int q = g & mask;
                 const float2 w = __ldg(tw + al + q);                  // pass l
-                const float2 x0 = buf[g], x1 = cmul(buf[g + half], w);
-                const float2 x2 = buf[g + quarter], x3 = cmul(buf[g + quarter + half], w);
+                const float2 x0 = buf[fsw(g)], x1 = cmul(buf[fsw(g + half)], w);
+                const float2 x2 = buf[fsw(g + quarter)], x3 = cmul(buf[fsw(g + quarter + half)], w);
                 u0[i] = cadd(x0, x1);
                 u1[i] = csub(x0, x1);
                 v0[i] = cmul(cadd(x2, x3), __ldg(tw + 2 * al + q));        // pass l+1, butterfly 2m 2^l + q
@@ -210,10 +280,10 @@ __device__ __forceinline__ void fft_general_passes(float2* buf, const float2* __
             for (int i = 0; i < G; i++) {
                 const int g = tid + i * NT;
                 const int o = 4 * (g >> l) * al + (g & mask);   // y'[2m 2^(l+1) + q]
-                buf[o] = cadd(u0[i], v0[i]);
-                buf[o + 2 * al] = csub(u0[i], v0[i]);
-                buf[o + al] = cadd(u1[i], v1[i]);
-                buf[o + 3 * al] = csub(u1[i], v1[i]);
+                buf[fsw(o)] = cadd(u0[i], v0[i]);
+                buf[fsw(o + 2 * al)] = csub(u0[i], v0[i]);
+                buf[fsw(o + al)] = cadd(u1[i], v1[i]);
+                buf[fsw(o + 3 * al)] = csub(u1[i], v1[i]);
             }
             __syncthreads();
         }
@@ -224,16 +294,16 @@ __device__ __forceinline__ void fft_general_passes(float2* buf, const float2* __
 #pragma unroll
         for (int i = 0; i < BPT; i++) {
             const int j = tid + i * NT;
-            a[i] = buf[j];
-            b[i] = cmul(buf[j + half], __ldg(tw + al + (j & mask)));
+            a[i] = buf[fsw(j)];
+            b[i] = cmul(buf[fsw(j + half)], __ldg(tw + al + (j & mask)));
         }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < BPT; i++) {
             const int j = tid + i * NT;
             const int o = 2 * j - (j & mask);
-            buf[o] = cadd(a[i], b[i]);
-            buf[o + al] = csub(a[i], b[i]);
+            buf[fsw(o)] = cadd(a[i], b[i]);
+            buf[fsw(o + al)] = csub(a[i], b[i]);
         }
         __syncthreads();
     }
@@ -299,8 +369,8 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
         const float pa = placed(half - 1 - j), pb = placed(n - 1 - j);
-        buf[2 * j] = make_float2(fadd(pa, pb), 0.0f);        // imaginary part 0 + 0
-        buf[2 * j + 1] = make_float2(fsub(pa, pb), 0.0f);    // and 0 - 0
+        st_pair(buf, j, make_float2(fadd(pa, pb), 0.0f),     // imaginary parts 0 + 0
+                make_float2(fsub(pa, pb), 0.0f));            // and 0 - 0
     }
     __syncthreads();
     fft_general_passes<BPT>(buf, tw, np, half, tid, NT);
@@ -312,8 +382,8 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
-        a[i] = buf[j];
-        b[i] = (j == 0) ? buf[j + half] : cmul(buf[j + half], __ldg(tw + half + j));
+        a[i] = buf[fsw(j)];
+        b[i] = (j == 0) ? buf[fsw(j + half)] : cmul(buf[fsw(j + half)], __ldg(tw + half + j));
     }
     __syncthreads();
 #pragma unroll
@@ -329,8 +399,7 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         // k = 0 for j = 0 (x[0] = yp, x[half] = ym)
         const int k = (j == 0) ? 0 : om;
         const float2 lo = (j == 0) ? yp : ym, hi = (j == 0) ? ym : yp;
-        buf[2 * k] = cadd(lo, hi);
-        buf[2 * k + 1] = csub(lo, hi);
+        st_pair(buf, k, cadd(lo, hi), csub(lo, hi));
     }
     __syncthreads();
     fft_general_passes<BPT>(buf, tw, np, half, tid, NT);
@@ -341,8 +410,8 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
 #pragma unroll
     for (int i = 0; i < BPT; i++) {
         const int j = tid + i * NT;
-        const float2 x = buf[j + half], w = __ldg(tw + half + j);
-        ar[i] = buf[j].x;
+        const float2 x = buf[fsw(j + half)], w = __ldg(tw + half + j);
+        ar[i] = buf[fsw(j)].x;
         br[i] = fsub(fmul(x.x, w.x), fmul(x.y, w.y));   // Re of cmul(x, w)
     }
     __syncthreads();

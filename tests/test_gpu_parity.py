@@ -28,6 +28,8 @@ SLICE_CASES = [
     (10, 160, 150, 79.9, 2, abi.FILT_SHEPP, abi.RQFLAGS_USEONLYODDFRAMES, -1.3),
     (11, 1000, 400, 499.3, 2, abi.FILT_SHEPP, 0, 0.0),       # not a multiple of the 64 tile
     (12, 300, 360, 150.0, 2, abi.FILT_RAMP, 0, 0.0),         # 360 views over 180 deg, integer centre
+    (13, 4096, 24, 2050.8, 2, abi.FILT_SHEPP, 0, 0.0),       # 8192-point transform
+    (14, 2048, 8, 1018.4, 4, abi.FILT_HAN, 0, 0.0),          # x4 zoom: 16384-point transform
 ]
 
 
