@@ -32,11 +32,17 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(
 // ---------------------------------------------------------------------------------------------
 // R1: one normalised sample (source/general.cpp:2466-2503).  The incident intensity is a float
 // expression in the reference (int*float, ushort+float, float-ushort); only the log ratio is in
-// double.  Fast path: FP32 log with an error bound of 7e-3 on v = 3000*log(I0/S) + 0.5; samples
-// whose v lies within 0.02 of an integer are recomputed in FP64 exactly as the reference does.
-// FP64 is slow on this GPU and a divergent FP64 branch costs its whole warp, so the row kernels
-// take the fast path for every sample first (norm_fast flags the ~4% it cannot decide) and run
-// the FP64 recheck (norm_exact) afterwards over a compacted list, 32 flagged samples per warp.
+// double: v = (short)(int)(3000 log(I0 / S) + 0.5).
+// Fast path in FP32: L = logf(fl(I0 / S)), and 3000 L + 0.5 held exactly as p + 0.5 + e
+// (p = fl(3000 L), e = fma(3000, L, -p) its exact rounding error; p + 0.5 is exact).  Its
+// distance from the true value is 3000 |L - ln(I0/S)| <= 3000 (ulp terms of logf + 2^-24 of the
+// correctly rounded quotient); the band below allows 4 ulp(L) for logf's documented 1 ulp and
+// 2^-12 for the remaining roundings, so every sample outside it is decided on the right side of
+// its integer.  Samples inside the band (under 1% for |L| < 4) are recomputed in FP64 exactly as
+// the reference does.  FP64 is slow on this GPU and a divergent FP64 branch costs its whole warp,
+// so the row kernels take the fast path for every sample first (norm_fast flags what it cannot
+// decide) and run the FP64 recheck (norm_exact) afterwards over a compacted list, 32 flagged
+// samples per warp.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ float norm_incident(int f0, int f1, int dark, float t0) {
     const float prod = fmul((float)(f1 - f0), t0);
@@ -50,10 +56,19 @@ __device__ __forceinline__ short norm_fast(int raw, int f0, int f1, int dark, fl
     if (!(dinc > 0.0f)) return 0;
     const int s = raw - dark;
     if (s < pixmin) return 0;
-    const float ratio = __fdiv_rn(dinc, (float)s);
-    const float w = fadd(fmul(logf(ratio), 3000.0f), 0.5f);
-    const float dist = fabsf(w - rintf(w));
-    if (dist > 0.02f) return (short)__float2int_rz(w);
+    const float L = logf(__fdiv_rn(dinc, (float)s));
+    const float p = __fmul_rn(L, 3000.0f);
+    const float e = __fmaf_rn(L, 3000.0f, -p);           // 3000 L = p + e exactly
+    const float wh = __fadd_rn(p, 0.5f);                  // exact: |p| < 2^22
+    const float N = rintf(wh);
+    const float t = __fadd_rn(__fsub_rn(wh, N), e);       // (3000 L + 0.5) - N, |t| <= 0.51
+    const float ulpL = __fmul_rn(__int_as_float(__float_as_int(L) & 0x7f800000), 1.1920929e-7f);   // 2^-23 2^E
+    const float band = __fadd_rn(__fmul_rn(ulpL, 12000.0f), 4.3e-4f);   // 3000 (4 ulp + 2^-24) + 2^-12
+    if (fabsf(t) > band) {
+        // truncation toward zero of N + t
+        const int n = __float2int_rn(N);
+        return (short)(n > 0 ? (t > 0.0f ? n : n - 1) : (n < 0 ? (t < 0.0f ? n : n + 1) : 0));
+    }
     *recheck = true;
     return 0;
 }
