@@ -204,7 +204,7 @@ __device__ __forceinline__ void st_pair(float2* buf, int i, float2 lo, float2 hi
 // The general radix-2 Stockham passes l = 1 .. np-2 (source/cfft.cpp:210-245, 310-345): pass l
 // reads x[j], x[j + n/2] for butterfly j = m 2^l + q and writes y[2m 2^l + q] = x[j] + w b,
 // y[(2m+1) 2^l + q] = x[j] - w b (b = x[j + n/2], w = pass l's twiddle q).
-// Three consecutive passes l, l+1, l+2 (2^(l+2) <= n/2) close over groups of eight: the inputs
+// Three consecutive general passes l, l+1, l+2 (l + 2 <= np - 2) close over groups of eight: the inputs
 // x[g + k n/8] (g < n/8, k = 0..7) of pass l feed butterflies c, c + 2^l, c + n/4, c + n/4 + 2^l
 // of pass l+1 (c = 2g - q), whose outputs are the inputs of butterflies B + t 2^l (t = 0..3,
 // B = 4m 2^l + q) of pass l+2, which write o + t 2^l and o + 4 2^l + t 2^l (o = 8m 2^l + q).
@@ -215,7 +215,7 @@ template <int BPT>
 __device__ __forceinline__ void fft_general_passes(float2* buf, const float2* __restrict__ tw, int np, int half,
                                                    int tid, int NT) {
     int l = 1;
-    if (BPT >= 4) {   // (smaller rows keep every thread busy with pairs)
+    if (BPT >= 4) {   // rows of n >= 8 x threads; smaller rows keep every thread busy with pairs
         constexpr int G = BPT >= 4 ? BPT / 4 : 1;   // groups of eight per thread
         const int eighth = half >> 2;
         for (; l + 2 < np - 1; l += 3) {
