@@ -11,8 +11,12 @@
 // an FMA; the REF outputs are therefore bit-identical to the reference CPU routine.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
+
+#include <atomic>
+#include <vector>
 
 #include "rv_internal.h"
 
@@ -72,10 +76,37 @@ __device__ __forceinline__ short norm_fast(int raw, int f0, int f1, int dark, fl
     *recheck = true;
     return 0;
 }
-// a sample that norm_fast flagged (so dinc > 0 and s >= pixmin): the reference's FP64 value
+// Boundaries of the flagged samples: w = 3000 ln(I0 / S) + 0.5 crosses the integer n exactly
+// where I0 = S exp((n - 0.5) / 3000).  g_exp_bound[n - kExpMin] holds that exponential as an
+// unevaluated float pair (hi + lo, about 2^-48 relative), filled once per device from the host's
+// double exp; g_exp_ready says it is filled (the recheck takes FP64 until then).
+constexpr int kExpMin = -30000, kExpMax = 34000, kExpReady = 0x45787042;
+__device__ float2 g_exp_bound[kExpMax - kExpMin + 1];
+__device__ int g_exp_ready;
+
+// a sample that norm_fast flagged (so dinc > 0 and s >= pixmin): the reference's value.
+// Its w lies within norm_fast's band of n = rint(fl(3000 L) + 0.5), so it truncates to n or to
+// the neighbour towards zero, decided by the sign of D = I0 - S exp((n - 0.5)/3000): S hi is
+// split exactly by one FMA, I0 - S hi is exact (the two agree to 1e-4), and the rest of D is off
+// by at most ~2e-12 I0.  |D| > 1e-9 I0 (3e-6 in w, far beyond the reference's own double
+// rounding) decides; closer samples, and n outside the table, take the FP64 formula.
 __device__ __forceinline__ short norm_exact(int raw, int f0, int f1, int dark, float t0) {
     const float dinc = norm_incident(f0, f1, dark, t0);
     const int s = raw - dark;
+    if (*(volatile int*)&g_exp_ready == kExpReady) {
+        const float L = logf(__fdiv_rn(dinc, (float)s));
+        const int n = __float2int_rn(rintf(__fadd_rn(__fmul_rn(L, 3000.0f), 0.5f)));
+        if (n == 0) return 0;
+        if (n >= kExpMin && n <= kExpMax) {
+            const float2 E = g_exp_bound[n - kExpMin];
+            const float sf = (float)s;
+            const float ph = __fmul_rn(sf, E.x);
+            const float pl = __fmaf_rn(sf, E.x, -ph);   // S hi = ph + pl exactly
+            const float D = __fsub_rn(__fsub_rn(__fsub_rn(dinc, ph), pl), __fmul_rn(sf, E.y));
+            if (fabsf(D) > __fmul_rn(dinc, 1e-9f))     // w > n  <=>  D > 0
+                return (short)(n > 0 ? (D > 0.0f ? n : n - 1) : (D > 0.0f ? n + 1 : n));
+        }
+    }
     const double vd = __dadd_rn(__dmul_rn(log(__ddiv_rn((double)dinc, (double)s)), 3000.0), 0.5);
     return (short)__double2int_rz(vd);
 }
@@ -180,7 +211,28 @@ __global__ void k_normalise(NormLaunch p) {
     normalise_row(r, f0, f1, dk, W, sh, job.zero != 0, job.t0, p.pixmin, p.zernike, out, sm_norm + 1, sm_norm);
 }
 
+// fills g_exp_bound once per device, outside stream capture (a capture leaves it for a later
+// call; until then the recheck uses FP64, with the same results)
+static void ensure_exp_bound(cudaStream_t s) {
+    static std::atomic<int> done[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev].load()) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    std::vector<float2> t(kExpMax - kExpMin + 1);
+    for (int n = kExpMin; n <= kExpMax; n++) {
+        const double e = exp((n - 0.5) / 3000.0);
+        const float hi = (float)e;
+        t[n - kExpMin] = make_float2(hi, (float)(e - (double)hi));
+    }
+    const int ready = kExpReady;
+    if (cudaMemcpyToSymbol(g_exp_bound, t.data(), t.size() * sizeof(float2)) == cudaSuccess &&
+        cudaMemcpyToSymbol(g_exp_ready, &ready, sizeof(int)) == cudaSuccess)
+        done[dev].store(1);
+}
+
 cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
+    ensure_exp_bound(s);
     if (p.njobs <= 0) return cudaSuccess;
     const size_t smem = p.row_ptr ? (((size_t)p.ixdim + 4) & ~(size_t)3) * sizeof(int) + (((size_t)p.ixdim * 2 + 15) & ~(size_t)15)
                                   : ((size_t)p.ixdim + 1) * sizeof(int);
@@ -517,6 +569,7 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
 
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {
     if (p.njobs <= 0) return cudaSuccess;
+    if (p.raw) ensure_exp_bound(s);
     const int n = p.d.ndim, half = n / 2;
     const int nt = half < 512 ? half : 512;
     const int bpt = half / nt;
