@@ -343,7 +343,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         a = filt_bytes / (filt_ms * 1e-3) / 1e9
         roof_filter = {"bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
                        "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
-                       "note": "HBM is not this kernel's binding resource: its radix-2 passes are shared-memory bound"}
+                       "note": "HBM is not this kernel's binding resource: its time goes to latency (each row's loads and recheck, the barriers between transform passes)"}
 
     if rank == 0:
         line = {
