@@ -211,8 +211,10 @@ __global__ void k_normalise(NormLaunch p) {
     normalise_row(r, f0, f1, dk, W, sh, job.zero != 0, job.t0, p.pixmin, p.zernike, out, sm_norm + 1, sm_norm);
 }
 
-// fills g_exp_bound once per device, outside stream capture (a capture leaves it for a later
-// call; until then the recheck uses FP64, with the same results)
+// fills g_exp_bound once per device with two synchronous copies (512 KB), outside stream capture
+// (a launch inside a capture leaves it for a later call; until then the recheck uses FP64, with
+// the same results).  A caller that captures in cudaStreamCaptureModeGlobal on another thread
+// should make one normalising call first.
 static void ensure_exp_bound(cudaStream_t s) {
     static std::atomic<int> done[64];
     int dev = 0;
