@@ -377,11 +377,12 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         if not args.no_cpu and world == 1:
             raw_c, bInc_c, fdeg_c, fexp_c, center_c = host_slice_data(args.seed)
             threads = os.cpu_count() or 1
-            tcpu = cpu_one_slice(raw_c, bInc_c, fdeg_c, fexp_c, center_c, F, threads, False)
+            runs = [cpu_one_slice(raw_c, bInc_c, fdeg_c, fexp_c, center_c, F, threads, False) for _ in range(3)]
+            tcpu = float(np.median(runs))
             tau_cpu = tcpu * 1e9 / (W_DET * W_DET * N_VIEWS)
             line["cpu_baseline"] = {"value": tau_cpu, "unit": "ns/(pixel*view)", "cores": threads, "kind": "port",
                                     "sample": "1 of 64 slices (2048^2 x 1800 views, normalisation + FBP), "
-                                              "reference multi-worker scheme", "seconds": tcpu}
+                                              "reference multi-worker scheme, median of 3 runs", "seconds": tcpu}
         if not args.no_forms and world == 1 and mode == abi.MODE_REF:
             line["forms"] = forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev)
             line["queue"] = queue_summary(dev, args.seed)
