@@ -16,6 +16,9 @@ slices inside the timed region).  The CPU baseline is the oracle restatement of 
 CPU routine (bit-identical to it) with the reference's multi-worker scheme on all host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--slices S]
+
+nvidia-smi clock samples taken during the timed region are summarised in the line (`clocks`);
+the raw samples go to RV_BENCH_LOG_DIR (default: the system's temporary directory).
 """
 from __future__ import annotations
 
