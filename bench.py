@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-centre", action="store_true", help="skip the centre-search summary of the default run")
     ap.add_argument("--no-forms", action="store_true", help="skip the reduced-storage and queue summaries")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed output")
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--workload", default="fbp", choices=["fbp", "centre", "precision"],
                     help="fbp: the back-projection stack (default); centre: train the centre-proposal network "
@@ -78,19 +79,20 @@ def centre_of(seed: int) -> float:
     return (W_DET - 1) / 2.0 + rng.uniform(-10.0, 10.0)
 
 
-def make_stack_gpu(seed: int, nslices: int, device):
+def make_stack_gpu(seed: int, nslices: int, device, W: int = W_DET, V: int = N_VIEWS, n_spheres: int = 0):
     """Raw frames on the device: [nframes + 1, nslices, W] uint16 stored in an int16 tensor
-    (frame 0 flat, 1..V samples, V+1 flat, last = dark)."""
+    (frame 0 flat, 1..V samples, V+1 flat, last = dark).  40 ellipsoids, plus n_spheres small
+    high-contrast spheres (radius 1-4 px, attenuation U[0.5, 2]) across the slice heights."""
     import torch
     from recview_gb300 import phantom
     rng = np.random.default_rng(seed)
     ells3 = phantom.random_ellipsoids(rng, 40)
-    center = centre_of(seed)
-    V, W = N_VIEWS, W_DET
+    center = (W - 1) / 2.0 + np.random.default_rng(seed).uniform(-10.0, 10.0)
     fdeg_s = phantom.angle_table(V)
     theta = torch.tensor(np.deg2rad(fdeg_s.astype(np.float64)), device=device)[:, None]
     t = torch.tensor(phantom.detector_coords(W, center), device=device)[None, :]
-    ys = (np.arange(nslices) - (nslices - 1) / 2.0) / (max(nslices, 2) / 2.0) * 0.5
+    ys = phantom.slice_heights(nslices)
+    spheres = phantom.random_spheres(rng, n_spheres, W, ys) if n_spheres else np.zeros((0, 5))
     gen = torch.Generator(device=device).manual_seed(seed)
     dark = 100.0 + 3.0 * torch.randn(nslices, W, device=device, generator=gen, dtype=torch.float64)
     flat = torch.tensor(20000.0 * (1.0 + 0.02 * phantom.smooth_noise(rng, (nslices, W), 16.0)), device=device)
@@ -103,7 +105,8 @@ def make_stack_gpu(seed: int, nslices: int, device):
 
     for s, y in enumerate(ys):
         p = torch.zeros((V, W), dtype=torch.float64, device=device)
-        for x0, z0, a, b, phi, mu in phantom.ellipsoid_slice(ells3, y):
+        discs = np.concatenate([phantom.ellipsoid_slice(ells3, y), phantom.sphere_slice(spheres, y)], axis=0)
+        for x0, z0, a, b, phi, mu in discs:
             sft = x0 * torch.cos(theta) + z0 * torch.sin(theta)
             d = theta - phi
             a2 = (a * torch.cos(d)) ** 2 + (b * torch.sin(d)) ** 2
@@ -206,6 +209,89 @@ def cpu_one_slice(raw_slice: np.ndarray, bInc, fdeg, fexp, center, F, threads: i
     return time.perf_counter() - t0
 
 
+def oracle_slice(raw_slice: np.ndarray, bInc, fdeg, fexp, center, F, threads: int, interp: int = 2,
+                 ref: bool = True, lin64: bool = False):
+    """The oracle on one detector row of raw frames ([nframes + 1, W] uint16 bits):
+    GenerateSinogramThread, then the reference's CPU FBP (int32, the bit-exact target) and/or
+    the FP64 end-to-end reconstruction (linear interpolation, double accumulation)."""
+    from recview_gb300.reconst import ReconInfo
+    from tests.rvtest import Oracle
+    oracle = Oracle()
+    r = np.ascontiguousarray(raw_slice).view(np.int16).copy()
+    ri = ReconInfo(r, fdeg, bInc, center=0, fexp=fexp, iMultiplex=1, maxSinogrLen=r.shape[0])
+    oracle.generate_sinogram(ri)
+    rs = ReconInfo(r, fdeg, bInc, center=center, fFilter=F, iInterpolation=interp, maxSinogrLen=r.shape[0],
+                   nviews=r.shape[0] - 1)
+    want = oracle.reconstruct(rs, threads=threads).copy() if ref else None
+    ref64 = oracle.lin64(rs, threads=threads) if lin64 else None
+    return want, ref64
+
+
+def circle_mask(n: int) -> np.ndarray:
+    yy, xx = np.mgrid[:n, :n]
+    return (xx - n / 2) ** 2 + (yy - n / 2) ** 2 < (0.45 * n) ** 2
+
+
+def error_vs_fp64(got: np.ndarray, ref64: np.ndarray) -> dict:
+    """Relative L2 and max-abs error inside the reconstruction circle (r < 0.45 of the width)."""
+    m = circle_mask(ref64.shape[0])
+    a = np.asarray(got, np.float64)[m]
+    b = ref64[m]
+    d = a - b
+    return {"rel_l2_vs_fp64": float(np.linalg.norm(d) / max(np.linalg.norm(b), 1e-300)),
+            "max_abs_vs_fp64": float(np.abs(d).max()), "max_abs_fp64": float(np.abs(b).max())}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+SCALAR_NOTE = ("the reference's scalar C back-projection loop (source/general.cpp:2147-2158); its MASM SIMD "
+               "loops (source/projx64.asm) are x64-only and cannot run on this Arm host")
+
+
+def cpu_other_configs(seed: int, threads: int, dev) -> dict:
+    """The CPU routine on the other configurations' shapes, one slice each, same host threads:
+    the 512-pixel x 900-view single slice (int16 sinogram, FBP only) and one 4096 x 3600 slice of
+    the precision study (raw frames: normalisation + FBP)."""
+    from recview_gb300 import abi, phantom
+    from recview_gb300.reconst import ReconInfo, dims
+    from tests.rvtest import Oracle
+    oracle = Oracle()
+    res = {}
+    sino, fdeg1 = phantom.sinogram_2d(seed, 512, 900, 255.5)
+    F1 = oracle.set_filter(abi.FILT_SHEPP, dims(512).ndim)
+    ri = ReconInfo(sino, fdeg1, np.ones(900, np.int8), center=255.5, fFilter=F1)
+    oracle.reconstruct(ri, threads=threads)
+    t0 = time.perf_counter()
+    oracle.reconstruct(ri, threads=threads)
+    t = time.perf_counter() - t0
+    res["fbp-512det-900views-1slice"] = {"seconds": t, "tau_ns": t * 1e9 / (512.0 * 512 * 900)}
+    raw4, bInc4, fdeg4, fexp4, cen4 = make_stack_gpu(seed, 1, dev, W=4096, V=3600)
+    raw4h = raw4[:, 0, :].cpu().numpy()
+    del raw4
+    F4 = oracle.set_filter(abi.FILT_SHEPP, dims(4096).ndim)
+    t = cpu_one_slice(raw4h, bInc4, fdeg4, fexp4, cen4, F4, threads, False)
+    res["precision-4096det-3600views-1slice"] = {"seconds": t, "tau_ns": t * 1e9 / (4096.0 * 4096 * 3600),
+                                                 "includes": "normalisation + FBP"}
+    return res
+
+
 def abi_copy(ri):
     from recview_gb300 import abi
     x = abi.RECONST_INFO()
@@ -246,8 +332,10 @@ def run_reference(args, rank: int, world: int):
                    "slices_in_workload": N_SLICES, "filter": "shepp-logan", "l2": "inputs larger than L2"},
         "slices_per_s": 1.0 / t,
         "cpu_baseline": {"value": tau, "unit": "ns/(pixel*view)", "cores": threads, "kind": kind,
+                         "cpu_model": cpu_model(),
                          "sample": "1 slice of the workload per step (2048^2 x 1800 views, normalisation + FBP), "
-                                   "reference multi-worker scheme (row bands, every worker filters all views)"},
+                                   "reference multi-worker scheme (row bands, every worker filters all views); "
+                                   + SCALAR_NOTE},
         "e2e": {"value": tau, "unit": "ns/(pixel*view)", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -381,6 +469,25 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "roofline_filter": roof_filter,
             "clocks": clocks,
         }
+        ref64 = slice0 = None
+        if mode == abi.MODE_REF and not args.no_parity:
+            # what was timed, checked against the oracle after the timed region: the first and the
+            # last slice of the stack (the last one is the second half of a slice pair)
+            threads = os.cpu_count() or 1
+            checked = sorted({0, S - 1})
+            t0 = time.perf_counter()
+            mism = {}
+            for s_ in checked:
+                got = out[s_].cpu().numpy()
+                want, r64 = oracle_slice(raw[:, s_, :].cpu().numpy(), bInc, fdeg, fexp, center, F, threads,
+                                         lin64=(s_ == 0))
+                mism[s_] = int(np.count_nonzero(got != want))
+                if s_ == 0:
+                    ref64, slice0 = r64, got
+            line["parity"] = {"slices_checked": checked, "bit_exact": all(v == 0 for v in mism.values()),
+                              "mismatched_pixels": [mism[s_] for s_ in checked],
+                              "against": "oracle (reference CPU routine restated), np.array_equal on int32",
+                              "seconds": time.perf_counter() - t0}
         if not args.no_cpu and world == 1:
             raw_c, bInc_c, fdeg_c, fexp_c, center_c = host_slice_data(args.seed)
             threads = os.cpu_count() or 1
@@ -388,10 +495,13 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             tcpu = float(np.median(runs))
             tau_cpu = tcpu * 1e9 / (W_DET * W_DET * N_VIEWS)
             line["cpu_baseline"] = {"value": tau_cpu, "unit": "ns/(pixel*view)", "cores": threads, "kind": "port",
+                                    "cpu_model": cpu_model(),
                                     "sample": "1 of 64 slices (2048^2 x 1800 views, normalisation + FBP), "
-                                              "reference multi-worker scheme, median of 3 runs", "seconds": tcpu}
+                                              "reference multi-worker scheme, median of 3 runs; " + SCALAR_NOTE,
+                                    "seconds": tcpu,
+                                    "other_configs": cpu_other_configs(args.seed, threads, dev)}
         if not args.no_forms and world == 1 and mode == abi.MODE_REF:
-            line["forms"] = forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev)
+            line["forms"] = forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, ref64=ref64, ref_slice0=slice0)
             line["queue"] = queue_summary(dev, args.seed)
             line["dropin"] = dropin_summary(raw, bInc, fdeg, fexp, center, F)
         if not args.no_centre and world == 1 and NET_FILE.exists():
@@ -445,14 +555,19 @@ def dropin_summary(raw, bInc, fdeg, fexp, center, F, reps: int = 20) -> dict:
     return out
 
 
-def forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, steps: int = 3) -> dict:
+def forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, steps: int = 3, ref64=None, ref_slice0=None) -> dict:
     """The reduced-storage forms on the same stack: filtered rows stored as FP32 / FP16 / BF16
-    (per-row scale), linear interpolation and FP32 accumulation (their FP64-oracle errors are
-    asserted in tests/test_gpu_parity.py::test_stack_lin_modes_vs_fp64)."""
+    (per-row scale), linear interpolation and FP32 accumulation.  With ref64 (the FP64 end-to-end
+    oracle of slice 0) each form's slice 0 error is reported, and the REF drop-in's beside them."""
     import torch
     import recview_gb300 as rv
     from recview_gb300 import abi
     out = {}
+    if ref64 is not None and ref_slice0 is not None:
+        out["error_measure"] = ("slice 0 of the timed stack against the FP64 end-to-end oracle "
+                                "(rvo_reconstruct_lin64_mt: the same normalisation, FP64 FFT filter, linear "
+                                "interpolation, double accumulation), inside r < 0.45 of the width")
+        out["ref"] = {"note": "the bit-exact drop-in (timed as the main figure)", **error_vs_fp64(ref_slice0, ref64)}
     for name, mode in (("lin_fp32", abi.MODE_LIN), ("lin_fp16", abi.MODE_LIN_F16), ("lin_bf16", abi.MODE_LIN_BF16)):
         st = rv.Stack(ixdim=W_DET, nframes=raw.shape[0] - 1, nslices=S, center=center, bInc=bInc, fdeg=fdeg,
                       fexp=fexp, fFilter=F, mode=mode)
@@ -467,6 +582,8 @@ def forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, steps: int = 3) -> d
         ms = float(np.mean(tt))
         out[name] = {"tau_ns": ms * 1e6 / (float(st.ixdimp) ** 2 * st.nviews * S), "ms_per_step": ms,
                      "backprojection_ms": float(np.mean(tb))}
+        if ref64 is not None:
+            out[name].update(error_vs_fp64(o[0].cpu().numpy(), ref64))
         st.close()
         del o
     return out
@@ -525,6 +642,8 @@ def queue_summary(dev, seed: int) -> dict:
         qdev.append(L.RvQueueLastMs(q))
     upd = L.RvQueueUpdates(q)
     L.RvQueueDestroy(q)
+    torch.cuda.synchronize()
+    queue_out = [x[10].clone() for x in data]
     stacks = [rv.Stack(ixdim=W, nframes=V + 2, nslices=S, center=cen, bInc=binc, fdeg=fdeg, fexp=fexp, fFilter=F,
                        iInterpolation=interp) for (W, V, S, interp, cen, raw, binc, fdeg, fexp, F, out) in data]
     for st, x in zip(stacks, data):
@@ -539,10 +658,12 @@ def queue_summary(dev, seed: int) -> dict:
         sms.append((time.perf_counter() - t0) * 1e3)
     for st in stacks:
         st.close()
+    same = all(torch.equal(a, x[10]) for a, x in zip(queue_out, data))
     qm, sm = float(np.median(qms)), float(np.median(sms))
     return {"datasets": len(data), "shapes_W_V_S_zoom": [list(x[:3]) + [2 ** (x[3] - 2)] for x in data],
             "updates": upd, "queue_ms": qm, "queue_device_ms": float(np.median(qdev)), "queue_tau_ns": qm * 1e6 / upd,
             "one_stack_at_a_time_ms": sm, "speedup_vs_stacks": sm / qm, "autotuned_variant": chosen.value,
+            "bit_exact_vs_stacks": bool(same),
             "timing": "host wall clock of the whole run, median of 3, both sides"}
 
 
@@ -585,8 +706,13 @@ def centre_evaluate(net, n: int, rng) -> dict:
 
 
 def run_precision(args):
-    """Configuration C4 shapes: 4096-pixel detector x 3600 views, 32 slices of 4096^2; the REF
-    drop-in and the FP32 / FP16 / BF16 filtered-row forms on the same device-resident frames."""
+    """Precision study (4096-pixel detector x 3600 views, 32 slices of 4096^2; 40 ellipsoids plus
+    200 small high-contrast spheres): the REF drop-in and the FP32 / FP16 / BF16 filtered-row
+    forms on the same device-resident raw frames, each timed and each measured against the FP64
+    end-to-end oracle on one slice, in one run.
+
+        python bench.py --workload precision [--steps K] [--warmup W]
+    """
     import torch
     import recview_gb300 as rv
     from recview_gb300 import abi
@@ -594,19 +720,14 @@ def run_precision(args):
     build_lib()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(0)
-    L = rv.lib()
     W, V, S = 4096, 3600, 32
-    deg = (np.arange(V) * (180.0 / V)).astype(np.float32)
-    raw = torch.empty((V + 3, S, W), dtype=torch.int16, device=dev)
-    bInc = np.zeros(V + 2, np.int8)
-    fdeg = np.zeros(V + 2, np.float32)
-    fexp = np.zeros(V + 2, np.float32)
-    rng = np.random.default_rng(args.seed)
-    cen = (W - 1) / 2.0 + float(rng.uniform(-10, 10))
-    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
-    assert L.RvPhantomFrames(args.seed, W, S, fp(deg), V, cen, 40, C.c_void_p(raw.data_ptr()),
-                             C.c_void_p(bInc.ctypes.data), fp(fdeg), fp(fexp), None) == 0, rv.last_error()
+    raw, bInc, fdeg, fexp, cen = make_stack_gpu(args.seed, S, dev, W=W, V=V, n_spheres=200)
     F = rv.set_filter(abi.FILT_SHEPP, rv.dims(W).ndim)
+    es = S // 2   # the error slice: a middle row of the stack
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    want, ref64 = oracle_slice(raw[:, es, :].cpu().numpy(), bInc, fdeg, fexp, cen, F, threads, lin64=True)
+    oracle_s = time.perf_counter() - t0
     res = {}
     for name, mode in (("ref", abi.MODE_REF), ("lin_fp32", abi.MODE_LIN), ("lin_fp16", abi.MODE_LIN_F16),
                        ("lin_bf16", abi.MODE_LIN_BF16)):
@@ -625,16 +746,24 @@ def run_precision(args):
             tt.append(c)
         ms = float(np.mean(tt))
         upd = float(st.ixdimp) ** 2 * st.nviews * S
+        got = out[es].cpu().numpy()
         res[name] = {"tau_ns": ms * 1e6 / upd, "ms_per_step": ms, "filter_ms": float(np.mean(tf)),
-                     "backprojection_ms": float(np.mean(tb)), "updates_per_s": upd / (ms * 1e-3)}
+                     "backprojection_ms": float(np.mean(tb)), "updates_per_s": upd / (ms * 1e-3),
+                     **error_vs_fp64(got, ref64)}
+        if mode == abi.MODE_REF:
+            res[name]["bit_exact_vs_reference_routine"] = bool(np.array_equal(got, want))
         st.close()
         del out
         torch.cuda.empty_cache()
     line = {"metric": "tau_ns_per_pixel_view", "value": res["ref"]["tau_ns"], "unit": "ns/(pixel*view)",
             "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "workload": "precision-4096det-3600views-32slices-raw-uint16", "data": "synthetic (seeded ellipsoid "
-            "phantom, Poisson uint16 frames)", "forms": res,
-            "errors": "FP64-oracle relative L2 per form: tests/test_gpu_parity.py and the design notes"}
+            "workload": "precision-4096det-3600views-32slices-raw-uint16-200spheres",
+            "data": "synthetic (seeded: 40 ellipsoids + 200 spheres of radius 1-4 px, attenuation U[0.5, 2], "
+                    "Poisson uint16 frames)",
+            "forms": res,
+            "error_measure": f"slice {es} against the FP64 end-to-end oracle (rvo_reconstruct_lin64_mt), inside "
+                             "r < 0.45 of the width; relative L2 and max-abs",
+            "oracle_seconds": oracle_s, "oracle_threads": threads}
     print(json.dumps(line), flush=True)
 
 

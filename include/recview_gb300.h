@@ -255,13 +255,23 @@ typedef struct RvStackDesc {
     int iFlag;              /* RV_READTIF8bit selects the 8-bit sample threshold */
     int mode;               /* RV_MODE_* */
     int input_is_sinogram;  /* 1: raw already holds log-normalised int16 rows (skip R1) */
+    /* R2 strip assembly (source/gazoDoc.cpp:3000-3004,3318-3342), raw frames only.  iRawWidth = 0:
+     * the frames are already trimmed and binned (nslices rows of ixdim samples per frame).
+     * iRawWidth > 0: every frame holds nslices * bin detector rows of iRawWidth samples (bin = 4
+     * for iInterpolation 0, 2 for 1, else 1); the library shifts each row by iTrim samples and
+     * averages bin x bin blocks (integer mean, truncated) before the normalisation, and ixdim must
+     * be the reference's width ((iRawWidth - 2 iTrim) / bin, the trim applied only when
+     * 0 < iTrim < iRawWidth / 2).  iTrim outside [0, iRawWidth / 2) is RV_ERR_BAD_ARGUMENT. */
+    int iTrim;
+    int iRawWidth;
 } RvStackDesc;
 
 typedef struct RvStack RvStack;
 /* Validates the description, builds per-view geometry and allocates device buffers. */
 int RvStackCreate(const RvStackDesc* desc, RvStack** out);
 void RvStackDestroy(RvStack* st);
-/* Bytes of one output slice (ixdimp^2 * 4) and of the raw input ((nframes+1)*nslices*ixdim*2). */
+/* Bytes of one output slice (ixdimp^2 * 4) and of the raw input ((nframes+1)*nslices*ixdim*2,
+ * or (nframes+1)*nslices*bin*iRawWidth*2 when the library assembles the strips). */
 size_t RvStackSliceBytes(const RvStack* st);
 size_t RvStackInputBytes(const RvStack* st);
 int RvStackNumViews(const RvStack* st);    /* SAMPLE views that are back-projected */
@@ -287,12 +297,20 @@ int RvStackLastLaunchCount(const RvStack* st);
  * Scratch (tables, geometry, FFT twiddles) lives in a fixed 64 MiB __device__ array that every
  * GPU loading this library keeps until the process exits; a slice needing more (about
  * nviews * 64 * ixdimp bytes) is rejected with RV_ERR_UNSUPPORTED.  The first call on a device
- * resolves the array's device address on that device, so make it before any stream capture.
- * All calls share the array: calls that overlap on the GPU race.  Returns 0 or an RV_ERR_* code
- * after the slice is complete on `stream`. */
+ * resolves the array's device address on that device, so make it before any stream capture; the
+ * address is resolved again after the device's context has changed (a device reset, e.g.
+ * CudaReconstResourceFree(ri, true)).  All calls share the array: calls that overlap on the GPU
+ * race.  They also share the device's kernel-status word, so an overlapping call may report the
+ * other's bounded-wait time-out.  The call is synchronous: it returns 0 or an RV_ERR_* code after
+ * the slice is complete on `stream`. */
 int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ixdim, int iInterpolation,
                               double center, const float* fdeg, float fTiltAngle,
                               const float* fFilter, int* d_slice, void* stream);
+/* Diagnostic query for RvReconstructSliceNoAlloc (no counterpart in the reference): *resolved =
+ * the scratch address the entry point would use on the current device now, *fresh = a new
+ * cudaGetSymbolAddress of the array.  Host-only (no launch, copy or allocation); they are equal
+ * unless the address cache is wrong.  Returns 0 or an RV_ERR_* code. */
+int RvNoAllocScratchAddress(void** resolved, void** fresh);
 
 /* Validation mode: while enabled, the REF back-projection runs a bounds-checked variant that
  * skips and counts every table index falling outside the window staged in shared memory (the

@@ -14,12 +14,14 @@
 #   source/gazoDoc.cpp:4379-4627                  computational part of CGazoDoc::GetAxis
 #   source/general.cpp:1313-1470                  WriteTifMonochrome16 (16-bit TIFF writer)
 #   source/gazoDoc.cpp:2967-2978, 3535-3666        GetSinogramYdim + offset-CT stitching tail
+#   source/gazoDoc.cpp:3002-3004, 3318-3342        strip assembly: trim and bin x bin average
 #   oracle/ref_wrap/libm_pin.cpp                  correctly rounded cosf/sinf for the twiddles
 #
 # The extracted ranges are checked against SHA-256 sums so a different checkout fails loudly
 # instead of silently compiling the wrong lines.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+# The reference checkout: RECVIEW_REFERENCE, else the location this recipe was written for.
 SRC="${RECVIEW_REFERENCE:-/root/reference}/source"
 OUT="$HERE/_ref"
 if [ ! -d "$SRC" ]; then
@@ -46,6 +48,8 @@ check general.cpp 1313 1470 80bb671236c506c654d4f1f620d23d219fa28b59a121d4f25384
 check gazoDoc.cpp 4379 4627 fcf94fb4d8af6e867fe5ecef64c6d776047c3b5bea9ea73fa5fd83c00b407774
 check gazoDoc.cpp 2967 2978 d0d0a88882e1b0a605ad40cbe58e122756669c99033dbdf55af4b2aceb72b678
 check gazoDoc.cpp 3535 3666 20e3f0e0c127d19e8d899301a4ddfc030737579b554f0435a85014666a383e8b
+check gazoDoc.cpp 3002 3004 b1dd6f55c31e6bfe54ab82aa991d67f686cd3b7021d472f12f134efadb2bae65
+check gazoDoc.cpp 3318 3342 14859f870809e364a7d248be4ea7ffef60de97ccacf31d2285216b9bb517ab18
 
 CXX="${CXX:-g++}"
 # -ffp-contract=off: the reference's x64 build rounds every float operation separately.
@@ -67,6 +71,9 @@ cd "$OUT/obj"   # empty directory: quote includes of the piped units resolve via
 { cat "$HERE/ref_wrap/ofct_head.inc"; sed -n 2967,2978p "$SRC/gazoDoc.cpp"; cat "$HERE/ref_wrap/ofct_mid.inc"; \
   sed -n 3535,3666p "$SRC/gazoDoc.cpp"; cat "$HERE/ref_wrap/ofct_tail.inc"; } \
     | "$CXX" "${FLAGS[@]}" -x c++ -c - -o ofct.o
+{ cat "$HERE/ref_wrap/bin_head.inc"; sed -n 3002,3004p "$SRC/gazoDoc.cpp"; sed -n 3318,3342p "$SRC/gazoDoc.cpp"; \
+  cat "$HERE/ref_wrap/bin_tail.inc"; } \
+    | "$CXX" "${FLAGS[@]}" -x c++ -c - -o bin.o
 "$CXX" "${FLAGS[@]}" -fno-builtin -c "$HERE/ref_wrap/libm_pin.cpp" -o libm_pin.o
-"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o axis.o tif.o ofct.o libm_pin.o -lm
+"$CXX" -shared -o "$OUT/librvref.so" cfft.o ccmplx.o fbp.o sino.o filter.o axis.o tif.o ofct.o bin.o libm_pin.o -lm
 echo "build_ref: $OUT/librvref.so"

@@ -963,3 +963,33 @@ int rvo_offset_ct_stitch(const short* sino, long long sino_stride, short* of, lo
     }
     return 0;
 }
+
+/* ---------------------------------------------------------------- R2: strip assembly ------- */
+int rvo_bin_width(int ixFrm, int iTrim, int iInterpolation) {
+    /* source/gazoDoc.cpp:2987, 3002-3004 (iBinning from iInterpolation; the trim narrows the row
+     * only when 0 < iTrim < ixFrm / 2) */
+    const int bin = (iInterpolation == 0) ? 4 : ((iInterpolation == 1) ? 2 : 1);
+    if (iTrim < 0 || (iTrim > 0 && iTrim >= ixFrm / 2)) return -1;
+    int ixlen = ixFrm;
+    if (iTrim > 0) ixlen -= 2 * iTrim;
+    return ixlen / bin;
+}
+
+int rvo_bin_strip(const unsigned short* strip, int ixFrm, int iTrim, int iInterpolation, int iMultiplex,
+                  unsigned short* out, long long out_stride) {
+    /* source/gazoDoc.cpp:3318-3342: sample k of slice j = (sum over the bin x bin block of rows
+     * j*bin + iy, columns k*bin + ix + iTrim) / bin^2 in int arithmetic; bin 1 is a plain copy */
+    const int bin = (iInterpolation == 0) ? 4 : ((iInterpolation == 1) ? 2 : 1);
+    const int ixlen = rvo_bin_width(ixFrm, iTrim, iInterpolation);
+    if (ixlen < 0) return -1;
+    for (int j = 0; j < iMultiplex; j++) {
+        for (int k = 0; k < ixlen; k++) {
+            int isum = 0;
+            for (int iy = 0; iy < bin; iy++)
+                for (int ix = 0; ix < bin; ix++)
+                    isum += strip[(long long)(j * bin + iy) * ixFrm + k * bin + ix + iTrim];
+            out[j * out_stride + k] = (unsigned short)(isum / (bin * bin));
+        }
+    }
+    return ixlen;
+}

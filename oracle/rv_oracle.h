@@ -96,6 +96,16 @@ int rvo_offset_ct_stitch(const short* sino, long long sino_stride, short* of, lo
                          double center, double deltaCent, int iInterpolation, int iTrimWidth,
                          int iRawSinoXdim, int iXdim);
 
+/* R2: strip assembly of CGazoDoc::GenerateSinogram for one frame (source/gazoDoc.cpp:3000-3004,
+ * 3318-3342): strip = iMultiplex * bin detector rows of ixFrm uint16 samples (bin from
+ * iInterpolation: 0 -> 4, 1 -> 2, else 1); row j of out (out_stride samples apart) receives the
+ * trimmed width, each sample the integer mean (truncated) of its bin x bin block, shifted right by
+ * iTrim samples.  Returns the width ixlen, or -1 when iTrim is negative or not below ixFrm / 2
+ * (the reference then reads outside the row). */
+int rvo_bin_width(int ixFrm, int iTrim, int iInterpolation);
+int rvo_bin_strip(const unsigned short* strip, int ixFrm, int iTrim, int iInterpolation, int iMultiplex,
+                  unsigned short* out, long long out_stride);
+
 #ifdef __cplusplus
 }
 #endif

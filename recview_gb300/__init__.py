@@ -75,7 +75,8 @@ class Stack:
 
     def __init__(self, *, ixdim: int, nframes: int, nslices: int, center: float, bInc, fdeg, fexp,
                  fFilter, iInterpolation: int = 2, tilt: float = 0.0, mode: int = abi.MODE_REF,
-                 flags: int = 0, iFlag: int = 0, input_is_sinogram: bool = False):
+                 flags: int = 0, iFlag: int = 0, input_is_sinogram: bool = False, iTrim: int = 0,
+                 raw_width: int = 0):
         self._keep = [np.ascontiguousarray(bInc, dtype=np.int8), np.ascontiguousarray(fdeg, dtype=np.float32),
                       np.ascontiguousarray(fexp, dtype=np.float32), np.ascontiguousarray(fFilter, dtype=np.float32)]
         b, fd, fe, ff = self._keep
@@ -94,6 +95,8 @@ class Stack:
         desc.iFlag = iFlag
         desc.mode = mode
         desc.input_is_sinogram = 1 if input_is_sinogram else 0
+        desc.iTrim = iTrim
+        desc.iRawWidth = raw_width
         h = C.c_void_p()
         rc = lib().RvStackCreate(C.byref(desc), C.byref(h))
         if rc:

@@ -106,6 +106,8 @@ class RvStackDesc(C.Structure):
         ("iFlag", C.c_int),
         ("mode", C.c_int),
         ("input_is_sinogram", C.c_int),
+        ("iTrim", C.c_int),
+        ("iRawWidth", C.c_int),
     ]
 
 
@@ -248,6 +250,7 @@ PROTOTYPES = {
     "RvGetBackprojectionVariant": (C.c_int, [c_int_p, c_int_p]),
     "RvReconstructSliceNoAlloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, c_float_p,
                                             C.c_float, c_float_p, C.c_void_p, C.c_void_p]),
+    "RvNoAllocScratchAddress": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "RvOffsetCtDims": (C.c_int, [C.POINTER(RvOffsetCtDesc), c_int_p, c_int_p, c_int_p]),
     "RvOffsetCtReconCenter": (C.c_double, [C.POINTER(RvOffsetCtDesc), C.c_double]),
     "RvOffsetCtStitchDevice": (C.c_int, [C.POINTER(RvOffsetCtDesc), C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -92,13 +92,15 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_ref(force: bool = False) -> Path | None:
-    """Reference sources compiled by oracle/build_ref.sh; None when the checkout is absent."""
-    ref_src = Path(os.environ.get("RECVIEW_REFERENCE", "/root/reference")) / "source"
-    if not ref_src.is_dir():
-        return None
+    """Reference sources compiled by oracle/build_ref.sh (the recipe locates the reference
+    checkout; RECVIEW_REFERENCE overrides it); None when the checkout is absent."""
     if REF_LIB.exists() and not force:
         return REF_LIB
-    _run(["bash", str(ORACLE_DIR / "build_ref.sh")])
+    r = subprocess.run(["bash", str(ORACLE_DIR / "build_ref.sh")], capture_output=True, text=True)
+    if r.returncode == 3:       # the recipe found no reference checkout
+        return None
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle/build_ref.sh failed ({r.returncode})\n{r.stdout}\n{r.stderr}")
     return REF_LIB
 
 

@@ -1911,8 +1911,10 @@ long long ref_table_stride(int ixdimp, int fmt) {
     return 16LL * ixdimp;
 }
 
+// Validation mode: window violations counted by the checked kernels into a __device__ word,
+// whose address is resolved at each checked launch (so a device reset never leaves a stale one).
 static int g_checked = 0;
-static unsigned int* g_counter = nullptr;
+__device__ unsigned int g_window_violation_count = 0;
 static unsigned long long g_violations = 0;
 
 template <typename K>
@@ -2168,11 +2170,13 @@ cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
     BackprojLaunch p = pin;
     load_defaults();
     const int variant = g_variant;
-    const bool checked = g_checked && g_counter;
+    const bool checked = g_checked != 0;
+    unsigned int* counter = nullptr;
     if (checked) {
-        p.status_counter = g_counter;
-        cudaError_t e = cudaMemsetAsync(g_counter, 0, sizeof(unsigned int), s);
+        cudaError_t e = cudaGetSymbolAddress((void**)&counter, g_window_violation_count);
+        if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
         if (e != cudaSuccess) return e;
+        p.status_counter = counter;
     }
     cudaError_t e;
     if (p.table_fmt == kTabPair) e = dispatch_pair(p, s, checked, variant);
@@ -2180,7 +2184,7 @@ cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
     else e = dispatch_bp<0>(p, s, checked, variant);
     if (checked && e == cudaSuccess) {
         unsigned int v = 0;
-        e = cudaMemcpyAsync(&v, g_counter, sizeof(v), cudaMemcpyDeviceToHost, s);
+        e = cudaMemcpyAsync(&v, counter, sizeof(v), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         g_violations += v;
     }
@@ -2189,10 +2193,20 @@ cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
 
 unsigned int take_kernel_status(cudaStream_t s) {
     unsigned int v = 0, zero = 0;
-    if (cudaMemcpyFromSymbolAsync(&v, g_kernel_status, sizeof(v), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess) return 0;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return 0;
-    if (v) cudaMemcpyToSymbolAsync(g_kernel_status, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s);
+    if (cudaMemcpyFromSymbolAsync(&v, g_kernel_status, sizeof(v), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return kStatusUnreadable;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return kStatusUnreadable;
+    if (v) {
+        if (cudaMemcpyToSymbolAsync(g_kernel_status, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            v |= kStatusUnreadable;
+    }
     return v;
+}
+const char* kernel_status_text(unsigned int status) {
+    if (status & kStatusUnreadable) return "the kernel status word could not be read (copy or synchronisation failed)";
+    if (status & kStatusWaitRanOut) return "a bounded wait for a table copy ran out";
+    return "no error";
 }
 
 }  // namespace rv
@@ -2247,9 +2261,6 @@ extern "C" int RvTestBoundedWait(int log2_tries, double* elapsed_ms) {
 }
 
 extern "C" int RvSetCheckedBackprojection(int enable) {
-    if (enable && !rv::g_counter) {
-        if (cudaMalloc(&rv::g_counter, sizeof(unsigned int)) != cudaSuccess) return RV_ERR_DEVICE_OOM;
-    }
     rv::g_checked = enable ? 1 : 0;
     rv::g_violations = 0;
     return 0;

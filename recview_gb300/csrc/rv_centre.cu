@@ -369,9 +369,11 @@ extern "C" int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInte
             scores[c0 + b] = t;
         }
     }
-    if (!rc && take_kernel_status(0)) {
-        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
-        rc = RV_ERR_KERNEL_STATUS;
+    if (!rc) {
+        if (const unsigned ks = take_kernel_status(0)) {
+            set_error(RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
+            rc = RV_ERR_KERNEL_STATUS;
+        }
     }
     void* bufs[] = {d_rows, d_filt, d_tw, d_jobs, d_geom, d_tab, d_out, d_part};
     for (void* p : bufs)

@@ -36,6 +36,35 @@ static bool progress(RECONST_INFO* ri, int step, int i, int* cur) {
     return false;
 }
 
+// ---------------------------------------------------------------------------- contexts -------
+// The driver's cuCtxGetCurrent / cuCtxGetId, looked up through the runtime so the library needs
+// no link-time dependency on libcuda (it still loads on machines without a driver).
+typedef int (*PfnCtxGetCurrent)(void** ctx);
+typedef int (*PfnCtxGetId)(void* ctx, unsigned long long* id);
+
+unsigned long long current_context_id() {
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    });
+    if (!get_current || !get_id) return 0;
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    if (get_id(ctx, &id) != 0) return 0;   // e.g. the context was destroyed by a reset
+    return id;
+}
+
 // ---------------------------------------------------------------------------- geometry -------
 Dims make_dims(int ixdim, int iInterpolation) {
     // source/general.cpp:2021-2035 (same double log / pow arithmetic)
@@ -397,8 +426,8 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
         ri->iStatus = RECONST_INFO_ERROR;
         return;
     }
-    if (take_kernel_status(s)) {
-        fail(ri, RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+    if (const unsigned ks = take_kernel_status(s)) {
+        fail(ri, RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
         return;
     }
     publish_fields(ri, c);

@@ -19,6 +19,13 @@ inline bool cuda_ok(cudaError_t e, int code, const char* what) {
     return false;
 }
 
+// ---- per-context state ----------------------------------------------------------------------
+// Identifier of the CUDA context current on the calling thread: unique for the life of the
+// process, so a device reset (which destroys the context and every device address resolved in
+// it) always yields a new value.  0 when no live context is current or the driver cannot say.
+// Host-side caches of device addresses or one-time device fills are keyed by it.
+unsigned long long current_context_id();
+
 // ---- geometry ----------------------------------------------------------------------------
 struct Dims {
     int ixdim, iZooming, iIntpDim, ndimp, ndim, ixdimp, ixdimh, ihoffset;
@@ -70,6 +77,12 @@ struct FilterLaunch {
     int table_fmt;            // REF table format, see ref_table_fmt()
     const short* const* row_ptr;  // sinogram mode: if set, row j is row_ptr[job.src_row] (it may be
                                   // host memory the device reads directly) instead of src + j * ixdim
+    // raw mode, strip assembly (R2): logical row r (a RowJob row) is detector rows r * bin ..
+    // r * bin + bin - 1 of raw_stride samples each (0: ixdim), sample x of the logical row the
+    // truncated mean of the bin x bin block at columns raw_x0 + x * bin ..; bin <= 1: no binning
+    long long raw_stride;
+    int raw_x0;
+    int bin;
 };
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
 // 1 when kernels on the current device may read and write pageable host memory directly (the
@@ -139,8 +152,14 @@ inline int lin_pair_bytes(int mode) { return mode == RV_MODE_LIN ? 8 : 4; }
 enum { kTabInt16 = 0, kTabInt17 = 1, kTabPair = 2 };
 int ref_table_fmt();
 long long ref_table_stride(int ixdimp, int fmt);
-// status word written by kernels whose bounded waits ran out (0 = fine); read-and-clear
+// Status word written by kernels whose bounded waits ran out (0 = fine); read-and-clear after
+// synchronising stream s.  One word per device, shared by every call on it: a call whose work
+// overlaps another's on the GPU may take the other's report.  kStatusUnreadable is returned
+// when the word could not be read (a failed copy or synchronisation), never 0.
+constexpr unsigned kStatusWaitRanOut = 1u;
+constexpr unsigned kStatusUnreadable = 0x80000000u;
 unsigned int take_kernel_status(cudaStream_t s);
+const char* kernel_status_text(unsigned int status);
 
 // ---- normalisation (R1) written back as int16 rows ------------------------------------------
 struct NormLaunch {

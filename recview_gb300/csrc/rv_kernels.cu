@@ -180,6 +180,44 @@ __device__ __forceinline__ void normalise_row(const uint16_t* r, const uint16_t*
     __syncthreads();
 }
 
+// R2 strip assembly (source/gazoDoc.cpp:3318-3342): the integer mean, truncated, of the bin x bin
+// block of a raw strip that makes sample x of a binned row (row points at the block's first
+// detector row, already shifted by the trim).
+__device__ __forceinline__ int binned_sample(const uint16_t* row, long long stride, int bin, int x) {
+    const uint16_t* q = row + (long long)x * bin;
+    int sum = 0;
+    for (int iy = 0; iy < bin; iy++)
+        for (int ix = 0; ix < bin; ix++) sum += q[iy * stride + ix];
+    return sum / (bin * bin);
+}
+
+// normalise_row for raw frames that are binned on the fly: each of the four rows is a strip of
+// bin detector rows, `stride` samples apart; samples come from binned_sample.  Same decision rule
+// and deferred recheck as normalise_row (no drift shift, no Zernike form on this path).
+__device__ __forceinline__ void normalise_row_binned(const uint16_t* r, const uint16_t* f0, const uint16_t* f1,
+                                                     const uint16_t* dk, long long stride, int bin, int W, bool zero,
+                                                     float t0, int pixmin, short* out, int* relist, int* count) {
+    const int tid = threadIdx.x, NT = blockDim.x;
+    for (int x = tid; x < W; x += NT) {
+        short v = 0;
+        if (!zero) {
+            bool re;
+            v = norm_fast(binned_sample(r, stride, bin, x), binned_sample(f0, stride, bin, x),
+                          binned_sample(f1, stride, bin, x), binned_sample(dk, stride, bin, x), t0, pixmin, &re);
+            if (re) relist[atomicAdd(count, 1)] = x;
+        }
+        out[x] = v;
+    }
+    __syncthreads();
+    const int n = *count;
+    for (int i = tid; i < n; i += NT) {
+        const int x = relist[i];
+        out[x] = norm_exact(binned_sample(r, stride, bin, x), binned_sample(f0, stride, bin, x),
+                            binned_sample(f1, stride, bin, x), binned_sample(dk, stride, bin, x), t0);
+    }
+    __syncthreads();
+}
+
 __global__ void k_normalise(NormLaunch p) {
     extern __shared__ int sm_norm[];   // [0]: recheck count, [1 .. W]: flagged positions, then
                                        // (row-pointer mode) a copy of the sample row
@@ -216,9 +254,13 @@ __global__ void k_normalise(NormLaunch p) {
 // the same results).  A caller that captures in cudaStreamCaptureModeGlobal on another thread
 // should make one normalising call first.
 static void ensure_exp_bound(cudaStream_t s) {
-    static std::atomic<int> done[64];
+    // per device: the context the table was filled in (a device reset makes a new context whose
+    // copy of the table is empty again, so it is filled anew there)
+    static std::atomic<unsigned long long> done[64];
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev].load()) return;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    const unsigned long long ctx = current_context_id();
+    if (ctx != 0 && done[dev].load() == ctx) return;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
     std::vector<float2> t(kExpMax - kExpMin + 1);
@@ -230,7 +272,7 @@ static void ensure_exp_bound(cudaStream_t s) {
     const int ready = kExpReady;
     if (cudaMemcpyToSymbol(g_exp_bound, t.data(), t.size() * sizeof(float2)) == cudaSuccess &&
         cudaMemcpyToSymbol(g_exp_ready, &ready, sizeof(int)) == cudaSuccess)
-        done[dev].store(1);
+        done[dev].store(current_context_id());
 }
 
 cudaError_t launch_normalise(const NormLaunch& p, cudaStream_t s) {
@@ -403,10 +445,18 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
         __shared__ int s_nre;
         if (tid == 0) s_nre = 0;
         __syncthreads();
-        const uint16_t* base = static_cast<const uint16_t*>(p.src);
-        normalise_row(base + (size_t)job.src_row * W, base + (size_t)job.flat0_row * W,
-                      base + (size_t)job.flat1_row * W, base + (size_t)job.dark_row * W, W, 0, job.zero != 0, job.t0,
-                      p.pixmin, 0, strip, reinterpret_cast<int*>(buf), &s_nre);
+        const uint16_t* base = static_cast<const uint16_t*>(p.src) + p.raw_x0;
+        const long long rs = p.raw_stride > 0 ? p.raw_stride : W;
+        if (p.bin > 1) {
+            const long long lr = rs * p.bin;   // samples per logical (binned) row
+            normalise_row_binned(base + job.src_row * lr, base + job.flat0_row * lr, base + job.flat1_row * lr,
+                                 base + job.dark_row * lr, rs, p.bin, W, job.zero != 0, job.t0, p.pixmin, strip,
+                                 reinterpret_cast<int*>(buf), &s_nre);
+        } else {
+            normalise_row(base + (size_t)job.src_row * rs, base + (size_t)job.flat0_row * rs,
+                          base + (size_t)job.flat1_row * rs, base + (size_t)job.dark_row * rs, W, 0, job.zero != 0,
+                          job.t0, p.pixmin, 0, strip, reinterpret_cast<int*>(buf), &s_nre);
+        }
     } else {
         const short* r = p.row_ptr ? p.row_ptr[job.src_row] : static_cast<const short*>(p.src) + (size_t)job.src_row * W;
         for (int x = tid; x < W; x += NT) strip[x] = job.zero ? (short)0 : r[x];

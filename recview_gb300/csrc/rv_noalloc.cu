@@ -25,30 +25,42 @@ namespace rv {
 constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;   // 64 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of the array, resolved once per device with that device current (host code
-// cannot use the symbol's host-side stand-in as a device pointer).
+// Device address of the array, resolved with the device current (host code cannot use the
+// symbol's host-side stand-in as a device pointer).  It is resolved on the first call on a device
+// and again whenever the device's context has changed since: a device reset
+// (CudaReconstResourceFree(ri, true), or the caller's own cudaDeviceReset) destroys the context,
+// the module is loaded afresh in the next one, and the array may then sit at another address.
+// A cached address from the old context is never handed to a kernel.
 constexpr int kMaxDevices = 64;
-static void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+    void* ptr;
+    unsigned long long ctx;   // context the address was resolved in (0: unknown, always resolve)
+};
+static ScratchAddr g_scratch_addr[kMaxDevices] = {};
 static std::mutex g_scratch_mu;
 
 static void* scratch_for_current_device(int* code) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         *code = RV_ERR_SET_DEVICE;
+        set_error(RV_ERR_SET_DEVICE, "RvReconstructSliceNoAlloc: no usable current device");
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr) {
-            set_error(RV_ERR_LAUNCH, std::string("cudaGetSymbolAddress of the scratch array: ") + cudaGetErrorString(e));
-            *code = RV_ERR_LAUNCH;
-            return nullptr;
-        }
-        g_scratch_addr[dev] = ptr;
+    ScratchAddr& a = g_scratch_addr[dev];
+    const unsigned long long ctx = current_context_id();
+    if (a.ptr && ctx != 0 && a.ctx == ctx) return a.ptr;
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+        a.ptr = nullptr;
+        set_error(RV_ERR_LAUNCH, std::string("cudaGetSymbolAddress of the scratch array: ") + cudaGetErrorString(e));
+        *code = RV_ERR_LAUNCH;
+        return nullptr;
     }
-    return g_scratch_addr[dev];
+    a.ptr = ptr;
+    a.ctx = current_context_id();   // the resolution made the device's context current if it was not
+    return ptr;
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -139,9 +151,24 @@ extern "C" int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ix
     bl.table_fmt = pad;
     if (!cuda_ok(launch_backproject(bl, s), RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
     if (!cuda_ok(cudaStreamSynchronize(s), RV_ERR_LAUNCH, "no-alloc slice")) return RV_ERR_LAUNCH;
-    if (take_kernel_status(s)) {
-        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+    if (const unsigned ks = take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
         return RV_ERR_KERNEL_STATUS;
     }
+    return 0;
+}
+
+// The address RvReconstructSliceNoAlloc would hand its kernels on the current device now
+// (*resolved, by the same context-checked cache) and a fresh cudaGetSymbolAddress of the array
+// (*fresh).  Host-only: nothing is launched, copied or allocated.  Tests use it to show that a
+// device reset never leaves the entry point with an address from the destroyed context.
+extern "C" int RvNoAllocScratchAddress(void** resolved, void** fresh) {
+    if (!resolved || !fresh) return RV_ERR_BAD_ARGUMENT;
+    int code = 0;
+    *resolved = scratch_for_current_device(&code);
+    if (!*resolved) return code;
+    *fresh = nullptr;
+    if (!cuda_ok(cudaGetSymbolAddress(fresh, g_noalloc_scratch), RV_ERR_LAUNCH, "cudaGetSymbolAddress"))
+        return RV_ERR_LAUNCH;
     return 0;
 }

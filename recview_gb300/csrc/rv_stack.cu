@@ -68,6 +68,21 @@ static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_table
         set_error(RV_ERR_BAD_ARGUMENT, "RvStackCreate: invalid description");
         return RV_ERR_BAD_ARGUMENT;
     }
+    if (desc->iRawWidth != 0) {
+        // R2: source/gazoDoc.cpp:2987 (bin from iInterpolation), 3002-3004 (width)
+        const int bin = desc->iInterpolation == 0 ? 4 : (desc->iInterpolation == 1 ? 2 : 1);
+        const int F = desc->iRawWidth, T = desc->iTrim;
+        const int want = (T >= 0 && (T == 0 || T < F / 2)) ? (F - (T > 0 ? 2 * T : 0)) / bin : -1;
+        if (desc->input_is_sinogram || F < 0 || want < 0 || want != desc->ixdim) {
+            set_error(RV_ERR_BAD_ARGUMENT, "RvStackCreate: iRawWidth/iTrim/binning do not give ixdim (width " +
+                                               std::to_string(want) + ", ixdim " + std::to_string(desc->ixdim) +
+                                               "), or the input is a sinogram");
+            return RV_ERR_BAD_ARGUMENT;
+        }
+    } else if (desc->iTrim != 0) {
+        set_error(RV_ERR_BAD_ARGUMENT, "RvStackCreate: iTrim needs iRawWidth (the untrimmed frame width)");
+        return RV_ERR_BAD_ARGUMENT;
+    }
     RvStack* st = new RvStack();
     st->desc = *desc;
     st->d = make_dims(desc->ixdim, desc->iInterpolation);
@@ -216,8 +231,23 @@ extern "C" void RvStackDestroy(RvStack* st) {
 extern "C" size_t RvStackSliceBytes(const RvStack* st) {
     return st ? (size_t)st->d.ixdimp * st->d.ixdimp * 4 : 0;
 }
+// raw samples per logical row (one slice of one frame): ixdim, or bin detector rows of the
+// untrimmed width when the library assembles the strips
+static long long raw_row_samples(const RvStack* st) {
+    if (st->desc.iRawWidth <= 0) return st->desc.ixdim;
+    const int bin = st->desc.iInterpolation == 0 ? 4 : (st->desc.iInterpolation == 1 ? 2 : 1);
+    return (long long)bin * st->desc.iRawWidth;
+}
+// the filter's view of the raw layout (R2 strip assembly)
+static void set_raw_layout(const RvStack* st, FilterLaunch& fl) {
+    if (st->desc.iRawWidth <= 0) return;
+    fl.raw_stride = st->desc.iRawWidth;
+    fl.raw_x0 = st->desc.iTrim;
+    fl.bin = st->desc.iInterpolation == 0 ? 4 : (st->desc.iInterpolation == 1 ? 2 : 1);
+}
+
 extern "C" size_t RvStackInputBytes(const RvStack* st) {
-    return st ? (size_t)(st->desc.nframes + 1) * st->desc.nslices * st->desc.ixdim * 2 : 0;
+    return st ? (size_t)(st->desc.nframes + 1) * st->desc.nslices * raw_row_samples(st) * 2 : 0;
 }
 extern "C" int RvStackNumViews(const RvStack* st) { return st ? st->nviews : 0; }
 extern "C" int RvStackOutputDim(const RvStack* st) { return st ? st->d.ixdimp : 0; }
@@ -233,6 +263,7 @@ static int run_slices(RvStack* st, const void* d_raw, void* d_out, int s0, int n
     FilterLaunch fl{};
     fl.src = d_raw;
     fl.raw = st->desc.input_is_sinogram ? 0 : 1;
+    set_raw_layout(st, fl);
     fl.pixmin = (st->desc.iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit : RV_SINOGRAM_PIXEL_MIN16bit;
     fl.jobs = static_cast<const RowJob*>(st->d_jobs) + (size_t)s0 * V;
     fl.njobs = nb * V;
@@ -309,8 +340,8 @@ extern "C" int RvStackRunDevice(RvStack* st, const void* d_raw, void* d_out, voi
     cudaEventRecord(st->ev[5], s);
     cudaError_t e = cudaEventSynchronize(st->ev[5]);
     if (!cuda_ok(e, RV_ERR_LAUNCH, "stack run")) return RV_ERR_LAUNCH;
-    if (take_kernel_status(s)) {
-        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+    if (const unsigned ks = take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
         return RV_ERR_KERNEL_STATUS;
     }
     float tt = 0;
@@ -370,7 +401,8 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
         return RV_ERR_BAD_ARGUMENT;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    const int S = st->desc.nslices, W = st->desc.ixdim, nfr = st->desc.nframes + 1;
+    const int S = st->desc.nslices, nfr = st->desc.nframes + 1;
+    const size_t W = (size_t)raw_row_samples(st);   // raw samples per slice of a frame
     const size_t in_b = RvStackInputBytes(st);
     const size_t slice_b = RvStackSliceBytes(st);
     int rc = ensure_host_buffers(st, in_b, slice_b * S);
@@ -421,8 +453,8 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
     cudaStreamWaitEvent(s, E[5 * (size_t)npieces], 0);
     cudaEventRecord(end, s);
     if (!cuda_ok(cudaEventSynchronize(end), RV_ERR_COPY_D2H, "stack run")) return RV_ERR_COPY_D2H;
-    if (take_kernel_status(s)) {
-        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+    if (const unsigned ks = take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
         return RV_ERR_KERNEL_STATUS;
     }
     float tf = 0, tb = 0, tt = 0;
@@ -586,6 +618,7 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
             FilterLaunch fl{};
             fl.src = q->items[pt.item].d_raw;
             fl.raw = st->desc.input_is_sinogram ? 0 : 1;
+            set_raw_layout(st, fl);
             fl.pixmin = (st->desc.iFlag & RV_READTIF8bit) ? RV_SINOGRAM_PIXEL_MIN8bit : RV_SINOGRAM_PIXEL_MIN16bit;
             fl.njobs = (pt.s1 - pt.s0) * V;
             fl.filt = static_cast<const float*>(st->d_filt);
@@ -695,8 +728,8 @@ extern "C" int RvQueueRun(RvQueue* q, void* stream) {
     cudaEventRecord(q->ev[1], s);
     if (!cuda_ok(cudaEventSynchronize(q->ev[1]), RV_ERR_LAUNCH, "queue run")) return RV_ERR_LAUNCH;
     cudaEventElapsedTime(&q->last_ms, q->ev[0], q->ev[1]);
-    if (take_kernel_status(s)) {
-        set_error(RV_ERR_KERNEL_STATUS, "back-projection: a bounded wait for a table copy ran out");
+    if (const unsigned ks = take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
         return RV_ERR_KERNEL_STATUS;
     }
     return 0;

@@ -47,6 +47,37 @@ def random_ellipsoids(rng: np.random.Generator, n: int) -> np.ndarray:
     return np.stack([x0, z0, y0, a, b, c, phi, mu], axis=1)
 
 
+def slice_heights(nslices: int) -> np.ndarray:
+    """Normalised heights y of the stack's detector rows: spread over [-0.25, 0.25]."""
+    return (np.arange(nslices) - (nslices - 1) / 2.0) / (max(nslices, 2) / 2.0) * 0.5
+
+
+def random_spheres(rng: np.random.Generator, n: int, ixdim: int, ys: np.ndarray) -> np.ndarray:
+    """[n, 5] = (x0, z0, y0, r, mu): small high-contrast spheres, radius U[1, 4] detector pixels,
+    attenuation U[0.5, 2] (the ellipsoids' units), centres uniform in a disk of radius 0.8 of the
+    slice plane.  Each sphere sits across one of the row heights ys (|y0 - y| < 0.9 r), so every
+    sphere cuts at least one reconstructed slice."""
+    half = ixdim / 2.0
+    r = rng.uniform(1.0, 4.0, n) / half
+    rho = 0.8 * np.sqrt(rng.uniform(0, 1, n))
+    ang = rng.uniform(0, 2 * np.pi, n)
+    y0 = np.asarray(ys, np.float64)[rng.integers(0, len(ys), n)] + rng.uniform(-0.9, 0.9, n) * r
+    mu = rng.uniform(0.5, 2.0, n)
+    return np.stack([rho * np.cos(ang), rho * np.sin(ang), y0, r, mu], axis=1)
+
+
+def sphere_slice(spheres: np.ndarray, y: float) -> np.ndarray:
+    """Cross-sections of spheres at height y as 2-D ellipses (discs)."""
+    out = []
+    for x0, z0, y0, r, mu in spheres:
+        h = r * r - (y - y0) ** 2
+        if h <= 0.0:
+            continue
+        rr = np.sqrt(h)
+        out.append((x0, z0, rr, rr, 0.0, mu))
+    return np.array(out, dtype=np.float64).reshape(-1, 6)
+
+
 def ellipsoid_slice(ells3: np.ndarray, y: float) -> np.ndarray:
     """Cross-sections of ellipsoids at height y (normalised) as 2-D ellipses."""
     out = []

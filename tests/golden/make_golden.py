@@ -51,6 +51,16 @@ OCT_CASES = [
 ]
 
 
+# (name, seed, raw frame width, trim, iInterpolation (0: bin 4, 1: bin 2, 2: none), slices)
+BIN_CASES = [
+    ("bin2_trim3", 41, 37, 3, 1, 2),
+    ("bin4_trim5", 42, 64, 5, 0, 3),
+    ("bin2_notrim", 43, 50, 0, 1, 1),
+    ("bin1_trim7", 44, 40, 7, 2, 2),
+    ("bin4_odd", 45, 45, 2, 0, 1),
+]
+
+
 def main() -> None:
     ref_path = build_ref()
     if ref_path is None:
@@ -172,6 +182,19 @@ def main() -> None:
         out[f"{name}_fdeg"] = fdeg
         out[f"{name}_params"] = np.array([F, 2 * F, interp, T, M, cen, dcent, rc])
         out[f"{name}_out"] = res
+    # strip assembly: trim and bin x bin averages of raw frames (CGazoDoc::GenerateSinogram)
+    from tests.rvtest import ref_bin_frames
+    Lr = C.CDLL(str(ref_path))
+    Lr.rvref_bin_strip.argtypes = [C.POINTER(C.c_short), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.POINTER(C.POINTER(C.c_short))]
+    for name, seed, F, T, interp, S in BIN_CASES:
+        rng = np.random.default_rng(seed)
+        B = 4 if interp == 0 else (2 if interp == 1 else 1)
+        frames = rng.integers(0, 65536, (3, S * B, F)).astype(np.uint16)
+        frames[0, :, :4] = 65535                      # sums near the top of the range
+        out[f"{name}_frames"] = frames
+        out[f"{name}_params"] = np.array([F, T, interp, S])
+        out[f"{name}_out"] = ref_bin_frames(Lr, frames, F, T, interp, S)
     dst = Path(__file__).with_name("golden.npz")
     np.savez_compressed(dst, **out)
     print(f"wrote {dst} ({dst.stat().st_size} bytes, {len(out)} arrays)")

@@ -55,6 +55,9 @@ class Oracle:
         L.rvo_tv_score.restype = C.c_double
         L.rvo_offset_ct_stitch.argtypes = OCT_ARGTYPES
         L.rvo_offset_ct_views.argtypes = [F32P, C.c_int]
+        L.rvo_bin_width.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.rvo_bin_strip.argtypes = [C.POINTER(C.c_ushort), C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.POINTER(C.c_ushort), C.c_longlong]
 
     def set_filter(self, kind, ndim, cutoff=0.5, order=2.0):
         t = np.zeros(ndim, np.float32)
@@ -113,6 +116,19 @@ class Oracle:
         return oct_call(self.L.rvo_offset_ct_stitch, rows, ixlen, bInc, fdeg, M, center, dcent, interp, trim, F,
                         iXdim if iXdim is not None else 2 * F, self.offset_ct_views(fdeg))
 
+    def bin_frames(self, frames: np.ndarray, ixFrm: int, iTrim: int, iInterpolation: int, S: int) -> np.ndarray:
+        """Strip assembly of every frame: frames[F, S * bin, ixFrm] uint16 -> [F, S, ixlen]."""
+        U16P = C.POINTER(C.c_ushort)
+        ixlen = self.L.rvo_bin_width(ixFrm, iTrim, iInterpolation)
+        assert ixlen > 0
+        frames = np.ascontiguousarray(frames, np.uint16)
+        out = np.zeros((frames.shape[0], S, ixlen), np.uint16)
+        for f in range(frames.shape[0]):
+            rc = self.L.rvo_bin_strip(frames[f].ctypes.data_as(U16P), ixFrm, iTrim, iInterpolation, S,
+                                      out[f].ctypes.data_as(U16P), ixlen)
+            assert rc == ixlen
+        return out
+
     def rescale(self, slice_, ixdimp, center_user, ipintp=1, ibinning=1):
         s = np.ascontiguousarray(slice_, np.int32).copy()
         imin, imax = C.c_int(), C.c_int()
@@ -135,7 +151,25 @@ def ref_lib():
                                  C.POINTER(C.c_double)]
     L.rvref_write_tif16.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int]
     L.rvref_offset_ct.argtypes = OCT_ARGTYPES
+    L.rvref_bin_strip.argtypes = [C.POINTER(C.c_short), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.POINTER(C.POINTER(C.c_short))]
     return L
+
+
+def ref_bin_frames(L, frames: np.ndarray, ixFrm: int, iTrim: int, iInterpolation: int, S: int) -> np.ndarray:
+    """The reference build's strip assembly (rvref_bin_strip) of every frame, into rows of the
+    width it returns: [F, S * bin, ixFrm] uint16 -> [F, S, ixlen]."""
+    B = 4 if iInterpolation == 0 else (2 if iInterpolation == 1 else 1)
+    frames = np.ascontiguousarray(frames, np.uint16)
+    nf = frames.shape[0]
+    rows = np.zeros((nf * S, ixFrm), np.int16)          # wide enough for any width
+    ptrs = (C.POINTER(C.c_short) * (nf * S))(*[rows[r].ctypes.data_as(C.POINTER(C.c_short)) for r in range(nf * S)])
+    ixlen = None
+    for f in range(nf):
+        n = L.rvref_bin_strip(frames[f].view(np.int16).ctypes.data_as(C.POINTER(C.c_short)), ixFrm, iTrim, B,
+                              0, S, f, ptrs)
+        ixlen = n
+    return rows[:, :ixlen].reshape(nf, S, ixlen).view(np.uint16).copy()
 
 
 def fbp_case(seed, W, V, center, interp=2, kind=abi.FILT_SHEPP, cutoff=0.5, flags=0, tilt=0.0,

@@ -83,3 +83,27 @@ def test_error_callback(rvlib):
     finally:
         rvlib.RvSetErrorCallback(abi.ErrorCallback())
     assert seen and seen[0][0] == abi.RV_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("ixdim,interp,trim,raw_width", [(100, 1, 50, 200),    # trim not below half the width
+                                                          (100, 1, -2, 200),    # negative trim
+                                                          (99, 1, 0, 200),      # width does not match
+                                                          (100, 2, 3, 0)])      # trim without the raw width
+def test_stack_rejects_inconsistent_strip_assembly(rvlib, ixdim, interp, trim, raw_width):
+    """RvStackCreate validates the strip-assembly fields before touching the device."""
+    V = 4
+    binc = np.ones(V + 1, np.int8)
+    binc[0] = 0
+    fdeg = np.zeros(V + 1, np.float32)
+    fexp = np.arange(V + 1, dtype=np.float32)
+    F = np.zeros(dims(max(ixdim, 4)).ndim, np.float32)
+    desc = abi.RvStackDesc()
+    desc.ixdim, desc.iInterpolation, desc.center, desc.nframes, desc.nslices = ixdim, interp, ixdim / 2, V + 1, 1
+    desc.bInc = C.cast(C.c_void_p(binc.ctypes.data), C.POINTER(C.c_char))
+    desc.fdeg = fdeg.ctypes.data_as(C.POINTER(C.c_float))
+    desc.fexp = fexp.ctypes.data_as(C.POINTER(C.c_float))
+    desc.fFilter = F.ctypes.data_as(C.POINTER(C.c_float))
+    desc.iTrim, desc.iRawWidth = trim, raw_width
+    h = C.c_void_p()
+    assert rvlib.RvStackCreate(C.byref(desc), C.byref(h)) == abi.RV_ERR_BAD_ARGUMENT
+    assert not h.value

@@ -84,3 +84,17 @@ def test_lin64_threads_equal_serial(oracle):
     from tests.rvtest import fbp_case
     ri = fbp_case(3, 96, 70, 47.3, oracle=oracle)
     assert np.array_equal(oracle.lin64(ri), oracle.lin64(ri, threads=3))
+
+
+@pytest.mark.parametrize("name", ["bin2_trim3", "bin4_trim5", "bin2_notrim", "bin1_trim7", "bin4_odd"])
+def test_strip_assembly(golden, oracle, name):
+    """Trim and bin x bin averaging of raw frames (CGazoDoc::GenerateSinogram's strip assembly)."""
+    F, T, interp, S = (int(v) for v in golden[f"{name}_params"])
+    got = oracle.bin_frames(golden[f"{name}_frames"], F, T, interp, S)
+    assert np.array_equal(got, golden[f"{name}_out"])
+
+
+def test_strip_assembly_rejects_bad_trim(oracle):
+    assert oracle.L.rvo_bin_width(40, 20, 1) == -1     # trim not below half the frame width
+    assert oracle.L.rvo_bin_width(40, -1, 2) == -1
+    assert oracle.L.rvo_bin_width(41, 3, 1) == (41 - 6) // 2

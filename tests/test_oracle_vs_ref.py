@@ -67,3 +67,16 @@ def test_get_axis_random(oracle, seed, W, S, V, cen, off):
                        C.byref(a), C.byref(b))
     got = oracle.get_axis(s0, s1, fl, off)
     assert (got[0], got[1]) == (a.value, b.value)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_strip_assembly_random(oracle, seed):
+    from tests.rvtest import ref_bin_frames
+    rng = np.random.default_rng(300 + seed)
+    interp = int(rng.choice([0, 1, 2, 3]))
+    B = 4 if interp == 0 else (2 if interp == 1 else 1)
+    F = int(rng.integers(8 * B, 90))
+    T = int(rng.choice([0, 0, 1, 2, 5])) if F > 12 else 0
+    S = int(rng.integers(1, 4))
+    frames = rng.integers(0, 65536, (4, S * B, F)).astype(np.uint16)
+    assert np.array_equal(oracle.bin_frames(frames, F, T, interp, S), ref_bin_frames(REF, frames, F, T, interp, S))
