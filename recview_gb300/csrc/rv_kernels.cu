@@ -547,7 +547,26 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
     const float inv_n = 1.0f / (float)n;
     const int ixdimp = p.d.ixdimp;
     const int rbase = n - 1 - p.d.ihoffset;  // q[j] = re[rbase - j] / n
-    if (p.table) {
+    if (p.table && p.table_fmt == kTabInt16) {
+        // dense 16-int table: thread t writes 16-byte group m = t, t + NT, ... (entries 4m .. 4m+3,
+        // pixel j = m / 4), so each warp store covers 512 contiguous bytes; the pixel's p0 and
+        // slope are formed per group with the same operations as below
+        int4* tab4 = reinterpret_cast<int4*>(p.table + (size_t)job.dst * p.table_stride);
+        for (int m = tid; m < 4 * ixdimp; m += NT) {
+            const int j = m >> 2, k0 = (m & 3) * 4;
+            const float qj = fmul(re[rbase - j], inv_n);
+            const float p0 = fmul(qj, 100.0f);
+            float p1p0 = 0.0f;
+            if (j != ixdimp - 1) {
+                const float qn = fmul(re[rbase - j - 1], inv_n);
+                p1p0 = fmul(fmul(fsub(qn, qj), 0.0625f), 100.0f);  // (q1-q0)/16*100
+            }
+            tab4[m] = make_int4(__float2int_rz(fadd(p0, fmul(p1p0, (float)k0))),
+                                __float2int_rz(fadd(p0, fmul(p1p0, (float)(k0 + 1)))),
+                                __float2int_rz(fadd(p0, fmul(p1p0, (float)(k0 + 2)))),
+                                __float2int_rz(fadd(p0, fmul(p1p0, (float)(k0 + 3)))));
+        }
+    } else if (p.table) {   // float pairs or the padded 17-word layout
         int* tab = p.table + (size_t)job.dst * p.table_stride;
         for (int j = tid; j < ixdimp; j += NT) {
             const float qj = fmul(re[rbase - j], inv_n);
@@ -561,21 +580,10 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
                 reinterpret_cast<float2*>(tab)[j] = make_float2(p0, p1p0);
                 continue;
             }
-            int v[16];
+            // 17 words per detector pixel (the 17th unused): shared-memory bank spreading
+            int* dst = tab + 17 * (size_t)j;
 #pragma unroll
-            for (int k = 0; k < 16; k++) v[k] = __float2int_rz(fadd(p0, fmul(p1p0, (float)k)));
-            if (p.table_fmt == kTabInt17) {
-                // 17 words per detector pixel (the 17th unused): shared-memory bank spreading
-                int* dst = tab + 17 * (size_t)j;
-#pragma unroll
-                for (int k = 0; k < 16; k++) dst[k] = v[k];
-            } else {
-                int4* dst = reinterpret_cast<int4*>(tab + 16 * (size_t)j);
-                dst[0] = make_int4(v[0], v[1], v[2], v[3]);
-                dst[1] = make_int4(v[4], v[5], v[6], v[7]);
-                dst[2] = make_int4(v[8], v[9], v[10], v[11]);
-                dst[3] = make_int4(v[12], v[13], v[14], v[15]);
-            }
+            for (int k = 0; k < 16; k++) dst[k] = __float2int_rz(fadd(p0, fmul(p1p0, (float)k)));
         }
         // pair tables are copied in 16-byte units: an odd row ends with a zero pair
         if (p.table_fmt == kTabPair && (ixdimp & 1) && tid == 0)
