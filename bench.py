@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the reduced-storage and queue summaries")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed output")
     ap.add_argument("--seed", type=int, default=2026)
-    ap.add_argument("--workload", default="fbp", choices=["fbp", "centre", "precision"],
+    ap.add_argument("--workload", default="fbp", choices=["fbp", "centre", "precision", "queue"],
                     help="fbp: the back-projection stack (default); centre: train the centre-proposal network "
                          "and compare the learned search with the full sweep")
     ap.add_argument("--datasets", type=int, default=200, help="centre: evaluation datasets")
@@ -431,13 +431,20 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm = peaks.get("hbm_gbs")
     nviews = st.nviews
-    # stage (a) bytes per row: raw uint16 row in + the 16-entry int table (64 B per detector pixel) out
-    filt_bytes = S * nviews * (2.0 * W_DET + 64.0 * st.ixdimp)
+    # stage (a) algorithmic bytes per sinogram sample: 2 B uint16 read + 4 B FP32 filtered value
+    # written (the row the back-projection interpolates); the REF path materialises that row as the
+    # reference's 16-entry int table (64 B per detector pixel), reported as traffic beside it
+    filt_bytes = S * nviews * (2.0 * W_DET + 4.0 * st.ixdimp)
+    table_bytes = S * nviews * (2.0 * W_DET + 64.0 * st.ixdimp)
     roof_filter = None
     if hbm and filt_ms > 0:
         a = filt_bytes / (filt_ms * 1e-3) / 1e9
         roof_filter = {"bound": "hbm", "achieved": a, "peak": hbm, "unit": "GB/s", "frac": a / hbm,
-                       "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                       "traffic": table_bytes if mode == abi.MODE_REF else None,
+                       "traffic_note": "raw rows in + the 16-entry int tables out (the REF back-projection's "
+                                       "gather format), bytes per step" if mode == abi.MODE_REF else None,
+                       "table_write_gbs": table_bytes / (filt_ms * 1e-3) / 1e9 if mode == abi.MODE_REF else None,
+                       "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
                        "note": "HBM is not this kernel's binding resource: its time goes to latency (each row's loads and recheck, the barriers between transform passes)"}
 
     if rank == 0:
@@ -767,6 +774,183 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
+def c3_draw(seed: int, n: int = 40) -> list[dict]:
+    """The uneven queue's datasets: detector width in {1024, 1536, 2048, 4096}, views in
+    {900, 1800, 3600}, 1-256 slices, rotation centre (W - 1) / 2 + U[-20, 20] px; every second
+    dataset is a zoomed region of interest: 1/4-1/2 of the field kept by trimming (iTrim) and
+    reconstructed at x2 or x4 (iInterpolation 3 / 4)."""
+    from recview_gb300.reconst import dims
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        W = int(rng.choice([1024, 1536, 2048, 4096]))
+        V = int(rng.choice([900, 1800, 3600]))
+        S = int(rng.integers(1, 257))
+        off = float(rng.uniform(-20.0, 20.0))
+        if i % 2:
+            frac = float(rng.uniform(0.25, 0.5))
+            interp = int(rng.choice([3, 4]))
+            T = int(round(W * (1.0 - frac) / 2.0))
+        else:
+            interp, T = 2, 0
+        ixlen = W - 2 * T
+        d = dims(ixlen, interp)
+        out.append(dict(W=W, V=V, S=S, cen_raw=(W - 1) / 2.0 + off, interp=interp, T=T, ixlen=ixlen, ixdimp=d.ixdimp,
+                        ndim=d.ndim, seed=seed * 1000 + i))
+    return out
+
+
+def run_queue(args):
+    """The uneven queue: 40 seeded datasets (c3_draw), raw uint16 frames at full detector width
+    on the device, the zoomed ones trimmed and zoomed by the library.  The datasets run in
+    batches that fit device memory; each batch runs as one queue (per-shape autotuned variants,
+    one captured graph, persistent back-projections) and, on the same buffers, one stack at a time
+    (RvStackRunDevice per dataset).  Outputs of the two are compared by checksums per dataset, and
+    slice 0 of two datasets against the oracle.
+
+        python bench.py --workload queue [--steps K] [--warmup W]
+    """
+    import torch
+    import recview_gb300 as rv
+    from recview_gb300 import abi
+    from recview_gb300.build import build_lib
+    build_lib()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    L = rv.lib()
+    specs = c3_draw(args.seed)
+    # one device-memory budget for the tables of the queue pool and of each stack (the stacks of
+    # a batch live side by side)
+    os.environ.setdefault("RV_TABLE_BUDGET_MB", "8192")
+    cap = float(os.environ.get("RV_QUEUE_BATCH_GB", "64")) * 1e9
+    batches, cur, size = [], [], 0.0
+    for i, d in enumerate(specs):
+        b = (d["V"] + 3) * d["S"] * d["W"] * 2 + d["S"] * d["ixdimp"] ** 2 * 4
+        if cur and size + b > cap:
+            batches.append(cur)
+            cur, size = [], 0.0
+        cur.append(i)
+        size += b
+    batches.append(cur)
+
+    def checksum(t):
+        # per slice: the sum and a position-weighted sum of the int32 values (in int64)
+        w = (torch.arange(t[0].numel(), device=t.device, dtype=torch.int64) % 65521) + 1
+        out = []
+        for sl in range(t.shape[0]):
+            x = t[sl].reshape(-1).long()
+            out.append((int(x.sum()), int((x * w).sum())))
+        return out
+
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    q_total = s_total = 0.0
+    upd_total = 0.0
+    same_all = True
+    variants, oracle_checks = {}, []
+    t_start = time.perf_counter()
+    for bi, idx in enumerate(batches):
+        data = []
+        for i in idx:
+            d = specs[i]
+            deg = (np.arange(d["V"]) * (180.0 / d["V"])).astype(np.float32)
+            raw = torch.empty((d["V"] + 3, d["S"], d["W"]), dtype=torch.int16, device=dev)
+            binc = np.zeros(d["V"] + 2, np.int8)
+            fdeg = np.zeros(d["V"] + 2, np.float32)
+            fexp = np.zeros(d["V"] + 2, np.float32)
+            assert L.RvPhantomFrames(d["seed"], d["W"], d["S"], fp(deg), d["V"], d["cen_raw"], 40,
+                                     C.c_void_p(raw.data_ptr()), C.c_void_p(binc.ctypes.data), fp(fdeg), fp(fexp),
+                                     None) == 0, rv.last_error()
+            F = rv.set_filter(abi.FILT_SHEPP, d["ndim"])
+            out = torch.empty((d["S"], d["ixdimp"], d["ixdimp"]), dtype=torch.int32, device=dev)
+            desc = abi.RvStackDesc()
+            desc.ixdim, desc.iInterpolation, desc.center = d["ixlen"], d["interp"], d["cen_raw"] - d["T"]
+            desc.nframes, desc.nslices = d["V"] + 2, d["S"]
+            desc.bInc = C.cast(C.c_void_p(binc.ctypes.data), C.POINTER(C.c_char))
+            desc.fdeg, desc.fexp, desc.fFilter = fp(fdeg), fp(fexp), fp(F)
+            desc.mode = abi.MODE_REF
+            if d["T"]:
+                desc.iTrim, desc.iRawWidth = d["T"], d["W"]
+            data.append(dict(i=i, raw=raw, out=out, desc=desc, keep=(binc, fdeg, fexp, F)))
+        torch.cuda.synchronize()
+        # ---- the queue: per-shape autotuning, graph capture, timed replays ----------------------
+        q = C.c_void_p()
+        assert L.RvQueueCreate(C.byref(q)) == 0
+        for x in data:
+            assert L.RvQueueAdd(q, C.byref(x["desc"]), C.c_void_p(x["raw"].data_ptr()),
+                                C.c_void_p(x["out"].data_ptr())) == 0, rv.last_error()
+        chosen = C.c_int(-1)
+        assert L.RvQueueAutotune(q, None, C.byref(chosen)) == 0, rv.last_error()
+        for k, x in enumerate(data):
+            variants[x["i"]] = L.RvQueueItemVariant(q, k)
+        assert L.RvQueueRun(q, None) == 0, rv.last_error()          # captures the graph
+        qt = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            assert L.RvQueueRun(q, None) == 0, rv.last_error()
+            qt.append(time.perf_counter() - t0)
+        upd_total += L.RvQueueUpdates(q)
+        L.RvQueueDestroy(q)
+        sums_q = [checksum(x["out"]) for x in data]
+        # ---- the same datasets one stack at a time ------------------------------------------------
+        stacks = []
+        for x in data:
+            h = C.c_void_p()
+            assert L.RvStackCreate(C.byref(x["desc"]), C.byref(h)) == 0, rv.last_error()
+            stacks.append(h)
+        for h, x in zip(stacks, data):
+            assert L.RvStackRunDevice(h, C.c_void_p(x["raw"].data_ptr()), C.c_void_p(x["out"].data_ptr()), None) == 0
+        st_t = []
+        for _ in range(max(1, args.steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for h, x in zip(stacks, data):
+                assert L.RvStackRunDevice(h, C.c_void_p(x["raw"].data_ptr()), C.c_void_p(x["out"].data_ptr()),
+                                          None) == 0, rv.last_error()
+            torch.cuda.synchronize()
+            st_t.append(time.perf_counter() - t0)
+        for h in stacks:
+            L.RvStackDestroy(h)
+        sums_s = [checksum(x["out"]) for x in data]
+        same_all &= sums_q == sums_s
+        q_total += float(np.median(qt))
+        s_total += float(np.median(st_t))
+        # ---- slice 0 of the smallest zoomed and unzoomed dataset of the first batch vs the oracle
+        if bi == 0:
+            from tests.rvtest import Oracle
+            oracle = Oracle()
+            for zoomed in (False, True):
+                cand = [x for x in data if (specs[x["i"]]["T"] > 0) == zoomed]
+                if not cand:
+                    continue
+                x = min(cand, key=lambda y: specs[y["i"]]["ixdimp"] ** 2 * specs[y["i"]]["V"])
+                d = specs[x["i"]]
+                frames = x["raw"][:, 0, :].cpu().numpy().view(np.uint16)
+                rows = oracle.bin_frames(frames[:, None, :], d["W"], d["T"], d["interp"], 1)[:, 0, :]
+                binc, fdeg, fexp, F = x["keep"]
+                want, _ = oracle_slice(rows, binc, fdeg, fexp, d["cen_raw"] - d["T"], F, os.cpu_count() or 1,
+                                       interp=d["interp"])
+                oracle_checks.append({"dataset": x["i"], "zoomed": zoomed,
+                                      "bit_exact": bool(np.array_equal(x["out"][0].cpu().numpy(), want))})
+        del data
+        torch.cuda.empty_cache()
+    line = {"metric": "tau_ns_per_pixel_view", "value": q_total * 1e9 / upd_total, "unit": "ns/(pixel*view)",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": 1,
+            "workload": "queue-40-datasets-uneven-width-views-slices-centre-zoomed-roi",
+            "data": "synthetic (seeded ellipsoid phantom frames at full detector width, Poisson uint16)",
+            "datasets": len(specs), "batches": len(batches),
+            "shapes_W_V_S_zoom_trim": [[d["W"], d["V"], d["S"], 2 ** max(d["interp"] - 2, 0), d["T"]] for d in specs],
+            "updates": upd_total, "queue_s": q_total, "one_stack_at_a_time_s": s_total,
+            "speedup_vs_stacks": s_total / q_total, "slices_per_s": sum(d["S"] for d in specs) / q_total,
+            "autotuned_variant_per_dataset": [variants[i] for i in range(len(specs))],
+            "outputs_equal_queue_vs_stacks": bool(same_all), "oracle_checks": oracle_checks,
+            "timing": "host wall clock per batch (each call returns after its work), median of the timed runs, summed "
+                      "over batches; autotuning and graph capture outside the timed runs",
+            "table_budget_mb": int(os.environ["RV_TABLE_BUDGET_MB"]),
+            "wall_s": time.perf_counter() - t_start}
+    print(json.dumps(line), flush=True)
+
+
 def run_centre(args):
     """Learned centre search vs the plain full sweep (configuration C5 shapes: 2048-pixel detector,
     1800 views, uint16 Poisson raw frames, true offset U[-40, 40] px)."""
@@ -832,6 +1016,9 @@ def main():
         return
     if args.workload == "precision":
         run_precision(args)
+        return
+    if args.workload == "queue":
+        run_queue(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
