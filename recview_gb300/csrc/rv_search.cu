@@ -3,14 +3,16 @@
 // grid centre (GetAxis's estimate), scored by RvCentreSweep's criterion; it picks the lowest score
 // and refines it with a parabola through its neighbours.  The learned search asks the network
 // (rv_cnn.cu) for a centre and its uncertainty, reconstructs the 2w+1 grid trials around it and
-// walks towards lower scores until the lowest score has evaluated neighbours on both sides.  It
-// runs the full sweep when the uncertainty is above sigma_max or the walk exceeds 5 (2w+1)
+// walks towards lower scores until the lowest score is confirmed over +-(w+1) grid steps; when
+// the grid centre lies outside the first 2w+1 trials, a second walk starts at the grid centre.
+// It runs the full sweep when the uncertainty is above sigma_max or the walks exceed 5 (2w+1)
 // trials (the criterion keeps disagreeing with the proposal).  Both paths pick the lowest
 // evaluated score with the same parabola, so the chosen centre equals the full sweep's whenever
 // the walk ends at the grid's lowest score; the final slice is always the plain reconstruction.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <chrono>
@@ -102,33 +104,56 @@ extern "C" int RvCentreSearch(RvCentreNet* net, const short* d_sino, int S, int 
     };
     bool full = !use_net;
     if (use_net) {
-        // start with 2*window+1 trials around the proposal and walk towards lower scores in steps of
-        // window+1 until the lowest score has evaluated neighbours on both sides
+        // A walk starts with 2*window+1 trials around k and moves towards lower scores in steps of
+        // window+1 until its lowest score m is confirmed: every grid point within window+1 of m
+        // evaluated and none lower (a shallow bump next to the basin does not stop it).  The first
+        // walk starts at the proposal; when the grid centre (GetAxis's estimate) lies outside the
+        // proposal's first 2*window+1 trials, a second walk starts there.  Both keep the trial cap.
+        const int cap = 5 * (2 * window + 1), conf = window + 1;
+        auto walk = [&](int kstart) -> int {
+            int lo = kstart - window, hi = kstart + window;
+            if (lo < -K) { hi += -K - lo; lo = -K; }
+            if (hi > K) { lo -= hi - K; hi = K; }
+            if (lo < -K) lo = -K;
+            int r = eval(lo, hi);
+            if (r) return r;
+            for (;;) {
+                int m = lo;
+                for (int k = lo + 1; k <= hi; k++)
+                    if (score[k + K] < score[m + K]) m = k;
+                if (m == lo && lo > -K) {
+                    const int nlo = lo - (window + 1) < -K ? -K : lo - (window + 1);
+                    if ((r = eval(nlo, lo - 1))) return r;
+                    lo = nlo;
+                } else if (m == hi && hi < K) {
+                    const int nhi = hi + window + 1 > K ? K : hi + window + 1;
+                    if ((r = eval(hi + 1, nhi))) return r;
+                    hi = nhi;
+                } else {
+                    // m has evaluated neighbours on both sides: confirm it over +-conf
+                    const int clo = m - conf < -K ? -K : m - conf, chi = m + conf > K ? K : m + conf;
+                    if (clo >= lo && chi <= hi) break;
+                    if (clo < lo) {
+                        if ((r = eval(clo, lo - 1))) return r;
+                        lo = clo;
+                    }
+                    if (chi > hi) {
+                        if ((r = eval(hi + 1, chi))) return r;
+                        hi = chi;
+                    }
+                    int m2 = lo;
+                    for (int k = lo + 1; k <= hi; k++)
+                        if (score[k + K] < score[m2 + K]) m2 = k;
+                    if (m2 == m) break;   // confirmed; otherwise keep walking from the lower point
+                }
+                if (out->trials > cap) { full = true; break; }   // the criterion keeps disagreeing
+            }
+            return 0;
+        };
         int kp = (int)floor((out->proposal - grid_centre) / step + 0.5);
         kp = kp < -K ? -K : (kp > K ? K : kp);
-        int lo = kp - window, hi = kp + window;
-        if (lo < -K) { hi += -K - lo; lo = -K; }
-        if (hi > K) { lo -= hi - K; hi = K; }
-        if (lo < -K) lo = -K;
-        if ((rc = eval(lo, hi))) return rc;
-        const int cap = 5 * (2 * window + 1);
-        for (;;) {
-            int m = lo;
-            for (int k = lo + 1; k <= hi; k++)
-                if (score[k + K] < score[m + K]) m = k;
-            if (m == lo && lo > -K) {
-                const int nlo = lo - (window + 1) < -K ? -K : lo - (window + 1);
-                if ((rc = eval(nlo, lo - 1))) return rc;
-                lo = nlo;
-            } else if (m == hi && hi < K) {
-                const int nhi = hi + window + 1 > K ? K : hi + window + 1;
-                if ((rc = eval(hi + 1, nhi))) return rc;
-                hi = nhi;
-            } else {
-                break;
-            }
-            if (out->trials > cap) { full = true; break; }   // the criterion keeps disagreeing
-        }
+        if ((rc = walk(kp))) return rc;
+        if (!full && abs(kp) > window && (rc = walk(0))) return rc;
     }
     if (full) {
         out->fallback = 1;
