@@ -352,12 +352,20 @@ int RvImageDescription(char* out, int cap, int nSinogr, double pixelWidth, float
  * wave as one filter launch per dataset plus one persistent back-projection kernel that takes
  * tiles of every dataset from a device work list, captures the whole sequence in a CUDA graph on
  * the first run and replays the graph afterwards.  REF mode only; results equal RvStackRunDevice's.
- * RvQueueAutotune (optional, before the first run) times the tile-shape variants of the
- * persistent kernel on this queue and keeps the fastest. */
+ * Each wave runs one persistent launch per back-projection variant in use.  RvQueueAutotune
+ * (optional, before the first run) tunes per shape class -- output size (ixdimp <= 1024 / 2048 /
+ * 4096 / more), view count (<= 1000 / 2000 / more), slice pairs possible or not: on 2-8 slices of
+ * one dataset of each class it times persistent variants that differ in pixel tile, views per
+ * staged chunk, slices per CTA and consumer warps, and keeps the fastest in a process-wide cache
+ * keyed by the class (datasets added later with a cached class use it).  *chosen_variant receives
+ * the first dataset's choice; RvQueueItemVariant gives any dataset's. */
 typedef struct RvQueue RvQueue;
 int RvQueueCreate(RvQueue** out);
 int RvQueueAdd(RvQueue* q, const RvStackDesc* desc, const void* d_raw, void* d_out);
 int RvQueueAutotune(RvQueue* q, void* stream, int* chosen_variant);
+int RvQueueItemVariant(const RvQueue* q, int item);   /* -1 for a bad index */
+/* Pins dataset `item` to a back-projection variant (0-20), overriding the tuned choice. */
+int RvQueueSetItemVariant(RvQueue* q, int item, int variant);
 int RvQueueRun(RvQueue* q, void* stream);
 float RvQueueLastMs(const RvQueue* q);        /* device time of the last run */
 double RvQueueUpdates(const RvQueue* q);      /* pixel-view updates of one run */
@@ -531,9 +539,11 @@ int RvCentreNetFit(RvCentreNet* net, const void* d_x, const float* d_y, int ntra
  * half_range (RvCentreSweep's criterion on detector row s_sweep of d_sino [nframes][S][W], the
  * SAMPLE frames of bInc at fdeg), narrowed by the network when net is not NULL: the network reads
  * rows s_net..s_net+3 (RvCentreNetInput, the proposal is (W-1)/2 + 16 mu with uncertainty
- * 16 e^(s/2) pixels) and only the 2*window+1 grid trials around the proposal are reconstructed.
- * The full sweep runs instead when the uncertainty exceeds sigma_max or the lowest score of the
- * window lies on its edge.  centre = the sweep criterion's choice (parabola-refined). */
+ * 16 e^(s/2) pixels) and the search starts with the 2*window+1 grid trials around the proposal,
+ * walking towards lower scores until the lowest is confirmed over +-(window+1) grid steps; a
+ * proposal more than window steps from grid_centre gets a second walk from grid_centre.  The full
+ * sweep runs instead when the uncertainty exceeds sigma_max or the walks exceed 5 (2*window+1)
+ * trials.  centre = the sweep criterion's choice (parabola-refined). */
 typedef struct RvCentreSearchResult {
     double centre;     /* chosen centre (ri->center convention) */
     double proposal;   /* network proposal (NaN without a network) */

@@ -243,6 +243,8 @@ PROTOTYPES = {
     "RvQueueAdd": (C.c_int, [C.c_void_p, C.POINTER(RvStackDesc), C.c_void_p, C.c_void_p]),
     "RvQueueAutotune": (C.c_int, [C.c_void_p, C.c_void_p, c_int_p]),
     "RvQueueRun": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "RvQueueItemVariant": (C.c_int, [C.c_void_p, C.c_int]),
+    "RvQueueSetItemVariant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "RvQueueLastMs": (C.c_float, [C.c_void_p]),
     "RvQueueUpdates": (C.c_double, [C.c_void_p]),
     "RvQueueDestroy": (None, [C.c_void_p]),

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "rv_internal.h"
 
@@ -759,6 +760,15 @@ __device__ __forceinline__ int ray_regime(float gc, float gs) {
     k = max(-NQ, min(NQ, k));
     return (h ? 1 : 0) | ((k + NQ) << 1);
 }
+// The regime of a view record: the producer of the geometry may store it in the record's unused
+// fourth component, tagged with NQ (ray_regime_tag, host side); otherwise it is computed here.
+constexpr unsigned kRegimeTag = 0x52000000u;   // | NQ << 16 | regime
+template <int NQ>
+__device__ __forceinline__ int regime_of(float4 g) {
+    const unsigned w = __float_as_uint(g.w);
+    if ((w >> 16) == ((kRegimeTag >> 16) | (unsigned)NQ)) return (int)(w & 0xffffu);
+    return ray_regime<NQ>(g.x, g.y);
+}
 // sh(j) = round(j k / NQ), halves up (the numerator is kept positive for the division)
 template <int NQ>
 __device__ __forceinline__ int ray_shift(int j, int regime) {
@@ -1029,16 +1039,10 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
             for (int s = 0; s < S; s++) acc[sl][s] = 0;
         float lin[Q], fix[2];
         int regime = 0;
-        float2 gnext = make_float2(0.0f, 0.0f);   // fcos, fsin of the first view of chunk k + 1
+        float4 gnext = make_float4(0.0f, 0.0f, 0.0f, 0.0f);   // record of the first view of chunk k + 1
         if (NQ > 0) {
-            if (nchunks > 0) {
-                const float4 g0 = __ldg(J.geom);
-                regime = ray_regime<NQ>(g0.x, g0.y);
-            }
-            if (nchunks > 1) {
-                const float4 g1 = __ldg(J.geom + VC);
-                gnext = make_float2(g1.x, g1.y);
-            }
+            if (nchunks > 0) regime = regime_of<NQ>(__ldg(J.geom));
+            if (nchunks > 1) gnext = __ldg(J.geom + VC);
             ray_coords<NQ, CW>(regime, X0, Y0, warp, lane, lin, fix);
         } else {
             const int tx = (warp % 2) * 8 + (lane & 7), ty = (warp / 2) * 4 + (lane >> 3);
@@ -1051,8 +1055,12 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
         for (int k = 0; k < nchunks; k++) {
             const unsigned g = gc + (unsigned)k;
             const int b = (int)(g % NB);
-            if (!failed && __any_sync(0xffffffffu, *abortw != 0)) failed = true;
-            if (!failed && !__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u))) failed = true;
+            // the producer's abort word is read only when the data wait does not succeed at once
+            if (!failed && !__all_sync(0xffffffffu, mbar_try_wait(smem_u32(&bars[b]), (g / NB) & 1u))) {
+                if (__any_sync(0xffffffffu, *abortw != 0) ||
+                    !__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[b]), (g / NB) & 1u)))
+                    failed = true;
+            }
             if (!failed) {
                 const int nv = min(VC, nviews - k * VC);
                 if (NQ == 0 || !(regime & 1))
@@ -1066,11 +1074,8 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                 // the next chunk's regime (the same value in every consumer thread)
                 int next = regime;
                 if (k + 1 < nchunks) {
-                    next = ray_regime<NQ>(gnext.x, gnext.y);
-                    if (k + 2 < nchunks) {
-                        const float4 gn = __ldg(J.geom + (size_t)(k + 2) * VC);
-                        gnext = make_float2(gn.x, gn.y);
-                    }
+                    next = regime_of<NQ>(gnext);
+                    if (k + 2 < nchunks) gnext = __ldg(J.geom + (size_t)(k + 2) * VC);
                 }
                 if (next != regime) {
                     // every consumer is done reading buffer b and none has released it: exchange
@@ -1905,6 +1910,26 @@ int ref_table_fmt() {
     load_defaults();
     return g_fmt;
 }
+// The default layout's regime (NQ = 12) of a view, tagged for regime_of: an orientation bit and
+// the shear k = rint(12 t), t = -fcos/fsin or -fsin/fcos, whichever has |t| <= 1.  Any value would
+// give the same slices; the tag only spares every consumer thread the division per chunk.
+float ray_regime_tag(float gc, float gs) {
+    constexpr int NQ = 12;
+    const bool h = fabsf(gs) > fabsf(gc);
+    const float den = h ? gs : gc;
+    int k = 0;
+    if (den != 0.0f) {
+        const float t = (h ? -gc : -gs) / den;
+        k = (int)lrintf(t * (float)NQ);
+        k = k < -NQ ? -NQ : (k > NQ ? NQ : k);
+    }
+    const unsigned r = (h ? 1u : 0u) | ((unsigned)(k + NQ) << 1);
+    const unsigned w = kRegimeTag | ((unsigned)NQ << 16) | r;
+    float f;
+    memcpy(&f, &w, sizeof f);
+    return f;
+}
+
 long long ref_table_stride(int ixdimp, int fmt) {
     if (fmt == kTabPair) return 2LL * ((ixdimp + 1) & ~1);   // floats, pairs rounded to an even count
     if (fmt == kTabInt17) return ((long long)17 * ixdimp + 15) & ~15LL;

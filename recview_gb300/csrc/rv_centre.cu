@@ -312,7 +312,7 @@ extern "C" int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInte
             for (int v = 0; v < nviews; v++) {
                 float fc, fs, fo;
                 view_geometry(d, centres[c0 + b], fdeg[v], fTiltAngle, &fc, &fs, &fo);
-                geom[(size_t)b * nviews + v] = make_float4(fc, fs, fo, 0.0f);
+                geom[(size_t)b * nviews + v] = make_float4(fc, fs, fo, ray_regime_tag(fc, fs));
                 RowJob j{};
                 j.src_row = v;
                 j.dst = b * nviews + v;

@@ -381,7 +381,7 @@ extern "C" void CudaReconstHost(RECONST_INFO* ri, int idev, bool bReport, bool b
             float fc, fs, fo;
             view_geometry(d, ri->center, ri->fdeg[views[v]], ri->fTiltAngle, &fc, &fs, &fo);
             if (shift16) fo = fo + (float)shift16;  // source/cudaReconst.cu:222
-            geom[v] = make_float4(fc, fs, fo, 0.0f);
+            geom[v] = make_float4(fc, fs, fo, ray_regime_tag(fc, fs));
         }
         if (!c->geom.ensure(nv * sizeof(float4))) {
             fail(ri, RV_ERR_DEVICE_OOM, "geometry table");

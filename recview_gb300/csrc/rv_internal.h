@@ -152,6 +152,9 @@ inline int lin_pair_bytes(int mode) { return mode == RV_MODE_LIN ? 8 : 4; }
 enum { kTabInt16 = 0, kTabInt17 = 1, kTabPair = 2 };
 int ref_table_fmt();
 long long ref_table_stride(int ixdimp, int fmt);
+// fourth component of a REF view record {fcos, fsin, foffset, .}: the back-projection's ray-layout
+// regime of the view, tagged (the kernels compute it themselves when the tag is absent)
+float ray_regime_tag(float fcos, float fsin);
 // Status word written by kernels whose bounded waits ran out (0 = fine); read-and-clear after
 // synchronising stream s.  One word per device, shared by every call on it: a call whose work
 // overlaps another's on the GPU may take the other's report.  kStatusUnreadable is returned

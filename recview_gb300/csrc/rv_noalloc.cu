@@ -112,7 +112,7 @@ extern "C" int RvReconstructSliceNoAlloc(const short* d_sino, int nviews, int ix
         jobs[v] = j;
         float fc, fs, fo;
         view_geometry(d, center, fdeg[v], fTiltAngle, &fc, &fs, &fo);
-        geom[v] = make_float4(fc, fs, fo, 0.0f);
+        geom[v] = make_float4(fc, fs, fo, ray_regime_tag(fc, fs));
     }
     if (!cuda_ok(cudaMemcpyAsync(base + o_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, s),
                  RV_ERR_COPY_H2D, "twiddles") ||

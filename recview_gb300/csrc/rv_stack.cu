@@ -12,6 +12,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "rv_internal.h"
@@ -158,7 +161,7 @@ static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_table
     for (int v = 0; v < V; v++) {
         float fc, fs, fo;
         view_geometry(d, desc->center, desc->fdeg[views[v]], desc->fTiltAngle, &fc, &fs, &fo);
-        st->geom_ref[v] = make_float4(fc, fs, fo, 0.0f);
+        st->geom_ref[v] = make_float4(fc, fs, fo, ray_regime_tag(fc, fs));
         const double th = (double)(desc->fdeg[views[v]] + desc->fTiltAngle) * (3.14159265358979323846 / 180.0);
         const double c = cos(th), sn = -sin(th);
         st->geom_lin[v] = LinGeom{c, sn, cen_lin - d.ixdimh * (c + sn), 0.0};
@@ -496,15 +499,39 @@ struct RvQueueItem {
     RvStack* st;
     const void* d_raw;
     void* d_out;
+    int variant;   // back-projection variant of this dataset's tiles (-1: the queue's default)
 };
+
+// ---- per-shape autotuning --------------------------------------------------------------------
+// A dataset's shape class: output size (ixdimp <= 1024 / 2048 / 4096 / more), view count
+// (<= 1000 / 2000 / more), whether its slices can run as pairs (two or more slices), and the
+// table layout.  RvQueueAutotune times candidate persistent variants -- they differ in pixel tile
+// (64x64, 128x64, 128x128), views per staged chunk, slices per CTA (1 or 2) and consumer warps
+// (8 or 16) -- on a few slices of one dataset of each class, and the winner is kept in a
+// process-wide cache keyed by the class, so later queues with the same shapes reuse it.
+static unsigned shape_key(const RvStack* st, int fmt) {
+    const int n = st->d.ixdimp, V = st->nviews;
+    const unsigned cx = n <= 1024 ? 0u : (n <= 2048 ? 1u : (n <= 4096 ? 2u : 3u));
+    const unsigned cv = V <= 1000 ? 0u : (V <= 2000 ? 1u : 2u);
+    const unsigned pr = st->desc.nslices >= 2 ? 1u : 0u;
+    return cx | (cv << 2) | (pr << 4) | ((unsigned)fmt << 5);
+}
+static std::mutex g_shape_mu;
+static std::map<unsigned, int> g_shape_variant;
+static int cached_variant(unsigned key) {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    auto it = g_shape_variant.find(key);
+    return it == g_shape_variant.end() ? -1 : it->second;
+}
 
 struct RvQueue {
     std::vector<RvQueueItem> items;
     int fmt = kTabInt16;
-    int variant = -1;
+    int variant = -1;   // default variant for datasets whose shape class has no tuned choice
     bool built = false;
-    struct FilterPart { FilterLaunch fl; };
-    struct Wave { std::vector<FilterLaunch> filters; int tile_begin = 0, ntiles = 0; };
+    // one persistent back-projection launch per variant group of a wave
+    struct Group { int variant = 0, tile_begin = 0, ntiles = 0; };
+    struct Wave { std::vector<FilterLaunch> filters; std::vector<Group> groups; };
     std::vector<Wave> waves;
     void* d_rowjobs = nullptr;
     void* d_tiles = nullptr;
@@ -529,6 +556,7 @@ struct RvQueue {
         waves.clear();
         built = false;
     }
+    int item_variant(int it) const { return items[it].variant >= 0 ? items[it].variant : variant; }
 };
 
 extern "C" int RvQueueCreate(RvQueue** out) {
@@ -558,56 +586,55 @@ extern "C" int RvQueueAdd(RvQueue* q, const RvStackDesc* desc, const void* d_raw
     RvStack* st = nullptr;   // the queue keeps its own table pool: no per-stack tables
     const int rc = stack_create(desc, &st, false);
     if (rc) return rc;
-    q->items.push_back({st, d_raw, d_out});
+    q->items.push_back({st, d_raw, d_out, cached_variant(shape_key(st, q->fmt))});
     q->release_plan();
     return 0;
 }
 
-static int queue_build(RvQueue* q, cudaStream_t s) {
+// slices [s0, s1) of item `item`, back-projected with `variant`
+struct QueueReq { int item, s0, s1, variant; };
+
+static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
     q->release_plan();
     q->total_updates = 0;
-    int tx = 64, ty = 64;
-    persistent_tile_xy(q->variant, &tx, &ty);
     size_t budget_mb = 32768;
     if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
     const size_t pool_words_max = (budget_mb << 20) / 4;
     // ---- waves of (item, slice range) whose tables fit the pool ---------------------------
-    struct Part { int item, s0, s1; size_t off; };
+    struct Part { int item, s0, s1, variant; size_t off; };
     std::vector<std::vector<Part>> wparts(1);
     size_t used = 0, pool_words = 0;
-    for (int it = 0; it < (int)q->items.size(); it++) {
-        RvStack* st = q->items[it].st;
+    for (const QueueReq& rq : reqs) {
+        RvStack* st = q->items[rq.item].st;
         const size_t per_slice = (size_t)st->nviews * (size_t)ref_table_stride(st->d.ixdimp, q->fmt);
         if (per_slice > pool_words_max) {
             set_error(RV_ERR_UNSUPPORTED, "RvQueueRun: one slice's tables exceed the table budget");
             return RV_ERR_UNSUPPORTED;
         }
-        int s = 0;
-        while (s < st->desc.nslices) {
+        int s = rq.s0;
+        while (s < rq.s1) {
             if (used + per_slice > pool_words_max) {
                 wparts.emplace_back();
                 used = 0;
             }
             int n = (int)((pool_words_max - used) / per_slice);
-            if (n > st->desc.nslices - s) n = st->desc.nslices - s;
-            wparts.back().push_back({it, s, s + n, used});
+            if (n > rq.s1 - s) n = rq.s1 - s;
+            wparts.back().push_back({rq.item, s, s + n, rq.variant, used});
             used += per_slice * n;
             if (used > pool_words) pool_words = used;
             s += n;
         }
     }
-    // ---- row jobs, filter launches and tile work lists --------------------------------------
+    // ---- row jobs, filter launches and tile work lists (tiles grouped by variant) ------------
     std::vector<RowJob> rowjobs;
     std::vector<TileJob> tiles;
     std::vector<size_t> rj_begin;   // per filter launch: start index into rowjobs
     for (auto& parts : wparts) {
         RvQueue::Wave w;
-        w.tile_begin = (int)tiles.size();
         for (const Part& pt : parts) {
             RvStack* st = q->items[pt.item].st;
             const int V = st->nviews;
             const long long ts = ref_table_stride(st->d.ixdimp, q->fmt);
-            const size_t npix = (size_t)st->d.ixdimp * st->d.ixdimp;
             rj_begin.push_back(rowjobs.size());
             for (int sl = pt.s0; sl < pt.s1; sl++)
                 for (int v = 0; v < V; v++) {
@@ -630,34 +657,55 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
             fl.table_stride = ts;
             fl.table_fmt = q->fmt;
             w.filters.push_back(fl);
-            const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
-            // the slice-pair kernel takes two consecutive slices of a part per job (they share
-            // the geometry and their tables follow each other in the pool)
-            const int step = (q->variant >= 18 && q->variant <= 20) ? 2 : 1;
-            for (int sl = pt.s0; sl < pt.s1; sl += step)
-                for (int t = 0; t < ntx * nty; t++) {
-                    TileJob J{};
-                    J.table = reinterpret_cast<const int*>((pt.off + (size_t)(sl - pt.s0) * V * ts) * 4);
-                    J.geom = static_cast<const float4*>(st->d_geom);
-                    J.out = static_cast<int*>(q->items[pt.item].d_out) + (size_t)sl * npix;
-                    J.table_stride = ts;
-                    J.nviews = V;
-                    J.ixdimp = st->d.ixdimp;
-                    J.X0 = (t % ntx) * tx;
-                    J.Y0 = (t / ntx) * ty;
-                    J.pair = (step == 2 && sl + 1 < pt.s1) ? 1 : 0;
-                    tiles.push_back(J);
-                }
-            q->total_updates += (double)(pt.s1 - pt.s0) * V * npix;
         }
-        w.ntiles = (int)tiles.size() - w.tile_begin;
+        // tiles: every part of a variant forms one group (one persistent launch)
+        std::vector<int> variants;
+        for (const Part& pt : parts)
+            if (std::find(variants.begin(), variants.end(), pt.variant) == variants.end()) variants.push_back(pt.variant);
+        for (int var : variants) {
+            RvQueue::Group g;
+            g.variant = var;
+            g.tile_begin = (int)tiles.size();
+            int tx = 64, ty = 64;
+            persistent_tile_xy(var, &tx, &ty);
+            // the slice-pair kernels take two consecutive slices of a part per job (they share
+            // the geometry and their tables follow each other in the pool)
+            const int step = (var >= 18 && var <= 20) ? 2 : 1;
+            for (const Part& pt : parts) {
+                if (pt.variant != var) continue;
+                RvStack* st = q->items[pt.item].st;
+                const int V = st->nviews;
+                const long long ts = ref_table_stride(st->d.ixdimp, q->fmt);
+                const size_t npix = (size_t)st->d.ixdimp * st->d.ixdimp;
+                const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
+                for (int sl = pt.s0; sl < pt.s1; sl += step)
+                    for (int t = 0; t < ntx * nty; t++) {
+                        TileJob J{};
+                        J.table = reinterpret_cast<const int*>((pt.off + (size_t)(sl - pt.s0) * V * ts) * 4);
+                        J.geom = static_cast<const float4*>(st->d_geom);
+                        J.out = static_cast<int*>(q->items[pt.item].d_out) + (size_t)sl * npix;
+                        J.table_stride = ts;
+                        J.nviews = V;
+                        J.ixdimp = st->d.ixdimp;
+                        J.X0 = (t % ntx) * tx;
+                        J.Y0 = (t / ntx) * ty;
+                        J.pair = (step == 2 && sl + 1 < pt.s1) ? 1 : 0;
+                        tiles.push_back(J);
+                    }
+                q->total_updates += (double)(pt.s1 - pt.s0) * V * npix;
+            }
+            g.ntiles = (int)tiles.size() - g.tile_begin;
+            w.groups.push_back(g);
+        }
         q->waves.push_back(std::move(w));
     }
+    size_t ngroups = 0;
+    for (const auto& w : q->waves) ngroups += w.groups.size();
     q->total_tiles = tiles.size();
     if (!cuda_ok(cudaMalloc(&q->d_pool, pool_words * 4 + 16), RV_ERR_DEVICE_OOM, "table pool") ||
         !cuda_ok(cudaMalloc(&q->d_rowjobs, rowjobs.size() * sizeof(RowJob) + 16), RV_ERR_DEVICE_OOM, "row jobs") ||
         !cuda_ok(cudaMalloc(&q->d_tiles, tiles.size() * sizeof(TileJob) + 16), RV_ERR_DEVICE_OOM, "tiles") ||
-        !cuda_ok(cudaMalloc((void**)&q->d_counters, q->waves.size() * sizeof(unsigned)), RV_ERR_DEVICE_OOM, "counters"))
+        !cuda_ok(cudaMalloc((void**)&q->d_counters, (ngroups + 1) * sizeof(unsigned)), RV_ERR_DEVICE_OOM, "counters"))
         return RvGetLastError();
     // rebase pool offsets to device addresses
     int* pool = static_cast<int*>(q->d_pool);
@@ -673,23 +721,35 @@ static int queue_build(RvQueue* q, cudaStream_t s) {
         !cuda_ok(cudaMemcpy(q->d_tiles, tiles.data(), tiles.size() * sizeof(TileJob), cudaMemcpyHostToDevice),
                  RV_ERR_COPY_H2D, "tiles"))
         return RvGetLastError();
-    (void)s;
     q->built = true;
     return 0;
 }
 
+// the whole queue: every dataset's slices with its own variant
+static int queue_build(RvQueue* q) {
+    std::vector<QueueReq> reqs;
+    for (int it = 0; it < (int)q->items.size(); it++)
+        reqs.push_back({it, 0, q->items[it].st->desc.nslices, q->item_variant(it)});
+    return queue_build_reqs(q, reqs);
+}
+
 static int queue_launch(RvQueue* q, cudaStream_t s) {
     const TileJob* tiles = static_cast<const TileJob*>(q->d_tiles);
+    size_t c = 0;
     for (size_t w = 0; w < q->waves.size(); w++) {
         RvQueue::Wave& wv = q->waves[w];
-        if (!cuda_ok(cudaMemsetAsync(q->d_counters + w, 0, sizeof(unsigned), s), RV_ERR_MEMSET, "counter"))
+        if (!wv.groups.empty() &&
+            !cuda_ok(cudaMemsetAsync(q->d_counters + c, 0, wv.groups.size() * sizeof(unsigned), s), RV_ERR_MEMSET,
+                     "counter"))
             return RV_ERR_MEMSET;
         for (const FilterLaunch& fl : wv.filters)
             if (!cuda_ok(launch_filter(fl, s), RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
-        if (!cuda_ok(launch_bp_ref_persistent(tiles + wv.tile_begin, wv.ntiles, q->d_counters + w, q->fmt,
-                                              q->variant, s),
-                     RV_ERR_LAUNCH, "persistent back-projection"))
-            return RV_ERR_LAUNCH;
+        for (const RvQueue::Group& g : wv.groups) {
+            if (!cuda_ok(launch_bp_ref_persistent(tiles + g.tile_begin, g.ntiles, q->d_counters + c, q->fmt, g.variant, s),
+                         RV_ERR_LAUNCH, "persistent back-projection"))
+                return RV_ERR_LAUNCH;
+            c++;
+        }
     }
     return 0;
 }
@@ -700,7 +760,7 @@ extern "C" int RvQueueRun(RvQueue* q, void* stream) {
     cudaStream_t cap = nullptr;
     int rc = 0;
     if (!q->built) {
-        if ((rc = queue_build(q, s))) return rc;
+        if ((rc = queue_build(q))) return rc;
         // capture the whole sequence once (on a private stream: the legacy stream cannot capture)
         if (!cuda_ok(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), RV_ERR_STREAM, "capture stream"))
             return RV_ERR_STREAM;
@@ -735,34 +795,86 @@ extern "C" int RvQueueRun(RvQueue* q, void* stream) {
     return 0;
 }
 
-extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
-    // times every int-table variant's persistent kernel on the whole queue (graph-free runs) and
-    // keeps the fastest for the captured graph
-    if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
-    cudaStream_t s = (cudaStream_t)stream;
-    const int cands[] = {18, 19, 16, 17, 11, 13, 14, 15, 6, 9, 3, 0, 7, 12};
+// device time of one plan launch (after one untimed launch), in ms; < 0 on error
+static float time_plan(RvQueue* q, cudaStream_t s, int reps) {
+    if (queue_launch(q, s)) return -1.0f;
     float best = 3.0e38f;
-    int bestv = q->variant;
-    for (int v : cands) {
-        q->variant = v;
-        int rc = queue_build(q, s);
-        if (rc) return rc;
-        if ((rc = queue_launch(q, s))) return rc;   // warm-up
+    for (int r = 0; r < reps; r++) {
         cudaEventRecord(q->ev[0], s);
-        if ((rc = queue_launch(q, s))) return rc;
+        if (queue_launch(q, s)) return -1.0f;
         cudaEventRecord(q->ev[1], s);
-        cudaEventSynchronize(q->ev[1]);
+        if (cudaEventSynchronize(q->ev[1]) != cudaSuccess) return -1.0f;
         float ms = 0;
         cudaEventElapsedTime(&ms, q->ev[0], q->ev[1]);
-        if (ms < best) {
-            best = ms;
-            bestv = v;
-        }
+        if (ms < best) best = ms;
     }
-    q->variant = bestv;
+    return best;
+}
+
+extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
+    // per shape class of the queue's datasets: time each candidate variant's persistent kernel on
+    // a few slices of the first dataset of the class, keep the fastest in the process-wide cache
+    // and in every dataset of the class
+    if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    // candidates spanning the tuned dimensions: 64x64 tiles with slice pairs and 4-view chunks
+    // (18), the same with 16 consumer warps (19), single slices with 6-view chunks (16), compact
+    // lane blocks (17), warp-0-produced pipelines with 4- and 5-view chunks (11, 14), 128x128 and
+    // 128x64 tiles (0, 4)
+    const int cands[] = {18, 19, 16, 17, 11, 14, 0, 4};
+    std::map<unsigned, int> tuned;
+    for (int it = 0; it < (int)q->items.size(); it++) {
+        const unsigned key = shape_key(q->items[it].st, q->fmt);
+        if (tuned.count(key)) continue;
+        // probe slices: enough 64x64 tiles to fill the GPU about twice (2..8 slices, even when
+        // the class runs slice pairs), never more than the dataset has
+        const int S = q->items[it].st->desc.nslices;
+        const int t64 = ((q->items[it].st->d.ixdimp + 63) / 64) * ((q->items[it].st->d.ixdimp + 63) / 64);
+        int n = (2048 + t64 - 1) / t64;
+        n = n < 2 ? 2 : (n > 8 ? 8 : n);
+        n += n & 1;
+        if (n > S) n = S;
+        float best = 3.0e38f;
+        int bestv = q->variant;
+        for (int v : cands) {
+            const int rc = queue_build_reqs(q, {QueueReq{it, 0, n, v}});
+            if (rc) return rc;
+            const float ms = time_plan(q, s, 2);
+            if (ms < 0.0f) {
+                q->release_plan();
+                set_error(RV_ERR_LAUNCH, "RvQueueAutotune: a probe launch failed");
+                return RV_ERR_LAUNCH;
+            }
+            if (ms < best) {
+                best = ms;
+                bestv = v;
+            }
+        }
+        tuned[key] = bestv;
+        std::lock_guard<std::mutex> lock(g_shape_mu);
+        g_shape_variant[key] = bestv;
+    }
+    for (RvQueueItem& item : q->items) item.variant = tuned[shape_key(item.st, q->fmt)];
     q->release_plan();
-    if (chosen) *chosen = bestv;
+    if (const unsigned ks = take_kernel_status(s)) {
+        set_error(RV_ERR_KERNEL_STATUS, std::string("back-projection: ") + kernel_status_text(ks));
+        return RV_ERR_KERNEL_STATUS;
+    }
+    if (chosen) *chosen = q->items[0].variant;
     return 0;
+}
+
+extern "C" int RvQueueSetItemVariant(RvQueue* q, int item, int variant) {
+    // every int-table variant 0..20 has a persistent form
+    if (!q || item < 0 || item >= (int)q->items.size() || variant < 0 || variant > 20) return RV_ERR_BAD_ARGUMENT;
+    q->items[item].variant = variant;
+    q->release_plan();
+    return 0;
+}
+
+extern "C" int RvQueueItemVariant(const RvQueue* q, int item) {
+    if (!q || item < 0 || item >= (int)q->items.size()) return -1;
+    return q->item_variant(item);
 }
 
 extern "C" float RvQueueLastMs(const RvQueue* q) { return q ? q->last_ms : 0.0f; }

@@ -49,8 +49,9 @@ def datasets(oracle):
     return out
 
 
-@pytest.mark.parametrize("budget_mb,autotune", [(None, False), (16, False), (None, True)])
-def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune):
+@pytest.mark.parametrize("budget_mb,autotune,pinned", [(None, False, None), (16, False, None), (None, True, None),
+                                                       (None, False, [18, 16, 0, 11]), (16, False, [16, 18, 9, 18])])
+def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune, pinned):
     torch = pytest.importorskip("torch")
     if budget_mb:
         monkeypatch.setenv("RV_TABLE_BUDGET_MB", str(budget_mb))   # several waves
@@ -72,6 +73,15 @@ def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune):
             chosen = C.c_int(-1)
             assert L.RvQueueAutotune(q, None, C.byref(chosen)) == 0, rv.last_error()
             assert 0 <= chosen.value <= 20
+            assert L.RvQueueItemVariant(q, 0) == chosen.value
+            for i in range(len(datasets)):
+                assert 0 <= L.RvQueueItemVariant(q, i) <= 20
+        if pinned:   # datasets on different variants: one persistent launch per variant and wave
+            for i, v in enumerate(pinned):
+                assert L.RvQueueSetItemVariant(q, i, v) == 0
+                assert L.RvQueueItemVariant(q, i) == v
+            assert L.RvQueueSetItemVariant(q, 0, 21) == abi.RV_ERR_BAD_ARGUMENT
+            assert L.RvQueueItemVariant(q, len(datasets)) == -1
         for run in range(2):   # first run captures the graph, second replays it
             for d_out, _ in outs:
                 d_out.fill_(-1)
@@ -81,5 +91,34 @@ def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune):
                 assert np.array_equal(d_out.cpu().numpy(), want), f"run {run}"
         assert L.RvQueueLastMs(q) > 0
         assert L.RvQueueUpdates(q) == sum(float(w.size) * (raw.shape[0] - 3) for (raw, *_r, w) in datasets)
+    finally:
+        L.RvQueueDestroy(q)
+
+
+def test_queue_strip_assembly_dataset(gpu, oracle):
+    """A dataset given as full-resolution frames with a trimmed region of interest and x2 zoom
+    (the library trims; iTrim / iRawWidth) runs through the queue bit-exactly."""
+    torch = pytest.importorskip("torch")
+    F, T, interp, S, V = 240, 60, 3, 2, 90
+    ixlen = oracle.L.rvo_bin_width(F, T, interp)
+    raw, bInc, fdeg, fexp, _ = phantom.raw_stack(81, F, V, S, 121.4, n_ellipsoids=10)
+    roi = oracle.bin_frames(raw, F, T, interp, S)
+    cen = ixlen / 2.0 + 1.3
+    Fl = oracle.set_filter(abi.FILT_SHEPP, rv.dims(ixlen, interp).ndim)
+    want = _oracle_stack(oracle, roi, bInc, fdeg, fexp, cen, Fl, interp)
+    L = rv.lib()
+    q = C.c_void_p()
+    assert L.RvQueueCreate(C.byref(q)) == 0
+    try:
+        d_raw = torch.from_numpy(raw.view(np.int16)).cuda()
+        n = rv.dims(ixlen, interp).ixdimp
+        d_out = torch.full((S, n, n), -1, dtype=torch.int32, device="cuda")
+        desc = _desc(ixlen, raw.shape[0] - 1, S, cen, interp, bInc, fdeg, fexp, Fl)
+        desc.iTrim, desc.iRawWidth = T, F
+        assert L.RvQueueAdd(q, C.byref(desc), C.c_void_p(d_raw.data_ptr()), C.c_void_p(d_out.data_ptr())) == 0, \
+            rv.last_error()
+        assert L.RvQueueRun(q, None) == 0, rv.last_error()
+        torch.cuda.synchronize()
+        assert np.array_equal(d_out.cpu().numpy(), want)
     finally:
         L.RvQueueDestroy(q)
