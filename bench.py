@@ -843,7 +843,7 @@ def run_queue(args):
         return out
 
     fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
-    q_total = s_total = 0.0
+    q_total = s_total = qdev_total = sdev_total = 0.0
     upd_total = 0.0
     same_all = True
     variants, oracle_checks = {}, []
@@ -883,12 +883,13 @@ def run_queue(args):
         for k, x in enumerate(data):
             variants[x["i"]] = L.RvQueueItemVariant(q, k)
         assert L.RvQueueRun(q, None) == 0, rv.last_error()          # captures the graph
-        qt = []
+        qt, qd = [], []
         for _ in range(max(1, args.steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             assert L.RvQueueRun(q, None) == 0, rv.last_error()
             qt.append(time.perf_counter() - t0)
+            qd.append(L.RvQueueLastMs(q) * 1e-3)
         upd_total += L.RvQueueUpdates(q)
         L.RvQueueDestroy(q)
         sums_q = [checksum(x["out"]) for x in data]
@@ -900,21 +901,28 @@ def run_queue(args):
             stacks.append(h)
         for h, x in zip(stacks, data):
             assert L.RvStackRunDevice(h, C.c_void_p(x["raw"].data_ptr()), C.c_void_p(x["out"].data_ptr()), None) == 0
-        st_t = []
+        st_t, st_d = [], []
+        tm = (C.c_float * 3)()
         for _ in range(max(1, args.steps)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
+            dev_s = 0.0
             for h, x in zip(stacks, data):
                 assert L.RvStackRunDevice(h, C.c_void_p(x["raw"].data_ptr()), C.c_void_p(x["out"].data_ptr()),
                                           None) == 0, rv.last_error()
+                L.RvStackLastTimings(h, tm)
+                dev_s += tm[2] * 1e-3
             torch.cuda.synchronize()
             st_t.append(time.perf_counter() - t0)
+            st_d.append(dev_s)
         for h in stacks:
             L.RvStackDestroy(h)
         sums_s = [checksum(x["out"]) for x in data]
         same_all &= sums_q == sums_s
         q_total += float(np.median(qt))
         s_total += float(np.median(st_t))
+        qdev_total += float(np.median(qd))
+        sdev_total += float(np.median(st_d))
         # ---- slice 0 of the smallest zoomed and unzoomed dataset of the first batch vs the oracle
         if bi == 0:
             from tests.rvtest import Oracle
@@ -942,6 +950,9 @@ def run_queue(args):
             "shapes_W_V_S_zoom_trim": [[d["W"], d["V"], d["S"], 2 ** max(d["interp"] - 2, 0), d["T"]] for d in specs],
             "updates": upd_total, "queue_s": q_total, "one_stack_at_a_time_s": s_total,
             "speedup_vs_stacks": s_total / q_total, "slices_per_s": sum(d["S"] for d in specs) / q_total,
+            "device_s": {"queue": qdev_total, "one_stack_at_a_time": sdev_total,
+                         "note": "device time between the events bracketing each call (queue graph, or each stack's "
+                                 "kernels); wall minus device is the host time between the GPU's work"},
             "autotuned_variant_per_dataset": [variants[i] for i in range(len(specs))],
             "outputs_equal_queue_vs_stacks": bool(same_all), "oracle_checks": oracle_checks,
             "timing": "host wall clock per batch (each call returns after its work), median of the timed runs, summed "

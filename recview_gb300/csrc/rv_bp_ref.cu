@@ -2192,9 +2192,13 @@ int default_variant() {
 }
 
 cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {
+    load_defaults();
+    return launch_bp_ref_variant(pin, s, g_variant);
+}
+
+cudaError_t launch_bp_ref_variant(const BackprojLaunch& pin, cudaStream_t s, int variant) {
     BackprojLaunch p = pin;
     load_defaults();
-    const int variant = g_variant;
     const bool checked = g_checked != 0;
     unsigned int* counter = nullptr;
     if (checked) {

@@ -138,6 +138,8 @@ int default_variant();
 cudaError_t launch_bp_ref_persistent(const TileJob* d_jobs, int njobs, unsigned* d_counter, int table_fmt,
                                      int variant, cudaStream_t s);
 cudaError_t launch_bp_ref(const BackprojLaunch& p, cudaStream_t s);
+// the same with an explicit variant (0..20) instead of the process default
+cudaError_t launch_bp_ref_variant(const BackprojLaunch& p, cudaStream_t s, int variant);
 // LIN / FP16 / BF16 back-projection of pair rows (rows16 = pairs (r[j], r[j+1]-r[j]) of 8 or 4 bytes,
 // row_stride / slice_row_stride in pairs, row_scale per row for the 16-bit forms)
 cudaError_t launch_bp_lin(const BackprojLaunch& p, cudaStream_t s);

@@ -529,8 +529,10 @@ struct RvQueue {
     int fmt = kTabInt16;
     int variant = -1;   // default variant for datasets whose shape class has no tuned choice
     bool built = false;
-    // one persistent back-projection launch per variant group of a wave
-    struct Group { int variant = 0, tile_begin = 0, ntiles = 0; };
+    // one back-projection per variant group of a wave: a persistent launch over the group's tile
+    // list, or -- for groups with many tiles, where a work list gains nothing over the hardware's
+    // own scheduling -- the regular grid launch of each part (grid non-empty)
+    struct Group { int variant = 0, tile_begin = 0, ntiles = 0; std::vector<BackprojLaunch> grid; };
     struct Wave { std::vector<FilterLaunch> filters; std::vector<Group> groups; };
     std::vector<Wave> waves;
     void* d_rowjobs = nullptr;
@@ -593,6 +595,12 @@ extern "C" int RvQueueAdd(RvQueue* q, const RvStackDesc* desc, const void* d_raw
 
 // slices [s0, s1) of item `item`, back-projected with `variant`
 struct QueueReq { int item, s0, s1, variant; };
+// tiles of a variant group from which the wave launches the regular grid kernels instead of the
+// persistent one (about eight waves of 64x64 tiles on the GPU; RV_QUEUE_GRID_TILES overrides)
+static int grid_tiles_threshold() {
+    const char* e = getenv("RV_QUEUE_GRID_TILES");
+    return e ? atoi(e) : 2432;
+}
 
 static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
     q->release_plan();
@@ -695,6 +703,28 @@ static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
                 q->total_updates += (double)(pt.s1 - pt.s0) * V * npix;
             }
             g.ntiles = (int)tiles.size() - g.tile_begin;
+            if (g.ntiles >= grid_tiles_threshold()) {
+                // large group: regular launches per part (tables at the part's pool offset)
+                for (const Part& pt : parts) {
+                    if (pt.variant != var) continue;
+                    RvStack* st = q->items[pt.item].st;
+                    const long long ts = ref_table_stride(st->d.ixdimp, q->fmt);
+                    const size_t npix = (size_t)st->d.ixdimp * st->d.ixdimp;
+                    BackprojLaunch bl{};
+                    bl.table = reinterpret_cast<const int*>((size_t)pt.off * 4);   // rebased below
+                    bl.geom = static_cast<const float4*>(st->d_geom);
+                    bl.nviews = st->nviews;
+                    bl.nslices = pt.s1 - pt.s0;
+                    bl.ixdimp = st->d.ixdimp;
+                    bl.table_stride = ts;
+                    bl.slice_table_stride = ts * st->nviews;
+                    bl.out = static_cast<int*>(q->items[pt.item].d_out) + (size_t)pt.s0 * npix;
+                    bl.out_slice_stride = (long long)npix;
+                    bl.mode = RV_MODE_REF;
+                    bl.table_fmt = q->fmt;
+                    g.grid.push_back(bl);
+                }
+            }
             w.groups.push_back(g);
         }
         q->waves.push_back(std::move(w));
@@ -710,6 +740,9 @@ static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
     // rebase pool offsets to device addresses
     int* pool = static_cast<int*>(q->d_pool);
     for (TileJob& J : tiles) J.table = pool + reinterpret_cast<size_t>(J.table) / 4;
+    for (auto& w : q->waves)
+        for (RvQueue::Group& g : w.groups)
+            for (BackprojLaunch& bl : g.grid) bl.table = pool + reinterpret_cast<size_t>(bl.table) / 4;
     size_t fi = 0;
     for (auto& w : q->waves)
         for (FilterLaunch& fl : w.filters) {
@@ -745,9 +778,15 @@ static int queue_launch(RvQueue* q, cudaStream_t s) {
         for (const FilterLaunch& fl : wv.filters)
             if (!cuda_ok(launch_filter(fl, s), RV_ERR_LAUNCH, "filter kernel")) return RV_ERR_LAUNCH;
         for (const RvQueue::Group& g : wv.groups) {
-            if (!cuda_ok(launch_bp_ref_persistent(tiles + g.tile_begin, g.ntiles, q->d_counters + c, q->fmt, g.variant, s),
-                         RV_ERR_LAUNCH, "persistent back-projection"))
+            if (!g.grid.empty()) {
+                for (const BackprojLaunch& bl : g.grid)
+                    if (!cuda_ok(launch_bp_ref_variant(bl, s, g.variant), RV_ERR_LAUNCH, "back-projection"))
+                        return RV_ERR_LAUNCH;
+            } else if (!cuda_ok(launch_bp_ref_persistent(tiles + g.tile_begin, g.ntiles, q->d_counters + c, q->fmt,
+                                                         g.variant, s),
+                                RV_ERR_LAUNCH, "persistent back-projection")) {
                 return RV_ERR_LAUNCH;
+            }
             c++;
         }
     }

@@ -49,12 +49,17 @@ def datasets(oracle):
     return out
 
 
-@pytest.mark.parametrize("budget_mb,autotune,pinned", [(None, False, None), (16, False, None), (None, True, None),
-                                                       (None, False, [18, 16, 0, 11]), (16, False, [16, 18, 9, 18])])
-def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune, pinned):
+@pytest.mark.parametrize("budget_mb,autotune,pinned,grid", [(None, False, None, False), (16, False, None, False),
+                                                            (None, True, None, False),
+                                                            (None, False, [18, 16, 0, 11], False),
+                                                            (16, False, [16, 18, 9, 18], False),
+                                                            (16, False, [18, 16, 0, 18], True)])
+def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune, pinned, grid):
     torch = pytest.importorskip("torch")
     if budget_mb:
         monkeypatch.setenv("RV_TABLE_BUDGET_MB", str(budget_mb))   # several waves
+    if grid:   # every group takes the regular grid launches per part instead of the persistent kernel
+        monkeypatch.setenv("RV_QUEUE_GRID_TILES", "1")
     L = rv.lib()
     q = C.c_void_p()
     assert L.RvQueueCreate(C.byref(q)) == 0
