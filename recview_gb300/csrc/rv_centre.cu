@@ -114,6 +114,68 @@ __global__ void k_tv_partial(const int* slices, int ixdimp, double* partial) {
     }
 }
 
+// ---- GetAxis host side ---------------------------------------------------------------------
+// Twice the rotation centre, in pixels, implied by a relative shift js of the two frames
+// (offset-CT frames are shifted by iAxisOffset first).
+static int doubled_centre(int js, int iAxisOffset, int ixdim) {
+    return iAxisOffset ? (js + iAxisOffset) * 2 : js + ixdim - 1;
+}
+
+// Shift (in [-h, h)) of the smallest value among the valid entries of curve[js + h]; the first
+// of equal values wins.  The running minimum is held in type R: the reference keeps it in float
+// for the per-row curves and in double for the overall one, which can decide between
+// near-equal neighbours, so both are kept.
+template <typename R>
+static int argmin_shift(const std::vector<double>& curve, const std::vector<unsigned char>& valid, int h) {
+    R lowest = (R)SHRT_MAX;
+    int best = 0;
+    for (int idx = 0; idx < 2 * h; idx++) {
+        if (!valid[idx] || !(curve[idx] < lowest)) continue;
+        lowest = (R)curve[idx];
+        best = idx - h;
+    }
+    return best;
+}
+
+// Centre of the parabola through three neighbouring curve values (left, middle, right) around
+// doubled centre c2, in the operation order of source/gazoDoc.cpp:4487-4491; a flat pair of
+// outer values keeps c2 / 2.
+static double parabola_vertex(double left, double mid, double right, int c2) {
+    if (right == left) return c2 / 2.;
+    const double r = (mid - left) / (right - left);
+    return (4 * r * c2 - (c2 * 2 - 1)) / (4 * r - 2) / 2;
+}
+
+// The centre of a curve whose arg-min is `best`: refined by the parabola unless the minimum
+// sits on the first or last shift.
+static double refined_centre(const std::vector<double>& curve, int h, int best, int iAxisOffset, int ixdim) {
+    const int c2 = doubled_centre(best, iAxisOffset, ixdim);
+    if (best == -h || best == h - 1) return c2 / 2.;
+    return parabola_vertex(curve[best - 1 + h], curve[best + h], curve[best + 1 + h], c2);
+}
+
+// Least-squares line centre(k) = intercept + slope k over the accepted rows k.  The sums of k and
+// k^2 are 32-bit ints in the reference and wrap on tall frames; unsigned arithmetic reproduces
+// the wrap without overflow.
+struct AxisLineFit {
+    int sum_k = 0, sum_kk = 0, n = 0;
+    double sum_c = 0, sum_kc = 0;
+    void add(int k, double c) {
+        sum_k += k;
+        sum_kk = (int)((unsigned)sum_kk + (unsigned)k * (unsigned)k);
+        sum_c += c;
+        sum_kc += k * c;
+        n++;
+    }
+    // false when fewer than min_rows rows were accepted (the caller then takes the overall centre)
+    bool solve(int min_rows, double* intercept, double* slope) const {
+        const int den = (int)((unsigned)n * (unsigned)sum_kk - (unsigned)sum_k * (unsigned)sum_k);
+        *intercept = (sum_kk * sum_c - sum_k * sum_kc) / den;
+        *slope = (sum_c - n * *intercept) / sum_k;
+        return n >= min_rows;
+    }
+};
+
 }  // namespace rv
 
 using namespace rv;
@@ -168,97 +230,46 @@ extern "C" int RvGetAxis(const unsigned short* sample0, const unsigned short* sa
     if (d_nd) cudaFree(d_nd);
     if (rc) return rc;
     // ---- host bookkeeping in the reference's arithmetic (source/gazoDoc.cpp:4443-4586) ----------
-    std::vector<double> sdiff(2 * ixdimh), center(icdim), sdifftotal(2 * ixdimh, 0.0);
-    std::vector<long long> ndifftotal(2 * ixdimh, 0);
+    // one SSD curve per sampled row, and the curve of all rows' sums
+    const int nshift = 2 * ixdimh;
+    std::vector<double> row_curve(nshift), total_sum(nshift, 0.0), center(icdim);
+    std::vector<long long> total_cnt(nshift, 0);
+    std::vector<unsigned char> row_valid(nshift), total_valid(nshift);
     for (int k = 0; k < iydim; k += istep) {
         const int icidx = k / istep;
-        float minDiff = SHRT_MAX;
-        int minIdx = 0;
-        for (int js = -ixdimh; js < ixdimh; js++) {
-            const int idx = js + ixdimh;
-            const long long s = ssd[(size_t)icidx * 2 * ixdimh + idx];
-            const int cnt = nd[(size_t)icidx * 2 * ixdimh + idx];
-            sdiff[idx] = (double)s;
-            sdifftotal[idx] += (double)s;
-            ndifftotal[idx] += cnt;
-            if (cnt == 0) continue;
-            sdiff[idx] /= cnt;
-            if (sdiff[idx] < minDiff) {
-                minDiff = (float)sdiff[idx];
-                minIdx = js;
-            }
+        for (int idx = 0; idx < nshift; idx++) {
+            const long long s = ssd[(size_t)icidx * nshift + idx];
+            const int cnt = nd[(size_t)icidx * nshift + idx];
+            total_sum[idx] += (double)s;
+            total_cnt[idx] += cnt;
+            row_valid[idx] = cnt != 0;
+            row_curve[idx] = cnt ? (double)s / cnt : (double)s;
         }
-        const int ixCenter2 = iAxisOffset ? (minIdx + iAxisOffset) * 2 : minIdx + ixdim - 1;
-        double c;
-        if (minIdx == -ixdimh || minIdx == ixdimh - 1) {
-            c = ixCenter2 / 2.;
-        } else {
-            const double dy1 = sdiff[minIdx + ixdimh];
-            double dy0 = sdiff[minIdx - 1 + ixdimh];
-            const double dy2 = sdiff[minIdx + 1 + ixdimh];
-            if (dy2 == dy0) c = (double)(ixCenter2 / 2.);
-            else {
-                dy0 = (dy1 - dy0) / (dy2 - dy0);
-                c = (4 * dy0 * ixCenter2 - (ixCenter2 * 2 - 1)) / (4 * dy0 - 2) / 2;
-            }
-        }
-        center[icidx] = c - 0.5;   // HALFPIXEL_OFFSET
+        const int best = argmin_shift<float>(row_curve, row_valid, ixdimh);
+        center[icidx] = refined_centre(row_curve, ixdimh, best, iAxisOffset, ixdim) - 0.5;   // HALFPIXEL_OFFSET
     }
-    double minDifftotal = SHRT_MAX;
-    int idifftotal = 0;
-    for (int j = -ixdimh; j < ixdimh; j++) {
-        const int idx = j + ixdimh;
-        if (ndifftotal[idx] == 0) continue;
-        sdifftotal[idx] /= (double)ndifftotal[idx];
-        if (sdifftotal[idx] < minDifftotal) {
-            minDifftotal = sdifftotal[idx];
-            idifftotal = j;
-        }
+    for (int idx = 0; idx < nshift; idx++) {
+        total_valid[idx] = total_cnt[idx] != 0;
+        if (total_valid[idx]) total_sum[idx] /= (double)total_cnt[idx];
     }
-    const int ixCenter2total = iAxisOffset ? (idifftotal + iAxisOffset) * 2 : idifftotal + ixdim - 1;
-    double dcentertotal = ixCenter2total / 2.;
-    if (idifftotal > -ixdimh && idifftotal < ixdimh - 1) {
-        const double dy1 = sdifftotal[idifftotal + ixdimh];
-        double dy0 = sdifftotal[idifftotal - 1 + ixdimh];
-        const double dy2 = sdifftotal[idifftotal + 1 + ixdimh];
-        if (dy2 != dy0) {
-            dy0 = (dy1 - dy0) / (dy2 - dy0);
-            dcentertotal = (4 * dy0 * ixCenter2total - (ixCenter2total * 2 - 1)) / (4 * dy0 - 2) / 2;
-        }
-    }
-    dcentertotal -= 0.5;
-    // least-squares line over rows within 3 px of the overall centre (:4558-4586); the
-    // reference's int products wrap on tall frames, reproduced with unsigned arithmetic
-    const double cavg = dcentertotal, csig = 1;
-    int isig1 = 0, isig2 = 0, nsig = 0;
-    double sigc = 0, sigcx = 0;
+    const int best_total = argmin_shift<double>(total_sum, total_valid, ixdimh);
+    const double overall = refined_centre(total_sum, ixdimh, best_total, iAxisOffset, ixdim) - 0.5;
+    // a line through the rows whose centre lies within 3 px of the overall one (:4558-4586)
+    AxisLineFit fit;
     for (int k = 0; k < iydim; k += istep) {
-        const int icidx = k / istep;
-        if (fabs(cavg - center[icidx]) > csig * 3) continue;
-        isig1 += k;
-        isig2 = (int)((unsigned)isig2 + (unsigned)k * (unsigned)k);
-        sigc += center[icidx];
-        sigcx += k * center[icidx];
-        nsig++;
+        const double c = center[k / istep];
+        if (!(fabs(overall - c) > 3)) fit.add(k, c);
     }
-    const int den = (int)((unsigned)nsig * (unsigned)isig2 - (unsigned)isig1 * (unsigned)isig1);
-    double coeffb = (isig2 * sigc - isig1 * sigcx) / den;
-    double coeffa = (sigc - nsig * coeffb) / isig1;
-    if (nsig < iydim / istep / 2) {
-        isig1 = 1;
-        coeffb = dcentertotal;
-        coeffa = 0;
+    double intercept, slope;
+    const bool use_line = fit.solve(iydim / istep / 2, &intercept, &slope);
+    if (use_line && !(intercept < 0)) {
+        *pCenter = intercept;
+        *pGrad = slope;
     } else {
-        isig1 = 0;
-    }
-    if ((coeffb < 0) || isig1) {
-        *pCenter = dcentertotal;
+        *pCenter = overall;
         *pGrad = 0;
-    } else {
-        *pCenter = coeffb;
-        *pGrad = coeffa;
     }
-    if (pOverall) *pOverall = dcentertotal;
+    if (pOverall) *pOverall = overall;
     return 0;
 }
 
