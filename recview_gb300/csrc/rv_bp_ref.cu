@@ -429,6 +429,46 @@ __device__ __forceinline__ void pipe_init_barriers(int* smi) {
     }
 }
 
+// The record of one view for a TX x TY tile at (X0, Y0): geometry, the table window the tile can
+// touch (start aligned to ALIGN, length a multiple of 4 words, at most WIN), the in-table part of
+// that window (nstore = table words per view slot) and the fast-path byte offset.
+template <int TX, int TY, int WIN, int ALIGN, int PAD>
+__device__ __forceinline__ ViewMeta view_window(float4 gg, int X0, int Y0, int nstore) {
+    float lo = 3.0e38f, hi = -3.0e38f;
+#pragma unroll
+    for (int cy = 0; cy < 2; cy++) {
+        const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), gg.y), gg.z);
+#pragma unroll
+        for (int cx = 0; cx < 2; cx++) {
+            const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), gg.x), fy);
+            lo = fminf(lo, fx);
+            hi = fmaxf(hi, fx);
+        }
+    }
+    const int ilo = (int)floorf(lo) - 2;
+    const int lo_a = ilo >= 0 ? (ilo & ~(ALIGN - 1)) : -((-ilo + ALIGN - 1) & ~(ALIGN - 1));
+    const int ihi = (int)floorf(hi) + 3;
+    ViewMeta m;
+    if (PAD) {
+        const int hi16 = (ihi + 15) & ~15;
+        m.w0 = lo_a + lo_a / 16;
+        const int w1 = hi16 + hi16 / 16;
+        m.nwin = min(((w1 - m.w0) + 3) & ~3, WIN);
+    } else {
+        m.w0 = lo_a;
+        m.nwin = min(((ihi - lo_a) + 3) & ~3, WIN);
+    }
+    m.a = max(m.w0, 0);
+    m.b = min(m.w0 + m.nwin, nstore);
+    const bool fast = lo >= 2.0f;
+    m.gc = gg.x;
+    m.gs = gg.y;
+    m.go = gg.z;
+    const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
+    m.off = (0u - 4u * (unsigned)m.w0 - (fast ? 4u * mag : 0u)) | (fast ? 1u : 0u);
+    return m;
+}
+
 // Warp 0 of a pipelined CTA: fill buffer g % NB with the table windows of chunk c (views
 // c*VC ..) once that buffer's empty barrier shows every warp is done with it.  Records each view's
 // geometry and window in meta, zero-fills the parts of a window outside the table, and issues one
@@ -450,42 +490,7 @@ __device__ __forceinline__ bool pipe_fill(const TileJob& J, int* win, ViewMeta* 
         return false;
     const int v0 = c * VC;
     const int nv = min(VC, nviews - v0);
-    if (lane < nv) {
-        const float4 gg = __ldg(J.geom + v0 + lane);
-        float lo = 3.0e38f, hi = -3.0e38f;
-#pragma unroll
-        for (int cy = 0; cy < 2; cy++) {
-            const float fy = faddr(fmulr((float)(Y0 + cy * (TY - 1)), gg.y), gg.z);
-#pragma unroll
-            for (int cx = 0; cx < 2; cx++) {
-                const float fx = faddr(fmulr((float)(X0 + cx * (TX - 1)), gg.x), fy);
-                lo = fminf(lo, fx);
-                hi = fmaxf(hi, fx);
-            }
-        }
-        const int ilo = (int)floorf(lo) - 2;
-        const int lo_a = ilo >= 0 ? (ilo & ~(ALIGN - 1)) : -((-ilo + ALIGN - 1) & ~(ALIGN - 1));
-        const int ihi = (int)floorf(hi) + 3;
-        ViewMeta m;
-        if (PAD) {
-            const int hi16 = (ihi + 15) & ~15;
-            m.w0 = lo_a + lo_a / 16;
-            const int w1 = hi16 + hi16 / 16;
-            m.nwin = min(((w1 - m.w0) + 3) & ~3, WIN);
-        } else {
-            m.w0 = lo_a;
-            m.nwin = min(((ihi - lo_a) + 3) & ~3, WIN);
-        }
-        m.a = max(m.w0, 0);
-        m.b = min(m.w0 + m.nwin, nstore);
-        const bool fast = lo >= 2.0f;
-        m.gc = gg.x;
-        m.gs = gg.y;
-        m.go = gg.z;
-        const unsigned mag = PAD ? (kMagicBits + (kMagicBits >> 4)) : kMagicBits;
-        m.off = (0u - 4u * (unsigned)m.w0 - (fast ? 4u * mag : 0u)) | (fast ? 1u : 0u);
-        meta[b * VC + lane] = m;
-    }
+    if (lane < nv) meta[b * VC + lane] = view_window<TX, TY, WIN, ALIGN, PAD>(__ldg(J.geom + v0 + lane), X0, Y0, nstore);
     __syncwarp();
     for (int vv = 0; vv < nv; vv++) {
         const ViewMeta m = meta[b * VC + vv];
@@ -736,6 +741,56 @@ __device__ __forceinline__ void consumers_bar() {
     asm volatile("bar.sync 1, %0;" ::"n"(32 * CW) : "memory");
 }
 
+// The producer warp of a warp-specialised CTA: publish chunk c's view records m (lane vv holds
+// view vv's, computed before this call) in buffer g % NB once its empty barrier shows every
+// consumer is done with it, zero-fill the window parts outside the table (edge tiles only), and
+// issue the bulk copies -- lane vv those of view vv -- on the buffer's full barrier.  Only the
+// record stores and the copy issue remain after the empty barrier; the geometry loads and the
+// window arithmetic of the next chunk run while the consumers still read the buffer.  Returns
+// false (warp-uniform) when the bounded wait ran out.
+template <int WIN, int VC, int NB, int NS, int NSL>
+__device__ __forceinline__ bool ws_fill(const TileJob& J, int* win, ViewMeta* meta, uint64_t* bars, int v0, int nv,
+                                        unsigned g, int lane, const ViewMeta& m, long long slice_tab_stride) {
+    const int b = (int)(g % NB);
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
+        return false;
+    const bool mine = lane < nv;
+    if (mine) meta[b * VC + lane] = m;
+    unsigned edges = __ballot_sync(0xffffffffu, mine && !(m.a == m.w0 && m.b == m.w0 + m.nwin));
+    while (edges) {   // warp-uniform
+        const int vv = __ffs(edges) - 1;
+        edges &= edges - 1;
+        const int w0 = __shfl_sync(0xffffffffu, m.w0, vv), nwin = __shfl_sync(0xffffffffu, m.nwin, vv);
+        const int a = __shfl_sync(0xffffffffu, m.a, vv), e1 = __shfl_sync(0xffffffffu, m.b, vv);
+        const int za = (e1 > a) ? (a - w0) >> 2 : nwin >> 2;
+        const int zb = (e1 > a) ? (e1 - w0) >> 2 : nwin >> 2;
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) {
+            int4* w4 = reinterpret_cast<int4*>(win + ((b * VC + vv) * NSL + sl) * WIN);
+            for (int e = lane; e < za; e += 32) w4[e] = make_int4(0, 0, 0, 0);
+            for (int e = zb + lane; e < (nwin >> 2); e += 32) w4[e] = make_int4(0, 0, 0, 0);
+        }
+    }
+    const bool copy = mine && m.b > m.a;
+    const unsigned bytes = __reduce_add_sync(0xffffffffu, copy ? 4u * NS * (unsigned)(m.b - m.a) : 0u);
+    // the records and zero fills are ordered before the barrier's completion, and every
+    // lane's generic accesses to the buffer before its own copies into it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncwarp();
+    const unsigned bar = smem_u32(&bars[b]);
+    if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+    __syncwarp();
+    if (copy) {
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) {
+            const int* src = J.table + sl * slice_tab_stride + (size_t)(v0 + lane) * J.table_stride + m.a;
+            const unsigned dst = smem_u32(win + ((b * VC + lane) * NSL + sl) * WIN + (m.a - m.w0));
+            tma_bulk_g2s(dst, src, 4u * (unsigned)(m.b - m.a), bar);
+        }
+    }
+    return true;
+}
+
 template <int VC, int NB, int PAD, int NS = 1, int CW = 8>
 struct WsCfg {
     using Pipe = PipeCfg<2, 4, 4, 4, VC, NB, PAD>;   // 64x64 tile: the same window size
@@ -746,7 +801,7 @@ struct WsCfg {
     static constexpr int BAR_OFF = META_OFF + NB * VC * 8;   // view records [NB][VC]
     static constexpr int ABORT_OFF = BAR_OFF + 4 * NB;       // after full[NB], empty[NB]
     static constexpr size_t SMEM = (size_t)ABORT_OFF * 4 + 16;
-    static constexpr bool EXCHANGE_FITS = VC * WIN >= 4096;   // one buffer holds a slice's exchange
+    static constexpr bool EXCHANGE_FITS = VC * NS * WIN >= 4096;   // one buffer holds a slice's exchange
     static_assert(TX == 64 && TY == 64 && (CW == 8 || CW == 16), "8 or 16 consumer warps tile 64x64 pixels");
 };
 
@@ -877,9 +932,6 @@ __device__ __forceinline__ void ws_gather(int (&acc)[NS][S], const int* win, con
     }
 }
 
-// one chunk of views: NQ == 0 compact blocks (8 consumer warps; colf/rowf in lin[0..3] /
-// lin[4..7]), else the ray layout of orientation O.  Products and y terms are scalar
-// (fl(x fcos), fl(fl(y fsin) + foffset)); the per-pixel sums are paired.
 // Two views at once (both on the fast path): each pixel's two gathers are added in one
 // three-operand integer add.
 template <int WIN, int PAD, int NS, int S, typename FA, typename FB>
@@ -905,15 +957,64 @@ __device__ __forceinline__ void ws_gather_two(int (&acc)[NS][S], unsigned baseA,
     }
 }
 
+// Two fast-path views (records g, g2; windows at baseA, baseB) of a ray layout of orientation O.
+template <int O, int WIN, int PAD, int NS, int Q>
+__device__ __forceinline__ void ws_view_pair(int (&acc)[NS][2 * Q], const float (&lin)[Q], const float (&fix)[2],
+                                             float4 g, float4 g2, unsigned baseA, unsigned baseB) {
+    constexpr int S = 2 * Q;
+    if (O == 0) {   // V: x = lin[q], y = fix[p]
+        float2 XA[Q / 2], XB[Q / 2];
+#pragma unroll
+        for (int k = 0; k < Q / 2; k++) {
+            XA[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
+            XB[k] = make_float2(fmulr(lin[2 * k], g2.x), fmulr(lin[2 * k + 1], g2.x));
+        }
+        const float2 YA0 = bcast2(faddr(fmulr(fix[0], g.y), g.z)), YA1 = bcast2(faddr(fmulr(fix[1], g.y), g.z));
+        const float2 YB0 = bcast2(faddr(fmulr(fix[0], g2.y), g2.z)), YB1 = bcast2(faddr(fmulr(fix[1], g2.y), g2.z));
+        ws_gather_two<WIN, PAD, NS, S>(acc, baseA, baseB,
+                                       [&](int i) { return add2_rn(XA[i >> 1], (i & 1) ? YA1 : YA0); },
+                                       [&](int i) { return add2_rn(XB[i >> 1], (i & 1) ? YB1 : YB0); });
+    } else {   // H: x = fix[p], y = lin[q]
+        float2 YA[Q / 2], YB[Q / 2];
+#pragma unroll
+        for (int k = 0; k < Q / 2; k++) {
+            YA[k] = make_float2(faddr(fmulr(lin[2 * k], g.y), g.z), faddr(fmulr(lin[2 * k + 1], g.y), g.z));
+            YB[k] = make_float2(faddr(fmulr(lin[2 * k], g2.y), g2.z), faddr(fmulr(lin[2 * k + 1], g2.y), g2.z));
+        }
+        const float2 XA0 = bcast2(fmulr(fix[0], g.x)), XA1 = bcast2(fmulr(fix[1], g.x));
+        const float2 XB0 = bcast2(fmulr(fix[0], g2.x)), XB1 = bcast2(fmulr(fix[1], g2.x));
+        ws_gather_two<WIN, PAD, NS, S>(acc, baseA, baseB,
+                                       [&](int i) { return add2_rn((i & 1) ? XA1 : XA0, YA[i >> 1]); },
+                                       [&](int i) { return add2_rn((i & 1) ? XB1 : XB0, YB[i >> 1]); });
+    }
+}
+
 // one chunk of views: NQ == 0 compact blocks (8 consumer warps; colf/rowf in lin[0..3] /
 // lin[4..7]), else the ray layout of orientation O.  Products and y terms are scalar
 // (fl(x fcos), fl(fl(y fsin) + foffset)); the per-pixel sums are paired.  Ray layouts take two
-// fast-path views at a time where they can.
+// fast-path views at a time where they can; a full chunk whose views are all on the fast path
+// (the common case) runs as straight-line code, with one test per chunk.
 template <int NQ, int O, int VC, int WIN, int PAD, bool CHECKED, int NS, int NSL, int CW>
 __device__ __forceinline__ void ws_consume(int (&acc)[NS][128 / CW], const float (&lin)[64 / CW],
                                            const float (&fix)[2], const int* win, const ViewMeta* meta, int b,
                                            int nv, unsigned& viol) {
     constexpr int Q = 64 / CW, S = 2 * Q;
+    if (NQ > 0 && !CHECKED && VC % 2 == 0 && nv == VC) {
+        unsigned all = 1u;
+#pragma unroll
+        for (int vv = 0; vv < VC; vv++) all &= meta[b * VC + vv].off;
+        if (all & 1u) {
+#pragma unroll 1
+            for (int vv = 0; vv < VC; vv += 2) {
+                const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
+                const float4 g2 = *reinterpret_cast<const float4*>(&meta[b * VC + vv + 1]);
+                const unsigned baseA = smem_u32(win + (b * VC + vv) * NSL * WIN) + (__float_as_uint(g.w) & ~3u);
+                const unsigned baseB = smem_u32(win + (b * VC + vv + 1) * NSL * WIN) + (__float_as_uint(g2.w) & ~3u);
+                ws_view_pair<O, WIN, PAD, NS, Q>(acc, lin, fix, g, g2, baseA, baseB);
+            }
+            return;
+        }
+    }
     for (int vv = 0; vv < nv; vv++) {
         const float4 g = *reinterpret_cast<const float4*>(&meta[b * VC + vv]);
         const unsigned offb = __float_as_uint(g.w);
@@ -923,31 +1024,7 @@ __device__ __forceinline__ void ws_consume(int (&acc)[NS][128 / CW], const float
             if (offb & offb2 & 1u) {
                 const unsigned baseA = smem_u32(win + (b * VC + vv) * NSL * WIN) + (offb & ~3u);
                 const unsigned baseB = smem_u32(win + (b * VC + vv + 1) * NSL * WIN) + (offb2 & ~3u);
-                if (O == 0) {   // V: x = lin[q], y = fix[p]
-                    float2 XA[Q / 2], XB[Q / 2];
-#pragma unroll
-                    for (int k = 0; k < Q / 2; k++) {
-                        XA[k] = make_float2(fmulr(lin[2 * k], g.x), fmulr(lin[2 * k + 1], g.x));
-                        XB[k] = make_float2(fmulr(lin[2 * k], g2.x), fmulr(lin[2 * k + 1], g2.x));
-                    }
-                    const float2 YA0 = bcast2(faddr(fmulr(fix[0], g.y), g.z)), YA1 = bcast2(faddr(fmulr(fix[1], g.y), g.z));
-                    const float2 YB0 = bcast2(faddr(fmulr(fix[0], g2.y), g2.z)), YB1 = bcast2(faddr(fmulr(fix[1], g2.y), g2.z));
-                    ws_gather_two<WIN, PAD, NS, S>(acc, baseA, baseB,
-                                                   [&](int i) { return add2_rn(XA[i >> 1], (i & 1) ? YA1 : YA0); },
-                                                   [&](int i) { return add2_rn(XB[i >> 1], (i & 1) ? YB1 : YB0); });
-                } else {   // H: x = fix[p], y = lin[q]
-                    float2 YA[Q / 2], YB[Q / 2];
-#pragma unroll
-                    for (int k = 0; k < Q / 2; k++) {
-                        YA[k] = make_float2(faddr(fmulr(lin[2 * k], g.y), g.z), faddr(fmulr(lin[2 * k + 1], g.y), g.z));
-                        YB[k] = make_float2(faddr(fmulr(lin[2 * k], g2.y), g2.z), faddr(fmulr(lin[2 * k + 1], g2.y), g2.z));
-                    }
-                    const float2 XA0 = bcast2(fmulr(fix[0], g.x)), XA1 = bcast2(fmulr(fix[1], g.x));
-                    const float2 XB0 = bcast2(fmulr(fix[0], g2.x)), XB1 = bcast2(fmulr(fix[1], g2.x));
-                    ws_gather_two<WIN, PAD, NS, S>(acc, baseA, baseB,
-                                                   [&](int i) { return add2_rn((i & 1) ? XA1 : XA0, YA[i >> 1]); },
-                                                   [&](int i) { return add2_rn((i & 1) ? XB1 : XB0, YB[i >> 1]); });
-                }
+                ws_view_pair<O, WIN, PAD, NS, Q>(acc, lin, fix, g, g2, baseA, baseB);
                 vv++;
                 continue;
             }
@@ -1018,13 +1095,18 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
     bool failed = false;   // warp-uniform
     int produced = 0;      // producer: chunks of this tile whose fill has been issued
     if (warp == CW) {
+        const int nstore = PAD ? ((17 * ixdimp + 3) & ~3) : 16 * ixdimp;
+        float4 gg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);   // this chunk's records, lane vv: view vv
+        if (nchunks > 0 && lane < min(VC, nviews)) gg = __ldg(J.geom + lane);
         for (; produced < nchunks; produced++) {
             if (__any_sync(0xffffffffu, *abortw != 0)) {
                 failed = true;
                 break;
             }
-            if (!pipe_fill<64, 64, WIN, Cfg::ALIGN, VC, NB, PAD, NS, NSL>(J, win, meta, bars, produced,
-                                                                          gc + (unsigned)produced, lane, tstride)) {
+            const int v0 = produced * VC, nv = min(VC, nviews - v0);
+            const ViewMeta m = view_window<64, 64, WIN, Cfg::ALIGN, PAD>(gg, X0, Y0, nstore);
+            if (lane < min(VC, nviews - v0 - VC)) gg = __ldg(J.geom + v0 + VC + lane);
+            if (!ws_fill<WIN, VC, NB, NS, NSL>(J, win, meta, bars, v0, nv, gc + (unsigned)produced, lane, m, tstride)) {
                 failed = true;
                 if (lane == 0) *abortw = 1;
                 break;
@@ -1083,27 +1165,34 @@ __device__ __forceinline__ bool bp_ref_tile_ws(const TileJob& J, int* smi, unsig
                         failed = true;
                         break;
                     }
-                    int* xs = win + b * VC * NSL * WIN;   // [NS][S slots][NC threads]
-#pragma unroll
-                    for (int sl = 0; sl < NS; sl++)
-#pragma unroll
-                        for (int s = 0; s < S; s++) xs[(sl * S + s) * NC + tid] = acc[sl][s];
-                    consumers_bar<CW>();
+                    // [slices of a round][S slots][NC threads]: all NS slices in one round when the
+                    // buffer holds them, else one slice per round
+                    int* xs = win + b * VC * NSL * WIN;
+                    constexpr int XR = VC * NSL * WIN >= NS * S * NC ? NS : 1;
                     const int on = next & 1, oo = regime & 1;
                     const int shn = ray_shift<NQ>(lane, next);
 #pragma unroll
-                    for (int q = 0; q < Q; q++)
+                    for (int r0 = 0; r0 < NS; r0 += XR) {
+                        if (r0 > 0) consumers_bar<CW>();   // the previous round's reads are done
 #pragma unroll
-                        for (int p = 0; p < 2; p++) {
-                            const int u = (warp + shn + CW * q) & 63, f = lane + 32 * p;   // new layout
-                            const int xr = on ? f : u, yr = on ? u : f;
-                            const int a = oo ? xr : yr, c = oo ? yr : xr;                   // old fixed / sheared
-                            const int jj = a & 31, pp = a >> 5;
-                            const int m = (c - ray_shift<NQ>(jj, regime)) & 63;              // old w + CW q
-                            const int src = ((m / CW) * 2 + pp) * NC + (m % CW) * 32 + jj;
+                        for (int sl = r0; sl < r0 + XR; sl++)
 #pragma unroll
-                            for (int sl = 0; sl < NS; sl++) acc[sl][2 * q + p] = xs[sl * S * NC + src];
-                        }
+                            for (int s = 0; s < S; s++) xs[((sl - r0) * S + s) * NC + tid] = acc[sl][s];
+                        consumers_bar<CW>();
+#pragma unroll
+                        for (int q = 0; q < Q; q++)
+#pragma unroll
+                            for (int p = 0; p < 2; p++) {
+                                const int u = (warp + shn + CW * q) & 63, f = lane + 32 * p;   // new layout
+                                const int xr = on ? f : u, yr = on ? u : f;
+                                const int a = oo ? xr : yr, c = oo ? yr : xr;                   // old fixed / sheared
+                                const int jj = a & 31, pp = a >> 5;
+                                const int m = (c - ray_shift<NQ>(jj, regime)) & 63;              // old w + CW q
+                                const int src = ((m / CW) * 2 + pp) * NC + (m % CW) * 32 + jj;
+#pragma unroll
+                                for (int sl = r0; sl < r0 + XR; sl++) acc[sl][2 * q + p] = xs[(sl - r0) * S * NC + src];
+                            }
+                    }
                     regime = next;
                     ray_coords<NQ, CW>(regime, X0, Y0, warp, lane, lin, fix);
                     // these generic accesses come before the next TMA fill of buffer b
@@ -1316,49 +1405,65 @@ __device__ __forceinline__ LinTile lin_tile(const BackprojLaunch& p, int TX, int
     return t;
 }
 
-// One warp fills buffer c % NB with the pair windows of chunk c (views c*VC ..) once that
-// buffer's empty barrier shows every consumer is done with it; false (warp-uniform) when that
-// bounded wait ran out.
+// The LIN record of view v: its FP64 geometry and the scales of its NS slices (slice sl's scales
+// follow at sl * nviews).
 template <typename Cfg>
-__device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, ViewMeta* meta, uint64_t* bars, int c,
-                                         int lane, float* scl = nullptr) {
-    constexpr int NB = Cfg::NB_, VC = Cfg::VC_, TX = Cfg::TX, TY = Cfg::TY, WINP = Cfg::WINP, ES = Cfg::ES;
-    constexpr int NS = Cfg::NS_;
+__device__ __forceinline__ void lin_load(const LinTile& T, int v, LinGeom& gg, float (&sc)[Cfg::NS_]) {
+    gg = T.geom[v];
+#pragma unroll
+    for (int sl = 0; sl < Cfg::NS_; sl++) sc[sl] = T.scales ? T.scales[(size_t)sl * T.nviews + v] : 1.0f;
+}
+// The window record of a view for the tile: u at the tile origin in FP64 (two FMAs); the tile's
+// lowest u adds the negative parts of the tile's extent, which FP32 gives well inside the
+// window's 2-pixel margin.  sc0: slice 0's scale (kept in the record's fourth word).
+template <typename Cfg>
+__device__ __forceinline__ ViewMeta lin_record(const LinTile& T, const LinGeom& gg, float sc0) {
+    constexpr int TX = Cfg::TX, TY = Cfg::TY, WINP = Cfg::WINP;
+    const double base = fma((double)T.X0, gg.c, fma((double)T.Y0, gg.s, gg.off));
+    const float lo = (float)base + fminf(0.0f, (float)(TX - 1) * (float)gg.c) + fminf(0.0f, (float)(TY - 1) * (float)gg.s);
+    const int ilo = (int)floorf(lo) - 2;
+    const int w0 = ilo >= 0 ? (ilo & ~3) : -((-ilo + 3) & ~3);
+    ViewMeta m;
+    m.w0 = w0;
+    m.nwin = WINP;
+    m.a = max(w0, 0);
+    m.b = min(w0 + WINP, (T.ixdimp + 3) & ~3);
+    m.gc = (float)gg.c;
+    m.gs = (float)gg.s;
+    m.go = (float)(base - (double)w0);   // window-relative u at the tile origin
+    m.off = __float_as_uint(sc0);
+    return m;
+}
+
+// Publish chunk c's records (lane vv: view vv's record m and slice scales sc) in buffer c % NB
+// once its empty barrier shows every consumer is done with it, zero-fill the window parts outside
+// the rows (edge tiles only), and issue the bulk copies -- lane vv those of view vv -- on the
+// buffer's full barrier.  False (warp-uniform) when the bounded wait ran out.
+template <typename Cfg>
+__device__ __forceinline__ bool lin_publish(const LinTile& T, unsigned char* smb, ViewMeta* meta, uint64_t* bars,
+                                            int c, int lane, int nv, const ViewMeta& m,
+                                            const float (&sc)[Cfg::NS_], float* scl) {
+    constexpr int NB = Cfg::NB_, VC = Cfg::VC_, ES = Cfg::ES, NS = Cfg::NS_;
     const unsigned g = (unsigned)c;
     const int b = (int)(g % NB);
     if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&bars[NB + b]), ((g / NB) & 1u) ^ 1u)))
         return false;
     const int v0 = c * VC;
-    const int nv = min(VC, T.nviews - v0);
-    if (lane < nv) {
-        const LinGeom gg = T.geom[v0 + lane];
-        // u at the tile origin in FP64 (two FMAs); the tile's lowest u adds the negative parts of
-        // the tile's extent, which FP32 gives well inside the window's 2-pixel margin
-        const double base = fma((double)T.X0, gg.c, fma((double)T.Y0, gg.s, gg.off));
-        const float lo = (float)base + fminf(0.0f, (float)(TX - 1) * (float)gg.c) + fminf(0.0f, (float)(TY - 1) * (float)gg.s);
-        const int ilo = (int)floorf(lo) - 2;
-        const int w0 = ilo >= 0 ? (ilo & ~3) : -((-ilo + 3) & ~3);
-        ViewMeta m;
-        m.w0 = w0;
-        m.nwin = WINP;
-        m.a = max(w0, 0);
-        m.b = min(w0 + WINP, (T.ixdimp + 3) & ~3);
-        m.gc = (float)gg.c;
-        m.gs = (float)gg.s;
-        m.go = (float)(base - (double)w0);   // window-relative u at the tile origin
-        m.off = __float_as_uint(T.scales ? T.scales[v0 + lane] : 1.0f);
+    const bool mine = lane < nv;
+    if (mine) {
         meta[b * VC + lane] = m;
-        if (NS > 1 && scl) {   // every slice's scale of this view (slice sl's scales follow at sl * nviews)
+        if (NS > 1 && scl) {
 #pragma unroll
-            for (int sl = 0; sl < NS; sl++)
-                scl[(b * VC + lane) * NS + sl] = T.scales ? T.scales[(size_t)sl * T.nviews + v0 + lane] : 1.0f;
+            for (int sl = 0; sl < NS; sl++) scl[(b * VC + lane) * NS + sl] = sc[sl];
         }
     }
-    __syncwarp();
-    for (int vv = 0; vv < nv; vv++) {
-        const ViewMeta m = meta[b * VC + vv];
-        if (m.a == m.w0 && m.b == m.w0 + m.nwin) continue;
-        const int bytes_a = (m.b > m.a ? m.a - m.w0 : m.nwin) * ES, bytes_b = (m.b > m.a ? m.b - m.w0 : m.nwin) * ES;
+    unsigned edges = __ballot_sync(0xffffffffu, mine && !(m.a == m.w0 && m.b == m.w0 + m.nwin));
+    while (edges) {   // warp-uniform
+        const int vv = __ffs(edges) - 1;
+        edges &= edges - 1;
+        const int w0 = __shfl_sync(0xffffffffu, m.w0, vv), nwin = __shfl_sync(0xffffffffu, m.nwin, vv);
+        const int a = __shfl_sync(0xffffffffu, m.a, vv), e1 = __shfl_sync(0xffffffffu, m.b, vv);
+        const int bytes_a = (e1 > a ? a - w0 : nwin) * ES, bytes_b = (e1 > a ? e1 - w0 : nwin) * ES;
 #pragma unroll
         for (int sl = 0; sl < NS; sl++) {
             int4* w4 = reinterpret_cast<int4*>(smb + (size_t)((b * VC + vv) * NS + sl) * Cfg::WIN_BYTES);
@@ -1366,33 +1471,42 @@ __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, V
             for (int e = bytes_b / 16 + lane; e < Cfg::WIN_BYTES / 16; e += 32) w4[e] = make_int4(0, 0, 0, 0);
         }
     }
+    const bool copy = mine && m.b > m.a;
+    const unsigned bytes = __reduce_add_sync(0xffffffffu, copy ? (unsigned)(NS * (m.b - m.a) * ES) : 0u);
+    // the records and zero fills are ordered before the barrier's completion, and every lane's
+    // generic accesses to the buffer before its own copies into it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncwarp();
-    if (lane == 0) {
-        unsigned bytes = 0;
-        for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[b * VC + vv];
-            if (m.b > m.a) bytes += (unsigned)(NS * (m.b - m.a) * ES);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const unsigned bar = smem_u32(&bars[b]);
-        mbar_arrive_expect_tx(bar, bytes);
-        for (int vv = 0; vv < nv; vv++) {
-            const ViewMeta m = meta[b * VC + vv];
-            if (m.b <= m.a) continue;
+    const unsigned bar = smem_u32(&bars[b]);
+    if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+    __syncwarp();
+    if (copy) {
 #pragma unroll
-            for (int sl = 0; sl < NS; sl++) {
-                const unsigned char* src = T.rows + sl * T.slice_row_bytes + ((size_t)(v0 + vv) * T.row_stride + m.a) * ES;
-                const unsigned dst = smem_u32(smb + (size_t)((b * VC + vv) * NS + sl) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
-                tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
-            }
+        for (int sl = 0; sl < NS; sl++) {
+            const unsigned char* src = T.rows + sl * T.slice_row_bytes + ((size_t)(v0 + lane) * T.row_stride + m.a) * ES;
+            const unsigned dst = smem_u32(smb + (size_t)((b * VC + lane) * NS + sl) * Cfg::WIN_BYTES + (m.a - m.w0) * ES);
+            tma_bulk_g2s(dst, src, (unsigned)((m.b - m.a) * ES), bar);
         }
     }
-    __syncwarp();
     return true;
 }
 
-// acc += the interpolated, scaled row value of every pixel of the thread, for the nv views of
-// buffer b
+// One warp fills buffer c % NB with the pair windows of chunk c (views c*VC ..): records, then
+// lin_publish.  False (warp-uniform) when the bounded wait ran out.
+template <typename Cfg>
+__device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, ViewMeta* meta, uint64_t* bars, int c,
+                                         int lane, float* scl = nullptr) {
+    const int v0 = c * Cfg::VC_;
+    const int nv = min(Cfg::VC_, T.nviews - v0);
+    LinGeom gg{};
+    float sc[Cfg::NS_];
+#pragma unroll
+    for (int sl = 0; sl < Cfg::NS_; sl++) sc[sl] = 1.0f;
+    if (lane < nv) lin_load<Cfg>(T, v0 + lane, gg, sc);
+    const ViewMeta m = lin_record<Cfg>(T, gg, sc[0]);
+    return lin_publish<Cfg>(T, smb, meta, bars, c, lane, nv, m, sc, scl);
+}
+
 // one slice's update of a pixel: acc += (scaled) r + f * slope, from the pair at addr + sl windows
 template <typename Cfg, int MODE, int SL>
 __device__ __forceinline__ void lin_slice(float& acc, unsigned addr, float f, float sc) {
@@ -1548,9 +1662,21 @@ __global__ void __launch_bounds__(288, MINB) k_bp_lin_ws(BackprojLaunch p, int s
     bool failed = false;
     int produced = 0;
     if (warp == 8) {
+        // the records of chunk produced + 1 are loaded while chunk produced waits for its buffer
+        LinGeom gg{};
+        float sc[NS];
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) sc[sl] = 1.0f;
+        if (nchunks > 0 && lane < min(VC, T.nviews)) lin_load<Cfg>(T, lane, gg, sc);
         for (; produced < nchunks; produced++) {
             if (__any_sync(0xffffffffu, *abortw != 0)) { failed = true; break; }
-            if (!lin_fill<Cfg>(T, smb, meta, bars, produced, lane, scl)) {
+            const int v0 = produced * VC, nv = min(VC, T.nviews - v0);
+            const ViewMeta m = lin_record<Cfg>(T, gg, sc[0]);
+            float cur[NS];
+#pragma unroll
+            for (int sl = 0; sl < NS; sl++) cur[sl] = sc[sl];
+            if (lane < min(VC, T.nviews - v0 - VC)) lin_load<Cfg>(T, v0 + VC + lane, gg, sc);
+            if (!lin_publish<Cfg>(T, smb, meta, bars, produced, lane, nv, m, cur, scl)) {
                 failed = true;
                 if (lane == 0) *abortw = 1;
                 break;
