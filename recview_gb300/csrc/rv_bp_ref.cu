@@ -1363,6 +1363,24 @@ __device__ __forceinline__ float2 lin_pair(unsigned addr) {
     }
 }
 
+// BF16 rows are stored unscaled: acc += r + f * slope as a mixed-precision FMA and add (BF16
+// operands, FP32 arithmetic and result, one rounding each), with the fraction f rounded to BF16
+// once per pixel -- three instructions per slice-update with the gather, as the FP32 form.
+__device__ __forceinline__ unsigned short bf16_bits(float f) {
+    unsigned short h;
+    asm("cvt.rn.bf16.f32 %0, %1;" : "=h"(h) : "f"(f));
+    return h;
+}
+template <int OFF>
+__device__ __forceinline__ void lin_add_bf16(float& acc, unsigned addr, unsigned short fb) {
+    unsigned w;
+    asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(w) : "r"(addr), "n"(OFF));
+    asm("{\n .reg .b16 r, d;\n .reg .f32 t;\n mov.b32 {r, d}, %1;\n fma.rn.f32.bf16 t, d, %2, %3;\n"
+        " add.rn.f32.bf16 %0, r, t;\n}\n"
+        : "=f"(acc)
+        : "r"(w), "h"(fb), "f"(acc));
+}
+
 // NS windows per view (slices that share the geometry, one after the other), NS scales per view
 template <int WX, int WY, int RX, int RY, int VC, int NB, int MODE, int NS = 1>
 struct LinCfg {
@@ -1509,7 +1527,11 @@ __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, V
 
 // one slice's update of a pixel: acc += (scaled) r + f * slope, from the pair at addr + sl windows
 template <typename Cfg, int MODE, int SL>
-__device__ __forceinline__ void lin_slice(float& acc, unsigned addr, float f, float sc) {
+__device__ __forceinline__ void lin_slice(float& acc, unsigned addr, float f, float sc, unsigned short fb) {
+    if (MODE == RV_MODE_LIN_BF16) {
+        lin_add_bf16<SL * Cfg::WIN_BYTES>(acc, addr, fb);
+        return;
+    }
     const float2 q = lin_pair<MODE, SL * Cfg::WIN_BYTES>(addr);
     const float v = fmaf(f, q.y, q.x);
     if (MODE == RV_MODE_LIN) acc += v;
@@ -1546,10 +1568,11 @@ __device__ __forceinline__ void lin_consume(float (&acc)[Cfg::NS_][Cfg::RY_][Cfg
                 const unsigned bits = __float_as_uint(t);
                 const float f = u - (t - 8388608.0f);
                 const unsigned a = base + (unsigned)ES * bits;
-                lin_slice<Cfg, MODE, 0>(acc[0][r][c], a, f, sc[0]);
-                if (NS > 1) lin_slice<Cfg, MODE, (NS > 1 ? 1 : 0)>(acc[1 % NS][r][c], a, f, sc[1 % NS]);
-                if (NS > 2) lin_slice<Cfg, MODE, (NS > 2 ? 2 : 0)>(acc[2 % NS][r][c], a, f, sc[2 % NS]);
-                if (NS > 3) lin_slice<Cfg, MODE, (NS > 3 ? 3 : 0)>(acc[3 % NS][r][c], a, f, sc[3 % NS]);
+                const unsigned short fb = MODE == RV_MODE_LIN_BF16 ? bf16_bits(f) : (unsigned short)0;
+                lin_slice<Cfg, MODE, 0>(acc[0][r][c], a, f, sc[0], fb);
+                if (NS > 1) lin_slice<Cfg, MODE, (NS > 1 ? 1 : 0)>(acc[1 % NS][r][c], a, f, sc[1 % NS], fb);
+                if (NS > 2) lin_slice<Cfg, MODE, (NS > 2 ? 2 : 0)>(acc[2 % NS][r][c], a, f, sc[2 % NS], fb);
+                if (NS > 3) lin_slice<Cfg, MODE, (NS > 3 ? 3 : 0)>(acc[3 % NS][r][c], a, f, sc[3 % NS], fb);
             }
     }
 }

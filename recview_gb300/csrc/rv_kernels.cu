@@ -591,10 +591,12 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
     }
     if (p.rows16) {
         // LIN forms: pairs (r[j], r[j+1] - r[j]) of r = q * 100 (slope 0 at the last sample, zero
-        // pairs up to the padded stride), FP32 or -- with a per-row scale max |r| / 16384 that keeps
-        // FP16 far from overflow -- FP16 / BF16
+        // pairs up to the padded stride), FP32, FP16 with a per-row scale max |r| / 16384 that
+        // keeps it far from overflow, or BF16 unscaled (it has FP32's exponent range; its scale
+        // is 1)
         float scale = 1.0f, rs = 1.0f;
-        if (p.mode != RV_MODE_LIN) {
+        if (p.mode == RV_MODE_LIN_BF16 && tid == 0) p.row_scale[job.dst] = 1.0f;
+        if (p.mode == RV_MODE_LIN_F16) {
             __shared__ float red[32];
             float m = 0.0f;
             for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(re[rbase - j]));
