@@ -516,7 +516,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             from recview_gb300 import centre as cs
             net = cs.CentreNet(batch=1)
             net.set_params(np.fromfile(NET_FILE, dtype=np.float32))
-            summ = centre_evaluate(net, 8, np.random.default_rng(args.seed + 1))
+            summ = centre_evaluate(net, CENTRE_SCANS, np.random.default_rng(args.seed + 1))
             net.close()
             summ.pop("disagreements", None)
             line["centre_search"] = {"metric": "centre_search_s", "unit": "s/dataset", "value": summ.pop("learned_s"),
@@ -675,6 +675,11 @@ def queue_summary(dev, seed: int) -> dict:
 
 
 NET_FILE = ROOT / "recview_gb300" / "data" / "centre_net_256x512.f32"
+
+
+# fresh scans the default run's centre-search summary evaluates (about 0.2 s each); the
+# centre workload (--workload centre --datasets N) runs larger evaluations
+CENTRE_SCANS = 100
 
 
 def centre_evaluate(net, n: int, rng) -> dict:

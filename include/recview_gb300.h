@@ -365,7 +365,7 @@ int RvQueueCreate(RvQueue** out);
 int RvQueueAdd(RvQueue* q, const RvStackDesc* desc, const void* d_raw, void* d_out);
 int RvQueueAutotune(RvQueue* q, void* stream, int* chosen_variant);
 int RvQueueItemVariant(const RvQueue* q, int item);   /* -1 for a bad index */
-/* Pins dataset `item` to a back-projection variant (0-20), overriding the tuned choice. */
+/* Pins dataset `item` to a back-projection variant (0-21), overriding the tuned choice. */
 int RvQueueSetItemVariant(RvQueue* q, int item, int variant);
 int RvQueueRun(RvQueue* q, void* stream);
 float RvQueueLastMs(const RvQueue* q);        /* device time of the last run */
@@ -396,14 +396,15 @@ int RvCentreSweep(const short* sino, int nviews, int ixdim, int iInterpolation, 
  * afterwards).  format: 0 = the reference's 16-int table per detector pixel, 1 = the same padded
  * to 17 words (fewer shared-memory bank conflicts), 2 = the float pair (p0, slope) per
  * detector pixel, expanded by the kernel with the reference's operations (8x smaller tables,
- * conflict-free lookups).  variant 0..20 selects tile shape / threads / views per chunk, and
+ * conflict-free lookups).  variant 0..21 selects tile shape / threads / views per chunk, and
  * whether the per-view coordinate products are tabulated in shared memory (0-5) or formed in
- * registers (6-20), whether warps synchronise per chunk (0-8) or only wait for their data
- * (9-20), whether a dedicated warp stages the tables (16-20), whether each warp register
+ * registers (6-21), whether warps synchronise per chunk (0-8) or only wait for their data
+ * (9-21), whether a dedicated warp stages the tables (16-21), whether each warp register
  * covers a compact 8x4 pixel block (0-15, 17) or 32 pixels along the view's ray direction,
- * re-laid per angle range (16, 18-20), and how many slices that share the geometry a CTA
- * reconstructs with one index computation per pixel and view (18, 19: two; 20: four; 19 and
- * 20 with 16 consumer warps) (default: format 0, variant 18).  All combinations give
+ * re-laid per angle range (16, 18-21), and how many slices that share the geometry a CTA
+ * reconstructs with one index computation per pixel and view (18, 19: two; 21: three, the rest
+ * of a stack as pairs; 20: four; 19 and 20 with 16 consumer warps) (default: format 0,
+ * variant 21).  All combinations give
  * bit-identical slices.  Returns RV_ERR_BAD_ARGUMENT outside these ranges. */
 int RvSetBackprojectionVariant(int variant, int format);
 int RvGetBackprojectionVariant(int* variant, int* format);

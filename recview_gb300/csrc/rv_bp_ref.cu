@@ -2043,6 +2043,8 @@ __global__ void __launch_bounds__(32 * WX * WY, MINB) k_bp_pair(BackprojLaunch p
 //         2 buffers x 4 views x 2 slices, 2 CTAs/SM;  19: variant 18 with 16 consumer warps
 //         (8 pixels x 2 slices per thread);  20: four slices per CTA sharing the index, 16
 //         consumer warps (8 pixels x 4 slices per thread), 2 buffers x 4 views x 4 slices, 1 CTA/SM
+//     21: three slices per CTA sharing the index (16 pixels x 3 slices per thread), 2 buffers x
+//         3 views x 3 slices, 2 CTAs/SM; the rest of a stack as slice pairs (the default)
 //   pair tables (format 2):
 //     0: 128x128 tile, 512 threads, 16 views/chunk  1: 64x128, 256 threads, 2 CTAs/SM
 //     2: 128x64, 512 threads, 16 px/thread, 2 CTAs/SM
@@ -2052,7 +2054,7 @@ static int env_int(const char* name, int dflt) {
 }
 static int g_variant = -1, g_fmt = -1;
 static void load_defaults() {
-    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 18);
+    if (g_variant < 0) g_variant = env_int("RV_BP_VARIANT", 21);
     if (g_fmt < 0) g_fmt = env_int("RV_BP_FORMAT", kTabInt16);
 }
 int ref_table_fmt() {
@@ -2186,6 +2188,21 @@ static cudaError_t go_ws_quads(const BackprojLaunch& p, cudaStream_t s, bool che
     return e;
 }
 
+// groups of three slices per CTA (one index per pixel and view, three gathers), the rest as
+// slice pairs: n = 3t, 3t + 2 (one pair) or 3(t - 1) + 4 (two pairs); fewer than three slices,
+// or per-slice geometry, go to the pair form
+template <int VC, int NB, int PAD, int NQ, int MINB, int CW = 8>
+static cudaError_t go_ws_triples(const BackprojLaunch& p, cudaStream_t s, bool checked) {
+    if (p.geom_slice_stride != 0 || p.nslices < 3) return go_ws_pairs<4, 2, PAD, 12, 2>(p, s, checked);
+    int t3 = p.nslices / 3;
+    if (p.nslices % 3 == 1) t3--;
+    cudaError_t e = t3 > 0 ? go_ws_rows<VC, NB, PAD, NQ, MINB, 3, CW>(p, s, checked, 0, t3) : cudaSuccess;
+    const int rest = p.nslices - 3 * t3;
+    if (e == cudaSuccess && rest >= 2) e = go_ws_rows<4, 2, PAD, 12, 2, 2>(p, s, checked, 3 * t3, rest / 2);
+    if (e == cudaSuccess && (rest & 1)) e = go_ws_rows<6, 2, PAD, 12, 3>(p, s, checked, p.nslices - 1, 1);
+    return e;
+}
+
 template <int WX, int WY, int RX, int RY, int VC, int MINB>
 static cudaError_t go_pair(const BackprojLaunch& p, cudaStream_t s, bool checked) {
     using Cfg = PairCfg<WX, WY, RX, RY, VC>;
@@ -2217,6 +2234,7 @@ static cudaError_t dispatch_bp(const BackprojLaunch& p, cudaStream_t s, bool che
     case 17: return go_ws<4, 2, PAD, 0, 4>(p, s, checked);
     case 18: return go_ws_pairs<4, 2, PAD, 12, 2>(p, s, checked);
     case 19: return go_ws_pairs<4, 2, PAD, 8, 2, 16>(p, s, checked);
+    case 21: return go_ws_triples<3, 2, PAD, 12, 2>(p, s, checked);
     case 20: return go_ws_quads<4, 2, PAD, 8, 1, 16>(p, s, checked);
     default: return go_bp<4, 4, 4, 8, 8, PAD, 1>(p, s, checked);
     }
@@ -2324,6 +2342,7 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 18: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);
     case 19: return go_ws_persistent<4, 2, PAD, 8, 2, 2, 16>(jobs, njobs, counter, s);
     case 20: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);
+    case 21: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);   // pair jobs
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }
@@ -2446,7 +2465,7 @@ extern "C" int RvSetCheckedBackprojection(int enable) {
 extern "C" unsigned long long RvGetWindowViolations(void) { return rv::g_violations; }
 
 extern "C" int RvSetBackprojectionVariant(int variant, int format) {
-    if (variant < 0 || variant > 20 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
+    if (variant < 0 || variant > 21 || format < 0 || format > 2) return RV_ERR_BAD_ARGUMENT;
     rv::g_variant = variant;
     rv::g_fmt = format;
     return 0;

@@ -678,7 +678,7 @@ static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
             persistent_tile_xy(var, &tx, &ty);
             // the slice-pair kernels take two consecutive slices of a part per job (they share
             // the geometry and their tables follow each other in the pool)
-            const int step = (var >= 18 && var <= 20) ? 2 : 1;
+            const int step = (var >= 18 && var <= 21) ? 2 : 1;
             for (const Part& pt : parts) {
                 if (pt.variant != var) continue;
                 RvStack* st = q->items[pt.item].st;
@@ -904,8 +904,9 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
 }
 
 extern "C" int RvQueueSetItemVariant(RvQueue* q, int item, int variant) {
-    // every int-table variant 0..20 has a persistent form
-    if (!q || item < 0 || item >= (int)q->items.size() || variant < 0 || variant > 20) return RV_ERR_BAD_ARGUMENT;
+    // every int-table variant 0..21 has a persistent form (21, three slices per CTA in a stack, runs
+    // the queue's slice pairs as 18 does)
+    if (!q || item < 0 || item >= (int)q->items.size() || variant < 0 || variant > 21) return RV_ERR_BAD_ARGUMENT;
     q->items[item].variant = variant;
     q->release_plan();
     return 0;

@@ -2,7 +2,8 @@
 raw uint16 frames (Poisson counts of an ellipsoid phantom on a smooth flat field, a dark field
 ~N(100, 3)), rotation centre 1023.5 + U[-10, 10] px, Shepp-Logan filter.  This is the path the
 throughput figure is measured on: RvStackRunDevice / RvStackRunHost, the fused normalise + filter
-kernel, and the default back-projection on slice pairs (plus a single slice for an odd count).
+kernel, and the default back-projection on groups of three slices (the rest of a stack as slice
+pairs).
 Every slice must equal the oracle (the reference CPU routine restated) bit for bit."""
 import ctypes as C
 import os
@@ -42,7 +43,7 @@ def _oracle_slices(oracle, raw, bInc, fdeg, fexp, cen, F, S):
 
 @pytest.fixture(scope="module")
 def headline(oracle):
-    S = 3   # one slice pair and one single slice
+    S = 5   # one group of three slices and one slice pair
     raw, bInc, fdeg, fexp, cen = _case(2026, S)
     F = oracle.set_filter(abi.FILT_SHEPP, dims(W).ndim)
     want = _oracle_slices(oracle, raw, bInc, fdeg, fexp, cen, F, S)
@@ -52,7 +53,7 @@ def headline(oracle):
 def test_headline_uses_default_variant(gpu):
     v, f = C.c_int(), C.c_int()
     gpu.RvGetBackprojectionVariant(C.byref(v), C.byref(f))
-    assert (v.value, f.value) == (18, 0)   # slice pairs, dense 16-entry tables: what the bench times
+    assert (v.value, f.value) == (21, 0)   # three-slice groups, dense 16-entry tables: what the bench times
 
 
 def test_headline_stack_host_bit_exact(gpu, headline):
@@ -89,7 +90,7 @@ def test_headline_window_bound_checked(gpu, headline):
     """The bounds-checked twin of the default back-projection at the full geometry: no table
     index falls outside the staged window, and the slices are still the oracle's."""
     raw, bInc, fdeg, fexp, cen, F, want = headline
-    S = 2
+    S = 3   # one group of three slices
     raw2 = np.ascontiguousarray(raw[:, :S, :])
     L = rv.lib()
     assert L.RvSetCheckedBackprojection(1) == 0
@@ -101,6 +102,6 @@ def test_headline_window_bound_checked(gpu, headline):
         assert L.RvGetWindowViolations() == 0
     finally:
         L.RvSetCheckedBackprojection(0)
-    # slices 0 and 1 of a 2-row stack are the same detector rows as in the 3-row one
+    # the slices of a 3-row stack are the same detector rows as the first three of the 5-row one
     for s in range(S):
         assert np.array_equal(got[s], want[s])

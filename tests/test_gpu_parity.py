@@ -159,7 +159,7 @@ def test_progress_callback_abort(gpu, oracle):
     assert np.array_equal(got, oracle.reconstruct(ri2))
 
 
-@pytest.fixture(params=[(v, f) for f in (0, 1, 2) for v in range(21)], ids=lambda v: f"variant{v[0]}fmt{v[1]}")
+@pytest.fixture(params=[(v, f) for f in (0, 1, 2) for v in range(22)], ids=lambda v: f"variant{v[0]}fmt{v[1]}")
 def bp_variant(request, gpu):
     """Every back-projection variant and table format; restores the default afterwards."""
     L = rv.lib()

@@ -77,15 +77,15 @@ def test_queue_matches_oracle(gpu, datasets, monkeypatch, budget_mb, autotune, p
         if autotune:
             chosen = C.c_int(-1)
             assert L.RvQueueAutotune(q, None, C.byref(chosen)) == 0, rv.last_error()
-            assert 0 <= chosen.value <= 20
+            assert 0 <= chosen.value <= 21
             assert L.RvQueueItemVariant(q, 0) == chosen.value
             for i in range(len(datasets)):
-                assert 0 <= L.RvQueueItemVariant(q, i) <= 20
+                assert 0 <= L.RvQueueItemVariant(q, i) <= 21
         if pinned:   # datasets on different variants: one persistent launch per variant and wave
             for i, v in enumerate(pinned):
                 assert L.RvQueueSetItemVariant(q, i, v) == 0
                 assert L.RvQueueItemVariant(q, i) == v
-            assert L.RvQueueSetItemVariant(q, 0, 21) == abi.RV_ERR_BAD_ARGUMENT
+            assert L.RvQueueSetItemVariant(q, 0, 22) == abi.RV_ERR_BAD_ARGUMENT
             assert L.RvQueueItemVariant(q, len(datasets)) == -1
         for run in range(2):   # first run captures the graph, second replays it
             for d_out, _ in outs:
