@@ -384,18 +384,31 @@ static int ensure_host_buffers(RvStack* st, size_t in_b, size_t out_b) {
     return 0;
 }
 
+// Slices per piece of the host pipeline: about S / 16 (RV_STACK_PIECES pieces), rounded up to
+// whole slice groups of the default back-projection (three slices per CTA for variant 21, else
+// two), at most one table batch.  Pieces never straddle two table batches (slots s mod batch):
+// each batch is cut into pieces of this size, its last piece possibly shorter.
 static int piece_slices(const RvStack* st) {
     int pieces = 16;
     if (const char* e = getenv("RV_STACK_PIECES")) pieces = atoi(e);
     const int S = st->desc.nslices;
     if (pieces < 1) pieces = 1;
     int p = (S + pieces - 1) / pieces;
+    const int g = default_variant() == 21 ? 3 : 2;
+    p = (p + g - 1) / g * g;
     if (p > st->batch) p = st->batch;
     if (p < 1) p = 1;
-    // an even piece runs entirely as slice pairs in the back-projection
-    if ((p & 1) && p > 1 && p + 1 <= st->batch && st->batch % (p + 1) == 0) p++;
-    while (st->batch % p) p--;   // a piece never straddles two table batches (slots s mod batch)
     return p;
+}
+// piece k: slices [*s0, *s0 + *nb) (nb = 0 past the end); ppw pieces per table batch
+static void piece_range(const RvStack* st, int P, int ppw, int k, int* s0, int* nb) {
+    const int S = st->desc.nslices;
+    const int w = k / ppw, j = k % ppw;
+    *s0 = w * st->batch + j * P;
+    int n = P;
+    if (j * P + n > st->batch) n = st->batch - j * P;
+    if (*s0 + n > S) n = S - *s0;
+    *nb = n > 0 ? n : 0;
 }
 
 extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void* stream) {
@@ -411,7 +424,12 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
     int rc = ensure_host_buffers(st, in_b, slice_b * S);
     if (rc) return rc;
     const int P = piece_slices(st);
-    const int npieces = (S + P - 1) / P;
+    const int ppw = (st->batch + P - 1) / P;   // pieces per table batch; piece k reuses piece k - ppw's slots
+    int npieces = 0;
+    for (int s0 = 0, nb = 1; nb > 0; npieces++) {
+        piece_range(st, P, ppw, npieces, &s0, &nb);
+        if (nb == 0) break;
+    }
     // events: start, per piece {in copied, filter start, filter end, bp end, out copied}, end
     const size_t need = 2 + 5 * (size_t)npieces;
     while (st->pev.size() < need) {
@@ -427,9 +445,10 @@ extern "C" int RvStackRunHost(RvStack* st, const void* h_raw, void* h_out, void*
     cudaStreamWaitEvent(st->cs_out, E[0], 0);
     cudaStreamWaitEvent(st->cs_alt, E[0], 0);
     const size_t pitch = (size_t)S * W * 2;
-    const int reuse = st->batch / P;   // pieces later a piece's table slots come round again
+    const int reuse = ppw;   // pieces later a piece's table slots come round again
     for (int k = 0; k < npieces; k++) {
-        const int s0 = k * P, nb = (S - s0) < P ? (S - s0) : P;
+        int s0 = 0, nb = 0;
+        piece_range(st, P, ppw, k, &s0, &nb);
         cudaEvent_t* e = E + 1 + 5 * (size_t)k;
         const char* src = static_cast<const char*>(h_raw) + (size_t)s0 * W * 2;
         char* dst = static_cast<char*>(st->d_in) + (size_t)s0 * W * 2;
@@ -856,11 +875,12 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
     // and in every dataset of the class
     if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
-    // candidates spanning the tuned dimensions: 64x64 tiles with slice pairs and 4-view chunks
-    // (18), the same with 16 consumer warps (19), single slices with 6-view chunks (16), compact
+    // candidates spanning the tuned dimensions: 64x64 tiles with slice groups (21: slice pairs
+    // and 4-view chunks in the persistent kernel, three-slice groups in the grid launches of large
+    // groups), the same with 16 consumer warps (19), single slices with 6-view chunks (16), compact
     // lane blocks (17), warp-0-produced pipelines with 4- and 5-view chunks (11, 14), 128x128 and
     // 128x64 tiles (0, 4)
-    const int cands[] = {18, 19, 16, 17, 11, 14, 0, 4};
+    const int cands[] = {21, 19, 16, 17, 11, 14, 0, 4};
     std::map<unsigned, int> tuned;
     for (int it = 0; it < (int)q->items.size(); it++) {
         const unsigned key = shape_key(q->items[it].st, q->fmt);
