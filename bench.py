@@ -42,9 +42,10 @@ W_DET, N_VIEWS, N_SLICES = 2048, 1800, 64
 PUBLISHED_TAU_NS = 0.029  # RTX A4000, 2048^2 x 1800 views (reference README, Build-220422)
 WORKLOAD = "fbp-2048det-1800views-64slices-raw-uint16"
 # DRAM bytes (read + write) per pixel-view update of the REF back-projection, from one ncu capture
-# of the default variant on 2 slices of this geometry; the traffic grows in proportion to the
-# slices processed, so a full launch moves this times its updates.
-BP_DRAM_BYTES_PER_UPDATE = 6.768e-2
+# of the default variant (three slices per CTA) on 3 slices of this geometry: 2.42 GB + 398 MB
+# over 2.265e10 updates; the traffic grows in proportion to the slices processed, so a full
+# launch moves this times its updates.
+BP_DRAM_BYTES_PER_UPDATE = 1.244e-1
 
 
 def parse():
