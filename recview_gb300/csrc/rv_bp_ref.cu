@@ -38,6 +38,8 @@
 namespace rv {
 
 __device__ unsigned int g_kernel_status = 0;   // bit 0: an mbarrier wait ran out
+// back-projection kernels launched on this host thread since take_backproject_launches()
+static thread_local int t_bp_launches = 0;
 static int env_int(const char* name, int dflt);  // tuning overrides from the environment
 
 constexpr unsigned kMagicBits = 0x4B000000u;   // bit pattern of 2^23
@@ -1751,6 +1753,7 @@ static cudaError_t go_lin(const BackprojLaunch& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
     kern<<<dim3(tiles, p.nslices), Cfg::NT, Cfg::SMEM, s>>>(p);
+    t_bp_launches++;
     return cudaGetLastError();
 }
 
@@ -1762,6 +1765,7 @@ static cudaError_t go_lin_ws_rows(const BackprojLaunch& p, cudaStream_t s, int s
     if (e != cudaSuccess) return e;
     const int tiles = ((p.ixdimp + Cfg::TX - 1) / Cfg::TX) * ((p.ixdimp + Cfg::TY - 1) / Cfg::TY);
     kern<<<dim3(tiles, rows), 288, Cfg::SMEM_WS, s>>>(p, slice0);
+    t_bp_launches++;
     return cudaGetLastError();
 }
 
@@ -2116,6 +2120,7 @@ static cudaError_t launch_k(K kern, dim3 grid, int nt, size_t smem, const Backpr
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, nt, smem, s>>>(p);
+    t_bp_launches++;
     return cudaGetLastError();
 }
 
@@ -2175,6 +2180,7 @@ static cudaError_t go_ws_rows(const BackprojLaunch& p, cudaStream_t s, bool chec
         if (e != cudaSuccess) return e;
     }
     kern<<<dim3(tiles, rows, groups), Cfg::NT, Cfg::SMEM, s>>>(p, slice0);
+    t_bp_launches++;
     return cudaGetLastError();
 }
 
@@ -2375,6 +2381,11 @@ cudaError_t launch_bp_ref_persistent(const TileJob* d_jobs, int njobs, unsigned*
 int default_variant() {
     load_defaults();
     return g_variant;
+}
+int take_backproject_launches() {
+    const int n = t_bp_launches;
+    t_bp_launches = 0;
+    return n;
 }
 
 cudaError_t launch_bp_ref(const BackprojLaunch& pin, cudaStream_t s) {

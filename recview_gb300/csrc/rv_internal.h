@@ -119,6 +119,8 @@ struct BackprojLaunch {
     unsigned int* status_counter;  // validation mode: window-violation counter (else null)
 };
 cudaError_t launch_backproject(const BackprojLaunch& p, cudaStream_t s);
+// kernels launch_backproject started on this host thread since the previous call (then resets)
+int take_backproject_launches();
 
 // One tile of one slice for the persistent REF back-projection (batched queue).
 struct TileJob {

@@ -311,10 +311,11 @@ static int run_slices(RvStack* st, const void* d_raw, void* d_out, int s0, int n
     bl.out_slice_stride = (long long)npix;
     bl.mode = mode;
     bl.table_fmt = st->tfmt;
+    take_backproject_launches();
     e = launch_backproject(bl, s);
     if (!cuda_ok(e, RV_ERR_LAUNCH, "back-projection kernel")) return RV_ERR_LAUNCH;
     if (ev_c) cudaEventRecord(ev_c, s);
-    st->launches += 2;
+    st->launches += kernel_launches_per_filter() + take_backproject_launches();
     return 0;
 }
 

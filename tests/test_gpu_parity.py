@@ -267,7 +267,8 @@ def test_stack_host_pipeline_pieces(gpu, oracle, monkeypatch, pieces, budget_mb)
     for _ in range(2):                       # a second call reuses buffers, streams and events
         got = st.run_host(raw)
         assert np.array_equal(got, want)
-    assert st.launches() >= 2 and st.launches() % 2 == 0     # a filter and a back-projection per piece
+    # per piece a filter and one back-projection launch per slice-group form (triples, pairs)
+    assert 2 <= st.launches() <= 3 * pieces
     st.close()
 
 
