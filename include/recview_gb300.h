@@ -234,7 +234,9 @@ int RvGetDims(int ixdim, int iInterpolation, RvDims* out);
 /* Reconstruction modes. */
 #define RV_MODE_REF 0   /* reference semantics: 1/16 sub-sample int table, int32 slices (bit-exact) */
 #define RV_MODE_LIN 1   /* linear interpolation, FP32 filtered rows, FP32 slices */
-#define RV_MODE_LIN_F16 2  /* as LIN, filtered rows stored as FP16 with a per-row scale */
+#define RV_MODE_LIN_F16 2  /* as LIN, filtered rows stored as FP16 under one power-of-two scale per filter
+                              (bounded from the filter table), the interpolation as FP32 fma/add on the FP16
+                              operands */
 #define RV_MODE_LIN_BF16 3 /* as LIN, filtered rows stored as BF16 (unscaled: FP32's exponent range), the
                               interpolation as FP32 fma/add on the BF16 operands */
 

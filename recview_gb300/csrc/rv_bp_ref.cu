@@ -1365,22 +1365,32 @@ __device__ __forceinline__ float2 lin_pair(unsigned addr) {
     }
 }
 
-// BF16 rows are stored unscaled: acc += r + f * slope as a mixed-precision FMA and add (BF16
-// operands, FP32 arithmetic and result, one rounding each), with the fraction f rounded to BF16
-// once per pixel -- three instructions per slice-update with the gather, as the FP32 form.
-__device__ __forceinline__ unsigned short bf16_bits(float f) {
+// 16-bit rows: acc += r + f * slope as a mixed-precision FMA and add (16-bit operands, FP32
+// arithmetic and result, one rounding each), with the fraction f rounded to the row format once
+// per pixel -- three instructions per slice-update with the gather, as the FP32 form.  BF16 rows
+// are stored unscaled; FP16 rows carry one power-of-two scale per filter, applied exactly to the
+// finished sums (lin_store).
+template <int MODE>
+__device__ __forceinline__ unsigned short half_bits(float f) {
     unsigned short h;
-    asm("cvt.rn.bf16.f32 %0, %1;" : "=h"(h) : "f"(f));
+    if (MODE == RV_MODE_LIN_BF16) asm("cvt.rn.bf16.f32 %0, %1;" : "=h"(h) : "f"(f));
+    else asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h) : "f"(f));
     return h;
 }
-template <int OFF>
-__device__ __forceinline__ void lin_add_bf16(float& acc, unsigned addr, unsigned short fb) {
+template <int MODE, int OFF>
+__device__ __forceinline__ void lin_add_half(float& acc, unsigned addr, unsigned short fb) {
     unsigned w;
     asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(w) : "r"(addr), "n"(OFF));
-    asm("{\n .reg .b16 r, d;\n .reg .f32 t;\n mov.b32 {r, d}, %1;\n fma.rn.f32.bf16 t, d, %2, %3;\n"
-        " add.rn.f32.bf16 %0, r, t;\n}\n"
-        : "=f"(acc)
-        : "r"(w), "h"(fb), "f"(acc));
+    if (MODE == RV_MODE_LIN_BF16)
+        asm("{\n .reg .b16 r, d;\n .reg .f32 t;\n mov.b32 {r, d}, %1;\n fma.rn.f32.bf16 t, d, %2, %3;\n"
+            " add.rn.f32.bf16 %0, r, t;\n}\n"
+            : "=f"(acc)
+            : "r"(w), "h"(fb), "f"(acc));
+    else
+        asm("{\n .reg .b16 r, d;\n .reg .f32 t;\n mov.b32 {r, d}, %1;\n fma.rn.f32.f16 t, d, %2, %3;\n"
+            " add.rn.f32.f16 %0, r, t;\n}\n"
+            : "=f"(acc)
+            : "r"(w), "h"(fb), "f"(acc));
 }
 
 // NS windows per view (slices that share the geometry, one after the other), NS scales per view
@@ -1530,8 +1540,8 @@ __device__ __forceinline__ bool lin_fill(const LinTile& T, unsigned char* smb, V
 // one slice's update of a pixel: acc += (scaled) r + f * slope, from the pair at addr + sl windows
 template <typename Cfg, int MODE, int SL>
 __device__ __forceinline__ void lin_slice(float& acc, unsigned addr, float f, float sc, unsigned short fb) {
-    if (MODE == RV_MODE_LIN_BF16) {
-        lin_add_bf16<SL * Cfg::WIN_BYTES>(acc, addr, fb);
+    if (MODE != RV_MODE_LIN) {
+        lin_add_half<MODE, SL * Cfg::WIN_BYTES>(acc, addr, fb);
         return;
     }
     const float2 q = lin_pair<MODE, SL * Cfg::WIN_BYTES>(addr);
@@ -1570,7 +1580,7 @@ __device__ __forceinline__ void lin_consume(float (&acc)[Cfg::NS_][Cfg::RY_][Cfg
                 const unsigned bits = __float_as_uint(t);
                 const float f = u - (t - 8388608.0f);
                 const unsigned a = base + (unsigned)ES * bits;
-                const unsigned short fb = MODE == RV_MODE_LIN_BF16 ? bf16_bits(f) : (unsigned short)0;
+                const unsigned short fb = MODE != RV_MODE_LIN ? half_bits<MODE>(f) : (unsigned short)0;
                 lin_slice<Cfg, MODE, 0>(acc[0][r][c], a, f, sc[0], fb);
                 if (NS > 1) lin_slice<Cfg, MODE, (NS > 1 ? 1 : 0)>(acc[1 % NS][r][c], a, f, sc[1 % NS], fb);
                 if (NS > 2) lin_slice<Cfg, MODE, (NS > 2 ? 2 : 0)>(acc[2 % NS][r][c], a, f, sc[2 % NS], fb);
@@ -1585,6 +1595,9 @@ __device__ __forceinline__ void lin_store(const BackprojLaunch& p, const LinTile
 #pragma unroll
     for (int sl = 0; sl < Cfg::NS_; sl++) {
         float* out = static_cast<float*>(p.out) + (size_t)(slice + sl) * p.out_slice_stride;
+        // FP16 sums are in units of the slice's power-of-two row scale (every row of a slice has
+        // the same one): scaling them is exact
+        const float sc = (p.mode == RV_MODE_LIN_F16 && T.scales) ? T.scales[(size_t)sl * T.nviews] : 1.0f;
 #pragma unroll
         for (int r = 0; r < Cfg::RY_; r++) {
             const int y = T.Y0 + ty + Cfg::GY * r;
@@ -1592,7 +1605,7 @@ __device__ __forceinline__ void lin_store(const BackprojLaunch& p, const LinTile
 #pragma unroll
             for (int c = 0; c < Cfg::RX_; c++) {
                 const int x = T.X0 + tx + Cfg::GX * c;
-                if (x < T.ixdimp) out[(size_t)y * T.ixdimp + x] = acc[sl][r][c];
+                if (x < T.ixdimp) out[(size_t)y * T.ixdimp + x] = acc[sl][r][c] * sc;
             }
         }
     }

@@ -83,8 +83,14 @@ struct FilterLaunch {
     long long raw_stride;
     int raw_x0;
     int bin;
+    float lin16_scale;        // FP16 rows: the power-of-two scale of every row (fp16_row_scale)
 };
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s);
+// The power-of-two scale that keeps every FP16 pair row of a filter table (ndim entries) below
+// 16384 for any int16 sinogram: |r| <= 100 * 32768 * sqrt(sum_k H[k]^2), H[k] = (F[k] + F[-k]) / 2
+// the filter's even part (the filtered row is a circular convolution of the placed row with a
+// kernel whose L1 norm that bounds, by Cauchy-Schwarz and Parseval).
+float fp16_row_scale(const float* filt, int ndim);
 // 1 when kernels on the current device may read and write pageable host memory directly (the
 // host's page tables are shared with the GPU, as on Grace-based systems); RV_NO_HOST_DIRECT=1
 // turns the direct paths off

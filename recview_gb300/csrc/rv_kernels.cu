@@ -591,29 +591,12 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
     }
     if (p.rows16) {
         // LIN forms: pairs (r[j], r[j+1] - r[j]) of r = q * 100 (slope 0 at the last sample, zero
-        // pairs up to the padded stride), FP32, FP16 with a per-row scale max |r| / 16384 that
-        // keeps it far from overflow, or BF16 unscaled (it has FP32's exponent range; its scale
-        // is 1)
-        float scale = 1.0f, rs = 1.0f;
-        if (p.mode == RV_MODE_LIN_BF16 && tid == 0) p.row_scale[job.dst] = 1.0f;
-        if (p.mode == RV_MODE_LIN_F16) {
-            __shared__ float red[32];
-            float m = 0.0f;
-            for (int j = tid; j < ixdimp; j += NT) m = fmaxf(m, fabsf(re[rbase - j]));
-            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-            if ((tid & 31) == 0) red[tid >> 5] = m;
-            __syncthreads();
-            if (tid < 32) {
-                m = (tid < (NT >> 5)) ? red[tid] : 0.0f;
-                for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-                if (tid == 0) red[0] = m;
-            }
-            __syncthreads();
-            const float amax = red[0] * inv_n * 100.0f;
-            scale = amax > 0.0f ? amax / 16384.0f : 1.0f;
-            rs = 1.0f / scale;
-            if (tid == 0) p.row_scale[job.dst] = scale;
-        }
+        // pairs up to the padded stride), FP32, FP16 scaled by the launch's power of two (exact;
+        // it keeps every row of the filter far from overflow), or BF16 unscaled (it has FP32's
+        // exponent range); row_scale holds the scale (1 for BF16)
+        const float scale = p.mode == RV_MODE_LIN_F16 ? p.lin16_scale : 1.0f;
+        const float rs = 1.0f / scale;   // exact: a power of two
+        if (p.mode != RV_MODE_LIN && tid == 0) p.row_scale[job.dst] = scale;
         const int ps = (int)p.row_stride;
         for (int j = tid; j < ps; j += NT) {
             float v0 = 0.0f, dv = 0.0f;
@@ -627,6 +610,18 @@ __global__ void __launch_bounds__(512, (BPT <= 4 ? 3 : (BPT == 8 ? 2 : 1))) k_fi
             else static_cast<__nv_bfloat162*>(p.rows16)[at] = __floats2bfloat162_rn(v0 * rs, dv * rs);
         }
     }
+}
+
+float fp16_row_scale(const float* filt, int ndim) {
+    double s2 = 0.0;
+    for (int k = 0; k < ndim; k++) {
+        const double h = 0.5 * ((double)filt[k] + (double)filt[(ndim - k) % ndim]);
+        s2 += h * h;
+    }
+    const double bound = 100.0 * 32768.0 * sqrt(s2);
+    int e = bound > 0.0 ? (int)ceil(log2(bound / 16384.0)) : 0;
+    e = e < -20 ? -20 : (e > 40 ? 40 : e);
+    return ldexpf(1.0f, e);
 }
 
 cudaError_t launch_filter(const FilterLaunch& p, cudaStream_t s) {

@@ -48,6 +48,7 @@ struct RvStack {
     cudaStream_t cs_alt = nullptr;                    // RunHost second compute stream
     std::vector<cudaEvent_t> pev;   // RunHost pipeline events
     int tfmt = 0;                   // REF table layout (ref_table_fmt at creation)
+    float lin16_scale = 1.0f;       // FP16 rows: the power-of-two row scale of this filter
     long long tstride = 0;          // ints per table slot
 };
 
@@ -167,6 +168,7 @@ static int stack_create(const RvStackDesc* desc, RvStack** out, bool alloc_table
         st->geom_lin[v] = LinGeom{c, sn, cen_lin - d.ixdimh * (c + sn), 0.0};
     }
     st->filt.assign(desc->fFilter, desc->fFilter + d.ndim);
+    st->lin16_scale = fp16_row_scale(st->filt.data(), d.ndim);
     // ---- batch size from the table budget ----------------------------------------------------
     size_t budget_mb = 32768;
     if (const char* e = getenv("RV_TABLE_BUDGET_MB")) budget_mb = (size_t)atoll(e);
@@ -283,6 +285,7 @@ static int run_slices(RvStack* st, const void* d_raw, void* d_out, int s0, int n
         fl.rows16 = st->d_table;
         fl.row_scale = static_cast<float*>(st->d_scale);
         fl.row_stride = lin_pair_stride(d.ixdimp);
+        fl.lin16_scale = st->lin16_scale;
     }
     // jobs of slice s write table slot (s mod batch): rebase so the first slice of this call
     // lands where its jobs point
