@@ -511,6 +511,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         if not args.no_forms and world == 1 and mode == abi.MODE_REF:
             line["forms"] = forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, ref64=ref64, ref_slice0=slice0)
             line["queue"] = queue_summary(dev, args.seed)
+            line["queue_small_datasets"] = queue_summary(dev, args.seed + 7, QUEUE_SMALL_SHAPES)
             line["dropin"] = dropin_summary(raw, bInc, fdeg, fexp, center, F)
         if not args.no_centre and world == 1 and NET_FILE.exists():
             # the centre-search part of the metric: the shipped network on fresh scans (C5 shapes)
@@ -597,7 +598,14 @@ def forms_summary(raw, bInc, fdeg, fexp, center, F, S, dev, steps: int = 3, ref6
     return out
 
 
-def queue_summary(dev, seed: int) -> dict:
+QUEUE_SHAPES = [(1024, 900, 8, 2), (1536, 1800, 4, 2), (2048, 1800, 4, 2), (4096, 900, 2, 2), (1024, 900, 4, 3),
+                (512, 1800, 4, 4)]
+# many small datasets (1024-pixel detector, 900 views, one slice pair each): one stack's
+# back-projection is 256 CTAs, under one wave, so a queue's shared work list can fill the GPU
+QUEUE_SMALL_SHAPES = [(1024, 900, 2, 2)] * 48
+
+
+def queue_summary(dev, seed: int, shapes=None) -> dict:
     """An uneven queue (configuration C3 shapes, scaled to seconds): widths 512-4096, 900/1800
     views, 1-8 slices, zoom x1/x2/x4 ROIs, run as one persistent kernel per wave in a captured graph,
     against the same datasets one stack at a time."""
@@ -606,8 +614,7 @@ def queue_summary(dev, seed: int) -> dict:
     from recview_gb300 import abi
     L = rv.lib()
     rng = np.random.default_rng(seed)
-    shapes = [(1024, 900, 8, 2), (1536, 1800, 4, 2), (2048, 1800, 4, 2), (4096, 900, 2, 2), (1024, 900, 4, 3),
-              (512, 1800, 4, 4)]
+    shapes = QUEUE_SHAPES if shapes is None else shapes
     data = []
     for i, (W, V, S, interp) in enumerate(shapes):
         deg = (np.arange(V) * (180.0 / V)).astype(np.float32)
