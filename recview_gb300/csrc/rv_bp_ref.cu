@@ -1319,7 +1319,10 @@ __global__ void __launch_bounds__(32 * CW + 32, MINB) k_bp_ref_ws_persistent(con
         if (it >= njobs) break;
         const TileJob J = jobs[it];
         bool ok;
-        if (NSL > 1 && J.pair)
+        if (NSL > 2 && J.pair >= 2)
+            ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, (NSL > 2 ? 3 : 1), NSL, CW>(
+                J, smi, gc, nullptr, (long long)J.nviews * J.table_stride, (long long)J.ixdimp * J.ixdimp);
+        else if (NSL > 1 && J.pair)
             ok = bp_ref_tile_ws<VC, NB, PAD, NQ, false, (NSL > 1 ? 2 : 1), NSL, CW>(
                 J, smi, gc, nullptr, (long long)J.nviews * J.table_stride, (long long)J.ixdimp * J.ixdimp);
         else
@@ -2379,7 +2382,7 @@ static cudaError_t dispatch_persistent(const TileJob* jobs, int njobs, unsigned*
     case 18: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);
     case 19: return go_ws_persistent<4, 2, PAD, 8, 2, 2, 16>(jobs, njobs, counter, s);
     case 20: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);
-    case 21: return go_ws_persistent<4, 2, PAD, 12, 2, 2>(jobs, njobs, counter, s);   // pair jobs
+    case 21: return go_ws_persistent<3, 2, PAD, 12, 2, 3>(jobs, njobs, counter, s);   // triple and pair jobs
     case 17: return go_ws_persistent<4, 2, PAD, 0, 4>(jobs, njobs, counter, s);
     default: return go_persistent<2, 4, 4, 4, 4, PAD, 4>(jobs, njobs, counter, s);
     }

@@ -135,8 +135,9 @@ struct TileJob {
     int* out;                 // the slice (ixdimp^2 int32)
     long long table_stride;
     int nviews, ixdimp, X0, Y0;
-    int pair;                 // 1: also the next slice (tables at table + nviews * table_stride,
-                              // output at out + ixdimp^2), which shares the geometry
+    int pair;                 // 1 or 2: also the next 1 or 2 slices (slice k's tables at table +
+                              // k * nviews * table_stride, output at out + k * ixdimp^2), which
+                              // share the geometry
     int accumulate;           // 1: add the tile's sums into out atomically (a group of views of
                               // the slice; out zeroed before), 0: store them
 };

@@ -699,9 +699,10 @@ static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
             g.tile_begin = (int)tiles.size();
             int tx = 64, ty = 64;
             persistent_tile_xy(var, &tx, &ty);
-            // the slice-pair kernels take two consecutive slices of a part per job (they share
-            // the geometry and their tables follow each other in the pool)
-            const int step = (var >= 18 && var <= 21) ? 2 : 1;
+            // the slice-group kernels take two (18-20) or three (21, the rest of a part as pairs)
+            // consecutive slices of a part per job: they share the geometry and their tables
+            // follow each other in the pool
+            const int group = (var >= 18 && var <= 20) ? 2 : (var == 21 ? 3 : 1);
             for (const Part& pt : parts) {
                 if (pt.variant != var) continue;
                 RvStack* st = q->items[pt.item].st;
@@ -709,7 +710,15 @@ static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
                 const long long ts = ref_table_stride(st->d.ixdimp, q->fmt);
                 const size_t npix = (size_t)st->d.ixdimp * st->d.ixdimp;
                 const int ntx = (st->d.ixdimp + tx - 1) / tx, nty = (st->d.ixdimp + ty - 1) / ty;
-                for (int sl = pt.s0; sl < pt.s1; sl += step)
+                // slices per job: groups of `group`, a triple part's rest as pairs (n = 3t,
+                // 3t + 2, 3(t - 1) + 4), a single slice only when the part has one
+                const int n = pt.s1 - pt.s0;
+                int t3 = group == 3 ? n / 3 : 0;
+                if (group == 3 && n % 3 == 1 && t3 > 0) t3--;
+                for (int sl = pt.s0, step = 1; sl < pt.s1; sl += step) {
+                    const int done = sl - pt.s0;
+                    step = group == 3 ? (done < 3 * t3 ? 3 : 2) : group;
+                    if (step > pt.s1 - sl) step = pt.s1 - sl;
                     for (int t = 0; t < ntx * nty; t++) {
                         TileJob J{};
                         J.table = reinterpret_cast<const int*>((pt.off + (size_t)(sl - pt.s0) * V * ts) * 4);
@@ -720,9 +729,10 @@ static int queue_build_reqs(RvQueue* q, const std::vector<QueueReq>& reqs) {
                         J.ixdimp = st->d.ixdimp;
                         J.X0 = (t % ntx) * tx;
                         J.Y0 = (t / ntx) * ty;
-                        J.pair = (step == 2 && sl + 1 < pt.s1) ? 1 : 0;
+                        J.pair = step - 1;
                         tiles.push_back(J);
                     }
+                }
                 q->total_updates += (double)(pt.s1 - pt.s0) * V * npix;
             }
             g.ntiles = (int)tiles.size() - g.tile_begin;
