@@ -889,9 +889,9 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
     // and in every dataset of the class
     if (!q || q->items.empty()) return RV_ERR_BAD_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
-    // candidates spanning the tuned dimensions: 64x64 tiles with slice groups (21: slice pairs
-    // and 4-view chunks in the persistent kernel, three-slice groups in the grid launches of large
-    // groups), the same with 16 consumer warps (19), single slices with 6-view chunks (16), compact
+    // candidates spanning the tuned dimensions: 64x64 tiles with three-slice groups and 3-view
+    // chunks (21; the rest of a dataset as pairs), slice pairs with 16 consumer warps (19), single
+    // slices with 6-view chunks (16), compact
     // lane blocks (17), warp-0-produced pipelines with 4- and 5-view chunks (11, 14), 128x128 and
     // 128x64 tiles (0, 4)
     const int cands[] = {21, 19, 16, 17, 11, 14, 0, 4};
@@ -938,8 +938,7 @@ extern "C" int RvQueueAutotune(RvQueue* q, void* stream, int* chosen) {
 }
 
 extern "C" int RvQueueSetItemVariant(RvQueue* q, int item, int variant) {
-    // every int-table variant 0..21 has a persistent form (21, three slices per CTA in a stack, runs
-    // the queue's slice pairs as 18 does)
+    // every int-table variant 0..21 has a persistent form
     if (!q || item < 0 || item >= (int)q->items.size() || variant < 0 || variant > 21) return RV_ERR_BAD_ARGUMENT;
     q->items[item].variant = variant;
     q->release_plan();
