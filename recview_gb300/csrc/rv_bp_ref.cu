@@ -870,6 +870,11 @@ __device__ __forceinline__ float2 add2_rz(float2 a, float2 b) {
     asm("add.rz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
     return upk2(d);
 }
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
 
 // slot of half h of slot pair i.  Ray layouts: slot 2q + p, pairs (q, q+1) at even q;
 // compact (8 consumer warps): slot 4r + c, pairs (c, c+1)
@@ -1567,27 +1572,36 @@ __device__ __forceinline__ void lin_consume(float (&acc)[Cfg::NS_][Cfg::RY_][Cfg
         sc[0] = __uint_as_float(__float_as_uint(gm.w));
 #pragma unroll
         for (int sl = 1; sl < NS; sl++) sc[sl] = scl[(b * VC + vv) * NS + sl];
-        float xv[RX], yv[RY];
+        static_assert(RX % 2 == 0, "pixel columns go in pairs");
+        float2 xv[RX / 2];
+        float yv[RY];
 #pragma unroll
-        for (int c = 0; c < RX; c++) xv[c] = colf[c] * gm.x;
+        for (int c = 0; c < RX / 2; c++) xv[c] = make_float2(fmulr(colf[2 * c], gm.x), fmulr(colf[2 * c + 1], gm.x));
 #pragma unroll
         for (int r = 0; r < RY; r++) yv[r] = fmaf(rowf[r], gm.y, gm.z);
         // address of pair 0 minus the 2^23 bit pattern (unsigned wrap-around)
         const unsigned base = smem_u32(smb + (size_t)(b * VC + vv) * NS * Cfg::WIN_BYTES) - (unsigned)ES * kMagicBits;
+        const float2 mag = make_float2(8388608.0f, 8388608.0f);
 #pragma unroll
         for (int r = 0; r < RY; r++)
 #pragma unroll
-            for (int c = 0; c < RX; c++) {
-                const float u = xv[c] + yv[r];                       // >= 1.9 inside the window
-                const float t = __fadd_rz(u, 8388608.0f);
-                const unsigned bits = __float_as_uint(t);
-                const float f = u - (t - 8388608.0f);
+            for (int c2 = 0; c2 < RX / 2; c2++) {
+                // two pixels per instruction: u, its floor as bits (the 2^23 add), the fraction
+                const float2 u2 = add2_rn(xv[c2], bcast2(yv[r]));        // >= 1.9 inside the window
+                const float2 t2 = add2_rz(u2, mag);
+                const float2 f2 = sub2_rn(u2, sub2_rn(t2, mag));
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c = 2 * c2 + h;
+                const unsigned bits = __float_as_uint(h ? t2.y : t2.x);
+                const float f = h ? f2.y : f2.x;
                 const unsigned a = base + (unsigned)ES * bits;
                 const unsigned short fb = MODE != RV_MODE_LIN ? half_bits<MODE>(f) : (unsigned short)0;
                 lin_slice<Cfg, MODE, 0>(acc[0][r][c], a, f, sc[0], fb);
                 if (NS > 1) lin_slice<Cfg, MODE, (NS > 1 ? 1 : 0)>(acc[1 % NS][r][c], a, f, sc[1 % NS], fb);
                 if (NS > 2) lin_slice<Cfg, MODE, (NS > 2 ? 2 : 0)>(acc[2 % NS][r][c], a, f, sc[2 % NS], fb);
                 if (NS > 3) lin_slice<Cfg, MODE, (NS > 3 ? 3 : 0)>(acc[3 % NS][r][c], a, f, sc[3 % NS], fb);
+            }
             }
     }
 }
